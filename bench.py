@@ -1,0 +1,378 @@
+#!/usr/bin/env python
+"""Benchmark of the D2Q9 hot path: fused stream + bounce-back/moving lid + collide.
+
+Workload (default): lid-driven cavity, 8192 x 8192 cells, FP32 populations,
+omega = 1.7, lid velocity 0.1, from rest at equilibrium.  One step = one
+fused pull-stream + collide pass over the whole lattice (one kernel launch).
+Metric: MLUPS (million lattice-cell updates per second, physical cells only).
+
+Lines printed (rank 0, one JSON line):
+  value      device-timed MLUPS, populations resident in HBM (CUDA events on
+             the launching stream, barrier + synchronize on both sides)
+  e2e        MLUPS through the public API with the populations in pinned host
+             memory: every step copies them host->device, runs the step, and
+             copies them back, inside the timed region
+  roofline   HBM roofline of the fused kernel: 72 B/cell/step (FP32) or
+             36 B (16-bit deviations) over its CUDA-event launch time
+  cpu_baseline  the oracle's C port of the reference step on the host cores
+
+``--impl reference`` times the CPU implementation of the reference step (the
+C port of the oracle; the reference's own C++ extension needs Eigen, which is
+not available) on all host cores, on the same workload.
+
+Multi-GPU (torchrun): replicas only -- every rank runs its own lattice; value
+= total cells updated by all ranks / max time over ranks.
+"""
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+METRIC = "MLUPS (D2Q9 BGK fused stream-collide, lid-driven cavity)"
+UNIT = "MLUPS"
+
+
+def parse(argv=None):
+    p = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=50)
+    p.add_argument("--warmup", type=int, default=5)
+    p.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    p.add_argument("--nx", type=int, default=8192)
+    p.add_argument("--ny", type=int, default=8192)
+    p.add_argument("--storage", choices=["f32", "f16dev", "bf16dev", "f64"], default="f32")
+    p.add_argument("--boundary", choices=["cavity", "periodic"], default="cavity")
+    p.add_argument("--omega", type=float, default=1.7)
+    p.add_argument("--u0", type=float, default=0.1)
+    p.add_argument("--e2e-steps", type=int, default=5)
+    p.add_argument("--cpu-seconds", type=float, default=10.0, help="bound of the CPU-baseline sample")
+    p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--no-e2e", action="store_true")
+    return p.parse_args(argv)
+
+
+# ---------------------------------------------------------------- distributed
+class Dist:
+    """Rank bookkeeping; N>1 runs replicas (no data-path collective)."""
+
+    def __init__(self, backend=None):
+        import torch.distributed as dist
+        self.world = int(os.environ.get("WORLD_SIZE", "1"))
+        self.rank = int(os.environ.get("RANK", "0"))
+        self.local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+        self.dist = dist if self.world > 1 else None
+        if self.dist is not None and not dist.is_initialized():
+            dist.init_process_group(backend=backend or "nccl")
+
+    def barrier(self):
+        if self.dist is not None:
+            self.dist.barrier()
+
+    def max(self, x, device=None):
+        if self.dist is None:
+            return float(x)
+        import torch
+        t = torch.tensor([float(x)], dtype=torch.float64, device=device)
+        self.dist.all_reduce(t, op=self.dist.ReduceOp.MAX)
+        return float(t.item())
+
+    def sum(self, x, device=None):
+        if self.dist is None:
+            return float(x)
+        import torch
+        t = torch.tensor([float(x)], dtype=torch.float64, device=device)
+        self.dist.all_reduce(t, op=self.dist.ReduceOp.SUM)
+        return float(t.item())
+
+    def close(self):
+        if self.dist is not None and self.dist.is_initialized():
+            self.dist.destroy_process_group()
+
+
+def aggregate_mlups(cells_per_rank, steps, seconds_per_rank, d, device=None):
+    """Whole-job MLUPS: all ranks' cell updates over the slowest rank's time."""
+    total = d.sum(cells_per_rank * steps, device)
+    t = d.max(seconds_per_rank, device)
+    return total / t / 1e6, t
+
+
+# ---------------------------------------------------------------- clocks
+class ClockSampler:
+    """nvidia-smi clock / throttle sampling during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        import tempfile
+        fd, self.path = tempfile.mkstemp(prefix="lbgb_clocks_", suffix=".csv")
+        os.close(fd)
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.FIELDS, "--format=csv,noheader,nounits",
+                 "-lms", "100"], stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        time.sleep(0.25)
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        rows = []
+        for line in open(self.path):
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                rows.append({"sm": float(parts[1]), "max": float(parts[2]), "power": float(parts[3]),
+                             "hw": parts[5], "hwt": parts[6], "swt": parts[7], "pcap": parts[8]})
+            except ValueError:
+                continue
+        os.remove(self.path)
+        if not rows:
+            return None
+        import statistics
+        reasons = set()
+        for r in rows:
+            for k, name in (("hw", "hw_slowdown"), ("hwt", "hw_thermal_slowdown"), ("swt", "sw_thermal_slowdown"),
+                            ("pcap", "sw_power_cap")):
+                if r[k].lower() == "active":
+                    reasons.add(name)
+        return {"sm_mhz": statistics.median(r["sm"] for r in rows), "sm_max_mhz": max(r["max"] for r in rows),
+                "power_w_max": max(r["power"] for r in rows), "samples": len(rows), "reasons": sorted(reasons)}
+
+
+# ---------------------------------------------------------------- peaks, profiles
+def hbm_peak():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as fh:
+            return float(json.load(fh)["hbm_gbs"]), "measured (MEASURED_PEAKS.json hbm_gbs, copy burst)"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "fallback"
+
+
+def profiled_traffic(storage, boundary, cells):
+    """DRAM bytes per launch of the fused kernel from the committed ncu summary,
+    scaled from the captured grid to ``cells`` (traffic is proportional to cells)."""
+    path = os.path.join(ROOT, "profiles", "k_step_traffic.json")
+    try:
+        with open(path) as fh:
+            rows = json.load(fh)
+    except (OSError, ValueError):
+        return None, None
+    for r in rows:
+        if r.get("storage") == storage and r.get("boundary") == boundary:
+            return r["dram_bytes_per_launch"] * cells / r["cells"], r
+    return None, None
+
+
+# ---------------------------------------------------------------- CPU baseline
+def _cpu_lattice(rows, ny, storage):
+    import numpy as np
+    from oracle import port
+    dt = np.float64 if storage == "f64" else np.float32
+    a = np.empty((9, rows, ny), dtype=dt)
+    z = np.zeros(rows * ny, dtype=dt)
+    port.equilibrium(np.ones(rows * ny, dtype=dt), z, z, a.reshape(9, -1), nthreads=0)
+    return a, np.empty_like(a)
+
+
+def cpu_port_sample(nx, ny, omega, u0, storage, boundary, budget_s):
+    """Time the oracle's C port of the reference step on all host cores.
+
+    The sample is whole-lattice steps for about ``budget_s`` seconds; if one
+    whole-lattice step takes more than a third of the budget, a strip of rows
+    is used instead.  Returns (MLUPS, cores, sample description).
+    """
+    from oracle import port
+    cores = port.max_threads()
+    rows = nx
+    while True:
+        a, b = _cpu_lattice(rows, ny, storage)
+        t0 = time.perf_counter()
+        port.run_raw(a, b, boundary, omega, u0, 1)
+        t1 = time.perf_counter() - t0
+        if t1 <= budget_s / 3 or rows <= 64:
+            break
+        rows = max(64, int(rows * (budget_s / 3) / t1))
+    steps = max(1, int(budget_s / max(t1, 1e-6)))
+    t0 = time.perf_counter()
+    port.run_raw(a, b, boundary, omega, u0, steps)
+    el = time.perf_counter() - t0
+    mlups = rows * ny * steps / el / 1e6
+    sample = "%d steps of a %d x %d %s lattice (%s), %.1f s on %d host threads; C port of the reference step " \
+             "(stream + bounce-back pass, then collide pass)" % (steps, rows, ny, boundary, storage, el, cores)
+    return mlups, cores, sample
+
+
+def run_reference(args):
+    d = Dist(backend="gloo")
+    if d.rank != 0:
+        d.close()
+        return 0
+    from oracle import port
+    nx, ny = args.nx, args.ny
+    cores = port.max_threads()
+    # bounded sample: the whole lattice if all steps fit about two minutes,
+    # else a strip of rows of it
+    rows = nx
+    a, b = _cpu_lattice(rows, ny, args.storage)
+    t0 = time.perf_counter()
+    port.run_raw(a, b, args.boundary, args.omega, args.u0, 1)
+    t1 = time.perf_counter() - t0
+    budget = 120.0
+    if t1 * (args.steps + args.warmup) > budget:
+        rows = max(64, int(nx * budget / (t1 * (args.steps + args.warmup))))
+        a, b = _cpu_lattice(rows, ny, args.storage)
+    if args.warmup > 1:
+        port.run_raw(a, b, args.boundary, args.omega, args.u0, args.warmup - 1)
+    t0 = time.perf_counter()
+    port.run_raw(a, b, args.boundary, args.omega, args.u0, args.steps)
+    el = time.perf_counter() - t0
+    mlups = rows * ny * args.steps / el / 1e6
+    sample = "each step: one %s step of a %d x %d strip of the %d x %d lattice (%s), C port of the reference " \
+             "step on %d host threads" % (args.boundary, rows, ny, nx, ny, args.storage, cores)
+    line = {
+        "impl": "reference", "metric": METRIC, "value": round(mlups, 3), "unit": UNIT, "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(el / args.steps * 1e3, 3),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f64" if args.storage == "f64" else "f32", "data": "synthetic (cavity from rest at equilibrium)",
+        "config": workload_config(args),
+        "cpu_baseline": {"value": round(mlups, 3), "unit": UNIT, "cores": cores, "kind": "port", "sample": sample},
+        "e2e": {"value": round(mlups, 3), "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    d.close()
+    return 0
+
+
+def workload_config(args):
+    kind = "lid-driven cavity" if args.boundary == "cavity" else "periodic"
+    return {"workload": "D2Q9 BGK %s %dx%d, %s populations, omega=%g%s" % (
+        kind, args.nx, args.ny, args.storage, args.omega, (", u_lid=%g" % args.u0) if args.boundary == "cavity" else ""),
+        "nx": args.nx, "ny": args.ny, "storage": args.storage, "boundary": args.boundary, "omega": args.omega,
+        "u_lid": args.u0 if args.boundary == "cavity" else None,
+        "l2": "inputs larger than L2 (each population buffer %.2f GB vs 129 MB L2); no flush" % (
+            9 * args.nx * args.ny * {"f32": 4, "f64": 8}.get(args.storage, 2) / 1e9),
+        "parallelism": "replicas (one lattice per GPU)"}
+
+
+# ---------------------------------------------------------------- our arm
+def run_ours(args):
+    import torch
+    d = Dist()
+    dev = torch.device("cuda", d.local_rank)
+    torch.cuda.set_device(dev)
+    import latticeboltzmann_gb300 as PyLB
+
+    lat = PyLB.Lattice(args.nx, args.ny, args.omega, boundary=args.boundary, u0=args.u0, storage=args.storage,
+                       device=dev)
+    stream = torch.cuda.current_stream(dev)
+    for _ in range(args.warmup):
+        lat.step(1)
+    torch.cuda.synchronize(dev)
+
+    clocks = ClockSampler(d.local_rank)
+    if d.rank == 0:
+        clocks.start()
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps + 1)]
+    d.barrier()
+    torch.cuda.synchronize(dev)
+    ev[0].record(stream)
+    for i in range(args.steps):
+        lat.step(1)
+        ev[i + 1].record(stream)
+    torch.cuda.synchronize(dev)
+    d.barrier()
+    clk = clocks.stop() if d.rank == 0 else None
+    per_launch_ms = [ev[i].elapsed_time(ev[i + 1]) for i in range(args.steps)]
+    total_s = ev[0].elapsed_time(ev[-1]) / 1e3
+    mlups, t_max = aggregate_mlups(lat.cells, args.steps, total_s, d, dev)
+
+    # end to end through the public API with host-resident populations
+    e2e = None
+    if not args.no_e2e:
+        host = torch.empty((9, args.nx, args.ny), dtype=lat.state.dtype if args.storage in ("f32", "f64")
+                           else torch.float32, pin_memory=True)
+        lat.populations(out=host)
+        torch.cuda.synchronize(dev)
+        for _ in range(2):
+            lat.load(host)
+            lat.step(1)
+            lat.populations(out=host)
+        torch.cuda.synchronize(dev)
+        d.barrier()
+        t0 = time.perf_counter()
+        for _ in range(args.e2e_steps):
+            lat.load(host)
+            lat.step(1)
+            lat.populations(out=host)
+        torch.cuda.synchronize(dev)
+        el = time.perf_counter() - t0
+        d.barrier()
+        e_mlups, _ = aggregate_mlups(lat.cells, args.e2e_steps, el, d, dev)
+        nbytes = host.numel() * host.element_size()
+        e2e = {"value": round(e_mlups, 3), "unit": UNIT, "h2d_bytes_per_step": nbytes, "d2h_bytes_per_step": nbytes,
+               "steps": args.e2e_steps, "path": "Lattice.load(pinned host) + Lattice.step + Lattice.populations(out=pinned host)"}
+        del host
+
+    if d.rank != 0:
+        d.close()
+        return 0
+
+    bpc = lat.bytes_per_cell_update
+    avg_launch_s = sum(per_launch_ms) / len(per_launch_ms) / 1e3
+    achieved = bpc * lat.cells / avg_launch_s / 1e9
+    peak, peak_src = hbm_peak()
+    traffic, prof = profiled_traffic(args.storage, args.boundary, lat.cells)
+    roofline = {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+                "frac": round(achieved / peak, 4), "traffic": None if traffic is None else round(traffic),
+                "algorithmic_bytes": bpc * lat.cells, "kernel": "k_step (fused pull stream + bounce-back/lid + BGK)",
+                "peak_source": peak_src,
+                "traffic_source": None if prof is None else prof.get("source")}
+    cpu = None
+    if not args.no_cpu_baseline:
+        c_mlups, cores, sample = cpu_port_sample(args.nx, args.ny, args.omega, args.u0, args.storage, args.boundary,
+                                                 args.cpu_seconds)
+        cpu = {"value": round(c_mlups, 3), "unit": UNIT, "cores": cores, "kind": "port", "sample": sample}
+    line = {
+        "metric": METRIC, "value": round(mlups, 1), "unit": UNIT, "n_gpus": d.world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": round(t_max / args.steps * 1e3, 4), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64" if args.storage == "f64" else "f32",
+        "data": "synthetic (cavity from rest at equilibrium)", "config": workload_config(args),
+        "e2e": e2e, "gpu_launches": args.steps, "roofline": roofline, "cpu_baseline": cpu, "clocks": clk,
+        "hbm_gbs": round(achieved, 1),
+    }
+    print(json.dumps(line), flush=True)
+    d.close()
+    return 0
+
+
+def main(argv=None):
+    args = parse(argv)
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_ours(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

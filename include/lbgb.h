@@ -1,0 +1,133 @@
+/*
+ * lbgb -- C ABI of the GB300 D2Q9 lattice-Boltzmann library (liblbgb.so).
+ *
+ * Every entry point takes plain device pointers, sizes and a CUDA stream
+ * (cudaStream_t passed as void*; NULL = legacy default stream), launches
+ * asynchronously on that stream and returns 0 on success or a negative
+ * LBGB_E* code.  Nothing here allocates device memory: the caller owns every
+ * buffer (arrays, workspaces).  A message for the last failure on the calling
+ * host thread is available from lbgb_last_error().
+ *
+ * Population layout: channel-major structure of arrays, f[i * chan_stride + c]
+ * with cell c = k * ny + l (k = x index, l = y index, l fastest), i.e. a
+ * C-contiguous (9, nx, ny) array -- the layout of the reference's f_ikl
+ * (simulators/parallel_lid_drive_cavity/cavity_opt1.py:74-82) and of the
+ * (9, N) view its native kernels take (c/d2q9.h:38-39).
+ * Channel order: 0, E(1,0), N(0,1), W(-1,0), S(0,-1), NE(1,1), NW(-1,1),
+ * SW(-1,-1), SE(1,-1)  (PyLB/Streaming.py:28-29).
+ *
+ * Storage codes (dtype): LBGB_F32 and LBGB_F64 store f itself;
+ * LBGB_F16DEV / LBGB_BF16DEV store the deviation h_i = f_i - w_i as IEEE half
+ * or bfloat16; all arithmetic on those is FP32.
+ */
+#ifndef LBGB_H
+#define LBGB_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#if defined(__GNUC__)
+#define LBGB_API __attribute__((visibility("default")))
+#else
+#define LBGB_API
+#endif
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define LBGB_F32 0
+#define LBGB_F64 1
+#define LBGB_F16DEV 2
+#define LBGB_BF16DEV 3
+
+#define LBGB_PERIODIC 0
+#define LBGB_CAVITY 1
+
+#define LBGB_OK 0
+#define LBGB_EINVAL (-1)   /* bad size, pointer or option */
+#define LBGB_EDTYPE (-2)   /* unsupported storage code */
+#define LBGB_ECUDA (-3)    /* a CUDA call or launch failed */
+#define LBGB_EWORKSPACE (-4) /* workspace missing or too small */
+#define LBGB_ETIMEOUT (-5) /* a bounded device-side wait gave up */
+
+/* Library version as MAJOR*10000 + MINOR*100 + PATCH. */
+LBGB_API int lbgb_version(void);
+
+/* Copies the message of the last failure on this host thread into buf
+ * (NUL-terminated, truncated to len) and returns its full length. */
+LBGB_API int lbgb_last_error(char *buf, size_t len);
+
+/* Equilibrium populations from density and velocity fields (n cells) into
+ * f (9 rows, channel stride chan_stride >= n).  dtype: LBGB_F32 or LBGB_F64
+ * (rho/ux/uy/f all of that type).
+ * Replaces: PyLB.Collision.equilibrium -> d2q9_equilibriumn<T>
+ *           (PyLB/Collision.py:21, c/d2q9.h:98-108, c/_lbkernels.cpp:38,45). */
+LBGB_API int lbgb_equilibrium(const void *rho, const void *ux, const void *uy, void *f,
+                     int64_t n, int64_t chan_stride, int dtype, void *stream);
+
+/* BGK collision in place on f (9 rows of n cells, channel stride chan_stride).
+ * Any storage code.
+ * Replaces: PyLB.Collision.collide -> d2q9_colliden<T>
+ *           (PyLB/Collision.py:21, c/d2q9.h:121-131, c/_lbkernels.cpp:40,47). */
+LBGB_API int lbgb_collide(void *f, int64_t n, int64_t chan_stride, int dtype,
+                 double omega, void *stream);
+
+/* Periodic streaming, pull form, out of place: dst_i(k,l) = src_i(k-cx_i, l-cy_i)
+ * with periodic wrap.  src and dst are (9, nx, ny) and must not overlap.
+ * Replaces: PyLB.Streaming.stream (PyLB/Streaming.py:33-46). */
+LBGB_API int lbgb_stream_periodic(const void *src, void *dst, int nx, int ny, int dtype,
+                         void *stream);
+
+/* Streaming with half-way bounce-back on the four walls and a lid at l = ny-1
+ * moving with velocity u0 in +x (Ladd correction), out of place; u0 = 0 gives
+ * plain bounce-back on all walls.  nx, ny >= 2.
+ * Replaces: stream_and_bounce_back(f_ikl, u0)
+ *   (simulators/parallel_lid_drive_cavity/cavity_opt1.py:177-245, identical in
+ *    cavity_opt0.py:155-223 and cavity_opt2.py:109-177). */
+LBGB_API int lbgb_stream_bounce_back(const void *src, void *dst, int nx, int ny,
+                            double u0, int dtype, void *stream);
+
+/* One fused time step: pull streaming (boundary = LBGB_PERIODIC or
+ * LBGB_CAVITY with lid velocity u0) followed by BGK collision, src -> dst.
+ * Any storage code.
+ * Replaces the per-step pair stream/stream_and_bounce_back + collide
+ *   (cavity_opt2.py:276-277, shear_wave_opt2.py:96-97, cavity_opt1.py:342-343). */
+LBGB_API int lbgb_step_fused(const void *src, void *dst, int nx, int ny, int boundary,
+                    double omega, double u0, int dtype, void *stream);
+
+/* nsteps fused steps ping-ponging between a and b (a holds the initial
+ * state); *which receives 0 if the result is in a, 1 if in b.  Launch-only:
+ * suitable for CUDA-graph capture. */
+LBGB_API int lbgb_run_fused(void *a, void *b, int nx, int ny, int boundary,
+                   double omega, double u0, int dtype, int nsteps, int *which,
+                   void *stream);
+
+/* Density and velocity of every cell (the diagnostics of cavity_opt2.py:280-281
+ * and cavity_opt1.py:154-156).  rho/ux/uy are float for the F32/F16DEV/BF16DEV
+ * storage codes and double for F64. */
+LBGB_API int lbgb_macroscopic(const void *f, void *rho, void *ux, void *uy, int64_t n,
+                     int64_t chan_stride, int dtype, void *stream);
+
+/* Bytes of device workspace lbgb_mass_momentum needs (fixed, small). */
+LBGB_API size_t lbgb_mass_momentum_workspace_bytes(void);
+
+/* Total mass and momentum, sum_c sum_i f_i(c) * (1, cx_i, cy_i), accumulated in
+ * FP64 with a fixed reduction order (bit-reproducible run to run).  out_dev
+ * receives 3 doubles in device memory.  workspace: device buffer of at least
+ * lbgb_mass_momentum_workspace_bytes() bytes, 8-byte aligned.
+ * Replaces the host-side np.sum(f_ikl) mass checks of the reference drivers. */
+LBGB_API int lbgb_mass_momentum(const void *f, int64_t n, int64_t chan_stride, int dtype,
+                       double *out_dev, void *workspace, size_t workspace_bytes,
+                       void *stream);
+
+/* Converts populations between storage codes (n cells, channel strides
+ * src_stride / dst_stride): e.g. F32 -> F16DEV stores f_i - w_i in half. */
+LBGB_API int lbgb_convert(const void *src, int src_dtype, int64_t src_stride, void *dst,
+                 int dst_dtype, int64_t dst_stride, int64_t n, void *stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* LBGB_H */

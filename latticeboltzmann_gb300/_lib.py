@@ -1,0 +1,103 @@
+"""ctypes binding of liblbgb.so (the C ABI declared in include/lbgb.h).
+
+The library is loaded on first use.  There is no fallback: if it has not been
+built, every operator raises ``LBGBUnavailable``.
+"""
+
+import ctypes
+import os
+import threading
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "liblbgb.so")
+
+# storage codes
+F32, F64, F16DEV, BF16DEV = 0, 1, 2, 3
+# boundary codes
+PERIODIC, CAVITY = 0, 1
+# return codes
+OK, EINVAL, EDTYPE, ECUDA, EWORKSPACE, ETIMEOUT = 0, -1, -2, -3, -4, -5
+
+STORAGE_CODES = {"f32": F32, "f64": F64, "f16dev": F16DEV, "bf16dev": BF16DEV}
+BOUNDARY_CODES = {"periodic": PERIODIC, "cavity": CAVITY}
+
+
+class LBGBError(RuntimeError):
+    """A CUDA-side failure reported by liblbgb."""
+
+
+class LBGBTimeout(LBGBError):
+    """A bounded device-side wait of liblbgb gave up."""
+
+
+class LBGBUnavailable(RuntimeError):
+    """liblbgb.so is not built or cannot be loaded."""
+
+
+_lock = threading.Lock()
+_lib = None
+
+_P, _I, _I64, _D, _SZ = ctypes.c_void_p, ctypes.c_int, ctypes.c_int64, ctypes.c_double, ctypes.c_size_t
+
+# name -> (restype, argtypes); must match include/lbgb.h
+SIGNATURES = {
+    "lbgb_version": (_I, []),
+    "lbgb_last_error": (_I, [ctypes.c_char_p, _SZ]),
+    "lbgb_equilibrium": (_I, [_P, _P, _P, _P, _I64, _I64, _I, _P]),
+    "lbgb_collide": (_I, [_P, _I64, _I64, _I, _D, _P]),
+    "lbgb_stream_periodic": (_I, [_P, _P, _I, _I, _I, _P]),
+    "lbgb_stream_bounce_back": (_I, [_P, _P, _I, _I, _D, _I, _P]),
+    "lbgb_step_fused": (_I, [_P, _P, _I, _I, _I, _D, _D, _I, _P]),
+    "lbgb_run_fused": (_I, [_P, _P, _I, _I, _I, _D, _D, _I, _I, ctypes.POINTER(_I), _P]),
+    "lbgb_macroscopic": (_I, [_P, _P, _P, _P, _I64, _I64, _I, _P]),
+    "lbgb_mass_momentum_workspace_bytes": (_SZ, []),
+    "lbgb_mass_momentum": (_I, [_P, _I64, _I64, _I, _P, _P, _SZ, _P]),
+    "lbgb_convert": (_I, [_P, _I, _I64, _P, _I, _I64, _I64, _P]),
+}
+
+
+def load(path=LIB_PATH):
+    """Load (once) and return the ctypes handle of liblbgb.so."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    with _lock:
+        if _lib is None:
+            if not os.path.exists(path):
+                raise LBGBUnavailable(
+                    "liblbgb.so is not built (%s); run `python -c \"import __graft_entry__ as g; g.build()\"` "
+                    "or `python -m latticeboltzmann_gb300._build`" % path)
+            try:
+                handle = ctypes.CDLL(path)
+            except OSError as e:
+                raise LBGBUnavailable("cannot load %s: %s" % (path, e)) from e
+            for name, (res, args) in SIGNATURES.items():
+                fn = getattr(handle, name)
+                fn.restype = res
+                fn.argtypes = args
+            _lib = handle
+    return _lib
+
+
+def last_error():
+    buf = ctypes.create_string_buffer(512)
+    load().lbgb_last_error(buf, len(buf))
+    return buf.value.decode(errors="replace")
+
+
+def check(rc, what=""):
+    """Translate a liblbgb return code into the matching Python exception."""
+    if rc == OK:
+        return
+    msg = last_error() or what
+    if rc == EINVAL:
+        raise ValueError(msg)
+    if rc == EDTYPE:
+        raise TypeError(msg)
+    if rc == ETIMEOUT:
+        raise LBGBTimeout(msg)
+    raise LBGBError("%s (code %d)" % (msg, rc))
+
+
+def call(name, *args):
+    check(getattr(load(), name)(*args), name)

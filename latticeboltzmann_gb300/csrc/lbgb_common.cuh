@@ -1,0 +1,201 @@
+// Shared device code of liblbgb: D2Q9 constants, population storage codecs,
+// vector memory access and the BGK collision of one node.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <cuda_fp16.h>
+#include <cuda_bf16.h>
+#include <stdint.h>
+#include <string.h>
+
+#include "lbgb.h"
+
+namespace lbgb {
+
+// ---------------------------------------------------------------- lattice
+// Channel order 0, E, N, W, S, NE, NW, SW, SE (PyLB/Streaming.py:28-29).
+enum { C0 = 0, CE = 1, CN = 2, CW = 3, CS = 4, CNE = 5, CNW = 6, CSW = 7, CSE = 8 };
+
+__host__ __device__ constexpr int cx(int i) {
+    return (i == CE || i == CNE || i == CSE) ? 1 : (i == CW || i == CNW || i == CSW) ? -1 : 0;
+}
+__host__ __device__ constexpr int cy(int i) {
+    return (i == CN || i == CNE || i == CNW) ? 1 : (i == CS || i == CSW || i == CSE) ? -1 : 0;
+}
+__host__ __device__ constexpr int opp(int i) {
+    return i == 0 ? 0 : (i <= 4 ? (i + 1) % 4 + 1 : (i - 3) % 4 + 5);
+}
+// Lattice weights 4/9, 1/9, 1/36 (cavity_opt1.py:92-96).  Opposite channels
+// share a weight, which the bounce-back decode below relies on.
+template <class R>
+__host__ __device__ constexpr R wgt(int i) {
+    return i == 0 ? R(4.0 / 9.0) : (i <= 4 ? R(1.0 / 9.0) : R(1.0 / 36.0));
+}
+
+// ---------------------------------------------------------------- storage
+// raw = element type in HBM, real = arithmetic type.  The deviation codecs
+// store h_i = f_i - w_i as 16-bit bits (IEEE half or bfloat16).
+template <int DT> struct Codec;
+
+template <> struct Codec<LBGB_F32> {
+    using raw = float;
+    using real = float;
+    static __device__ __forceinline__ real dec(raw x, int) { return x; }
+    static __device__ __forceinline__ raw enc(real x, int) { return x; }
+};
+template <> struct Codec<LBGB_F64> {
+    using raw = double;
+    using real = double;
+    static __device__ __forceinline__ real dec(raw x, int) { return x; }
+    static __device__ __forceinline__ raw enc(real x, int) { return x; }
+};
+template <> struct Codec<LBGB_F16DEV> {
+    using raw = unsigned short;
+    using real = float;
+    static __device__ __forceinline__ real dec(raw x, int i) {
+        return __half2float(__ushort_as_half(x)) + wgt<float>(i);
+    }
+    static __device__ __forceinline__ raw enc(real x, int i) {
+        return __half_as_ushort(__float2half_rn(x - wgt<float>(i)));
+    }
+};
+template <> struct Codec<LBGB_BF16DEV> {
+    using raw = unsigned short;
+    using real = float;
+    static __device__ __forceinline__ real dec(raw x, int i) {
+        return __bfloat162float(__ushort_as_bfloat16(x)) + wgt<float>(i);
+    }
+    static __device__ __forceinline__ raw enc(real x, int i) {
+        return __bfloat16_as_ushort(__float2bfloat16_rn(x - wgt<float>(i)));
+    }
+};
+
+// ---------------------------------------------------------------- memory
+// A vector of V raw elements moved as one 2/4/8/16-byte access.
+template <int BYTES> struct VecBits;
+template <> struct VecBits<16> { using t = uint4; };
+template <> struct VecBits<8> { using t = uint2; };
+template <> struct VecBits<4> { using t = unsigned int; };
+template <> struct VecBits<2> { using t = unsigned short; };
+
+// Read-only, non-coherent load (src is never written by the same launch).
+template <class RAW, int V>
+__device__ __forceinline__ void ldv(const RAW *p, RAW (&o)[V]) {
+    using T = typename VecBits<V * sizeof(RAW)>::t;
+    T x = __ldg(reinterpret_cast<const T *>(p));
+    memcpy(o, &x, sizeof(T));
+}
+
+template <class RAW>
+__device__ __forceinline__ RAW ld1(const RAW *p) {
+    RAW o[1];
+    ldv<RAW, 1>(p, o);
+    return o[0];
+}
+
+// Streaming store: the written populations are not re-read by this launch.
+__device__ __forceinline__ void st_cs(uint4 *p, uint4 v) {
+    asm volatile("st.global.cs.v4.u32 [%0], {%1, %2, %3, %4};" ::"l"(p), "r"(v.x), "r"(v.y),
+                 "r"(v.z), "r"(v.w) : "memory");
+}
+__device__ __forceinline__ void st_cs(uint2 *p, uint2 v) {
+    asm volatile("st.global.cs.v2.u32 [%0], {%1, %2};" ::"l"(p), "r"(v.x), "r"(v.y) : "memory");
+}
+__device__ __forceinline__ void st_cs(unsigned int *p, unsigned int v) {
+    asm volatile("st.global.cs.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+__device__ __forceinline__ void st_cs(unsigned short *p, unsigned short v) {
+    asm volatile("st.global.cs.u16 [%0], %1;" ::"l"(p), "h"(v) : "memory");
+}
+
+template <class RAW, int V>
+__device__ __forceinline__ void stv(RAW *p, const RAW (&v)[V]) {
+    using T = typename VecBits<V * sizeof(RAW)>::t;
+    T x;
+    memcpy(&x, v, sizeof(T));
+    st_cs(reinterpret_cast<T *>(p), x);
+}
+
+// ---------------------------------------------------------------- collision
+// BGK relaxation of one node towards the D2Q9 equilibrium
+//   f_i += omega (w_i rho (1 + 3 c.u + 9/2 (c.u)^2 - 3/2 u^2) - f_i),
+// in the formulation of c/d2q9.h:59-81,121-131: rho = sum f, u = sum c f / rho,
+// ux, uy scaled by 3, uu = (ux^2 + uy^2)/6, feq_i = w_i rho (1 + cu + cu^2/2 - uu).
+template <class R>
+__device__ __forceinline__ void bgk_collide(R (&f)[9], R omega, R &rho_out, R &ux_out, R &uy_out) {
+    R rho = f[0];
+#pragma unroll
+    for (int i = 1; i < 9; ++i) rho += f[i];
+    const R inv = R(1) / rho;
+    R ux = (f[1] - f[3] + f[5] - f[6] - f[7] + f[8]) * inv;
+    R uy = (f[2] - f[4] + f[5] + f[6] - f[7] - f[8]) * inv;
+    ux_out = ux;
+    uy_out = uy;
+    rho_out = rho;
+    const R w0 = rho * R(4.0 / 9.0), w1 = rho * R(1.0 / 9.0), w5 = rho * R(1.0 / 36.0);
+    ux *= R(3);
+    uy *= R(3);
+    const R uu = (ux * ux + uy * uy) * R(1.0 / 6.0);
+    const R base = R(1) - uu;
+    const R cu5 = ux + uy, cu6 = uy - ux;
+    const R hx = R(0.5) * ux * ux, hy = R(0.5) * uy * uy;
+    const R h5 = R(0.5) * cu5 * cu5, h6 = R(0.5) * cu6 * cu6;
+    R feq[9];
+    feq[0] = w0 * base;
+    feq[1] = w1 * (base + ux + hx);
+    feq[2] = w1 * (base + uy + hy);
+    feq[3] = w1 * (base - ux + hx);
+    feq[4] = w1 * (base - uy + hy);
+    feq[5] = w5 * (base + cu5 + h5);
+    feq[6] = w5 * (base + cu6 + h6);
+    feq[7] = w5 * (base - cu5 + h5);
+    feq[8] = w5 * (base - cu6 + h6);
+#pragma unroll
+    for (int i = 0; i < 9; ++i) f[i] += omega * (feq[i] - f[i]);
+}
+
+template <class R>
+__device__ __forceinline__ void bgk_collide(R (&f)[9], R omega) {
+    R a, b, c;
+    bgk_collide(f, omega, a, b, c);
+}
+
+// Equilibrium of one node (same formulation as above).
+template <class R>
+__device__ __forceinline__ void equilibrium1(R rho, R ux, R uy, R (&feq)[9]) {
+    const R w0 = rho * R(4.0 / 9.0), w1 = rho * R(1.0 / 9.0), w5 = rho * R(1.0 / 36.0);
+    ux *= R(3);
+    uy *= R(3);
+    const R uu = (ux * ux + uy * uy) * R(1.0 / 6.0);
+    const R base = R(1) - uu;
+    const R cu5 = ux + uy, cu6 = uy - ux;
+    const R hx = R(0.5) * ux * ux, hy = R(0.5) * uy * uy;
+    const R h5 = R(0.5) * cu5 * cu5, h6 = R(0.5) * cu6 * cu6;
+    feq[0] = w0 * base;
+    feq[1] = w1 * (base + ux + hx);
+    feq[2] = w1 * (base + uy + hy);
+    feq[3] = w1 * (base - ux + hx);
+    feq[4] = w1 * (base - uy + hy);
+    feq[5] = w5 * (base + cu5 + h5);
+    feq[6] = w5 * (base + cu6 + h6);
+    feq[7] = w5 * (base - cu5 + h5);
+    feq[8] = w5 * (base - cu6 + h6);
+}
+
+// ---------------------------------------------------------------- host side
+void set_error(const char *fmt, ...);
+int check_launch(const char *what);
+
+inline bool aligned(const void *p, size_t a) { return (reinterpret_cast<uintptr_t>(p) % a) == 0; }
+
+inline size_t raw_size(int dt) {
+    switch (dt) {
+    case LBGB_F32: return 4;
+    case LBGB_F64: return 8;
+    case LBGB_F16DEV:
+    case LBGB_BF16DEV: return 2;
+    default: return 0;
+    }
+}
+
+}  // namespace lbgb

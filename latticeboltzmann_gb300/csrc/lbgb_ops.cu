@@ -1,0 +1,385 @@
+// Node-local operators of liblbgb (equilibrium, collision, macroscopic fields,
+// storage conversion), the deterministic mass/momentum reduction, and the
+// library's error state.
+#include <stdarg.h>
+#include <stdio.h>
+
+#include "lbgb_common.cuh"
+
+namespace lbgb {
+
+// ---------------------------------------------------------------- errors
+static thread_local char g_err[512] = "";
+
+void set_error(const char *fmt, ...) {
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(g_err, sizeof(g_err), fmt, ap);
+    va_end(ap);
+}
+
+int check_launch(const char *what) {
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) {
+        set_error("%s: %s", what, cudaGetErrorString(e));
+        return LBGB_ECUDA;
+    }
+    return LBGB_OK;
+}
+
+static int grid_for(int64_t items, int threads) {
+    int64_t b = (items + threads - 1) / threads;
+    if (b > (1 << 20)) b = 1 << 20;  // grid-stride beyond this
+    return (int)(b < 1 ? 1 : b);
+}
+
+// ---------------------------------------------------------------- equilibrium
+template <class T>
+__global__ void k_equilibrium(const T *__restrict__ rho, const T *__restrict__ ux, const T *__restrict__ uy,
+                              T *__restrict__ f, int64_t n, int64_t cs) {
+    for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < n; c += (int64_t)gridDim.x * blockDim.x) {
+        T feq[9];
+        equilibrium1<T>(rho[c], ux[c], uy[c], feq);
+#pragma unroll
+        for (int i = 0; i < 9; ++i) f[i * cs + c] = feq[i];
+    }
+}
+
+// ---------------------------------------------------------------- collide
+// One thread relaxes V consecutive cells; vector access when the channel
+// stride and the pointer allow it, else element by element.
+template <int DT, int V>
+__global__ void k_collide(typename Codec<DT>::raw *__restrict__ f, int64_t n, int64_t cs,
+                          typename Codec<DT>::real omega) {
+    using C = Codec<DT>;
+    using raw = typename C::raw;
+    using real = typename C::real;
+    const int64_t groups = (n + V - 1) / V;
+    for (int64_t g = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; g < groups;
+         g += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t c0 = g * V;
+        const int cnt = (int)((n - c0) < V ? (n - c0) : V);
+        real v[9][V];
+        if (cnt == V) {
+#pragma unroll
+            for (int i = 0; i < 9; ++i) {
+                raw r[V];
+                ldv<raw, V>(f + i * cs + c0, r);
+#pragma unroll
+                for (int j = 0; j < V; ++j) v[i][j] = C::dec(r[j], i);
+            }
+        } else {
+#pragma unroll
+            for (int i = 0; i < 9; ++i)
+#pragma unroll
+                for (int j = 0; j < V; ++j) v[i][j] = j < cnt ? C::dec(f[i * cs + c0 + j], i) : real(1.0 / 9.0);
+        }
+#pragma unroll
+        for (int j = 0; j < V; ++j) {
+            real x[9];
+#pragma unroll
+            for (int i = 0; i < 9; ++i) x[i] = v[i][j];
+            bgk_collide(x, omega);
+#pragma unroll
+            for (int i = 0; i < 9; ++i) v[i][j] = x[i];
+        }
+        if (cnt == V) {
+#pragma unroll
+            for (int i = 0; i < 9; ++i) {
+                raw r[V];
+#pragma unroll
+                for (int j = 0; j < V; ++j) r[j] = C::enc(v[i][j], i);
+                stv<raw, V>(f + i * cs + c0, r);
+            }
+        } else {
+            for (int i = 0; i < 9; ++i)
+                for (int j = 0; j < cnt; ++j) f[i * cs + c0 + j] = C::enc(v[i][j], i);
+        }
+    }
+}
+
+template <int DT>
+static int launch_collide(void *f, int64_t n, int64_t cs, double omega, cudaStream_t s) {
+    using C = Codec<DT>;
+    constexpr int VW = 16 / sizeof(typename C::raw);
+    if (cs % VW == 0 && aligned(f, 16)) {
+        k_collide<DT, VW><<<grid_for((n + VW - 1) / VW, 256), 256, 0, s>>>(static_cast<typename C::raw *>(f), n,
+                                                                          cs, (typename C::real)omega);
+    } else {
+        k_collide<DT, 1><<<grid_for(n, 256), 256, 0, s>>>(static_cast<typename C::raw *>(f), n, cs,
+                                                          (typename C::real)omega);
+    }
+    return check_launch("k_collide");
+}
+
+// ---------------------------------------------------------------- macroscopic
+template <int DT>
+__global__ void k_macroscopic(const typename Codec<DT>::raw *__restrict__ f, typename Codec<DT>::real *rho,
+                              typename Codec<DT>::real *ux, typename Codec<DT>::real *uy, int64_t n, int64_t cs) {
+    using C = Codec<DT>;
+    using real = typename C::real;
+    for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < n; c += (int64_t)gridDim.x * blockDim.x) {
+        real v[9];
+#pragma unroll
+        for (int i = 0; i < 9; ++i) v[i] = C::dec(f[i * cs + c], i);
+        real r = v[0];
+#pragma unroll
+        for (int i = 1; i < 9; ++i) r += v[i];
+        // same expressions as the reference's diagnostics (cavity_opt1.py:154-156)
+        const real jx = v[1] - v[3] + v[5] - v[6] - v[7] + v[8];
+        const real jy = v[2] - v[4] + v[5] + v[6] - v[7] - v[8];
+        if (rho) rho[c] = r;
+        if (ux) ux[c] = jx / r;
+        if (uy) uy[c] = jy / r;
+    }
+}
+
+// ---------------------------------------------------------------- convert
+template <int SD, int DD>
+__global__ void k_convert(const typename Codec<SD>::raw *__restrict__ src, int64_t ss,
+                          typename Codec<DD>::raw *__restrict__ dst, int64_t ds, int64_t n) {
+    for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < n; c += (int64_t)gridDim.x * blockDim.x) {
+#pragma unroll
+        for (int i = 0; i < 9; ++i) {
+            const double x = (double)Codec<SD>::dec(src[i * ss + c], i);
+            dst[i * ds + c] = Codec<DD>::enc((typename Codec<DD>::real)x, i);
+        }
+    }
+}
+
+template <int SD>
+static int launch_convert_to(const void *src, int64_t ss, void *dst, int dd, int64_t ds, int64_t n, cudaStream_t s) {
+    const int g = grid_for(n, 256);
+    const auto *a = static_cast<const typename Codec<SD>::raw *>(src);
+    switch (dd) {
+    case LBGB_F32: k_convert<SD, LBGB_F32><<<g, 256, 0, s>>>(a, ss, static_cast<float *>(dst), ds, n); break;
+    case LBGB_F64: k_convert<SD, LBGB_F64><<<g, 256, 0, s>>>(a, ss, static_cast<double *>(dst), ds, n); break;
+    case LBGB_F16DEV:
+        k_convert<SD, LBGB_F16DEV><<<g, 256, 0, s>>>(a, ss, static_cast<unsigned short *>(dst), ds, n);
+        break;
+    case LBGB_BF16DEV:
+        k_convert<SD, LBGB_BF16DEV><<<g, 256, 0, s>>>(a, ss, static_cast<unsigned short *>(dst), ds, n);
+        break;
+    default: set_error("lbgb_convert: unsupported destination storage code %d", dd); return LBGB_EDTYPE;
+    }
+    return check_launch("k_convert");
+}
+
+// ---------------------------------------------------------------- mass/momentum
+// Two passes with a fixed grid: pass 1 writes one (mass, px, py) partial per
+// block into the workspace, pass 2 sums the partials in block order.  The
+// grid size does not depend on the device, so the sum is reproducible.
+constexpr int RED_BLOCKS = 1024;
+constexpr int RED_THREADS = 256;
+
+template <int DT>
+__global__ void __launch_bounds__(RED_THREADS)
+k_mass_momentum_partial(const typename Codec<DT>::raw *__restrict__ f, int64_t n, int64_t cs, double *partial) {
+    using C = Codec<DT>;
+    double m = 0.0, px = 0.0, py = 0.0;
+    for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < n; c += (int64_t)gridDim.x * blockDim.x) {
+        double v[9];
+#pragma unroll
+        for (int i = 0; i < 9; ++i) v[i] = (double)C::dec(f[i * cs + c], i);
+        double r = v[0];
+#pragma unroll
+        for (int i = 1; i < 9; ++i) r += v[i];
+        m += r;
+        px += v[1] - v[3] + v[5] - v[6] - v[7] + v[8];
+        py += v[2] - v[4] + v[5] + v[6] - v[7] - v[8];
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        m += __shfl_down_sync(0xffffffffu, m, o);
+        px += __shfl_down_sync(0xffffffffu, px, o);
+        py += __shfl_down_sync(0xffffffffu, py, o);
+    }
+    __shared__ double sm[3][RED_THREADS / 32];
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    if (lane == 0) {
+        sm[0][w] = m;
+        sm[1][w] = px;
+        sm[2][w] = py;
+    }
+    __syncthreads();
+    if (threadIdx.x < 3) {
+        double acc = 0.0;
+        for (int i = 0; i < RED_THREADS / 32; ++i) acc += sm[threadIdx.x][i];
+        partial[blockIdx.x * 3 + threadIdx.x] = acc;
+    }
+}
+
+__global__ void __launch_bounds__(RED_THREADS) k_sum_partials(const double *partial, int nblocks, double *out) {
+    // thread t sums partials t, t+256, ... then a fixed-order tree
+    __shared__ double sm[3][RED_THREADS];
+    for (int q = 0; q < 3; ++q) {
+        double acc = 0.0;
+        for (int b = threadIdx.x; b < nblocks; b += RED_THREADS) acc += partial[b * 3 + q];
+        sm[q][threadIdx.x] = acc;
+    }
+    __syncthreads();
+    for (int s = RED_THREADS / 2; s > 0; s >>= 1) {
+        if (threadIdx.x < s)
+            for (int q = 0; q < 3; ++q) sm[q][threadIdx.x] += sm[q][threadIdx.x + s];
+        __syncthreads();
+    }
+    if (threadIdx.x < 3) out[threadIdx.x] = sm[threadIdx.x][0];
+}
+
+static int check_cells(const void *f, int64_t n, int64_t cs, int dtype, const char *what) {
+    if (raw_size(dtype) == 0) {
+        set_error("%s: unsupported storage code %d", what, dtype);
+        return LBGB_EDTYPE;
+    }
+    if (n < 0 || cs < n) {
+        set_error("%s: need 0 <= n <= chan_stride (n=%lld, chan_stride=%lld)", what, (long long)n, (long long)cs);
+        return LBGB_EINVAL;
+    }
+    if (n > 0 && !f) {
+        set_error("%s: null population pointer", what);
+        return LBGB_EINVAL;
+    }
+    if (!aligned(f, raw_size(dtype))) {
+        set_error("%s: population pointer must be aligned to the element size", what);
+        return LBGB_EINVAL;
+    }
+    return LBGB_OK;
+}
+
+}  // namespace lbgb
+
+using namespace lbgb;
+
+extern "C" int lbgb_version(void) { return 1 * 10000 + 0 * 100 + 0; }
+
+extern "C" int lbgb_last_error(char *buf, size_t len) {
+    const size_t n = strlen(g_err);
+    if (buf && len) {
+        const size_t m = n < len - 1 ? n : len - 1;
+        memcpy(buf, g_err, m);
+        buf[m] = 0;
+    }
+    return (int)n;
+}
+
+extern "C" int lbgb_equilibrium(const void *rho, const void *ux, const void *uy, void *f, int64_t n,
+                                int64_t chan_stride, int dtype, void *stream) {
+    int rc = check_cells(f, n, chan_stride, dtype, "lbgb_equilibrium");
+    if (rc) return rc;
+    if (n == 0) return LBGB_OK;
+    if (!rho || !ux || !uy) {
+        set_error("lbgb_equilibrium: null field pointer");
+        return LBGB_EINVAL;
+    }
+    cudaStream_t s = (cudaStream_t)stream;
+    if (dtype == LBGB_F32) {
+        k_equilibrium<float><<<grid_for(n, 256), 256, 0, s>>>((const float *)rho, (const float *)ux,
+                                                              (const float *)uy, (float *)f, n, chan_stride);
+    } else if (dtype == LBGB_F64) {
+        k_equilibrium<double><<<grid_for(n, 256), 256, 0, s>>>((const double *)rho, (const double *)ux,
+                                                               (const double *)uy, (double *)f, n, chan_stride);
+    } else {
+        set_error("lbgb_equilibrium: storage code %d not supported (F32 or F64)", dtype);
+        return LBGB_EDTYPE;
+    }
+    return check_launch("k_equilibrium");
+}
+
+extern "C" int lbgb_collide(void *f, int64_t n, int64_t chan_stride, int dtype, double omega, void *stream) {
+    int rc = check_cells(f, n, chan_stride, dtype, "lbgb_collide");
+    if (rc) return rc;
+    if (n == 0) return LBGB_OK;
+    cudaStream_t s = (cudaStream_t)stream;
+    switch (dtype) {
+    case LBGB_F32: return launch_collide<LBGB_F32>(f, n, chan_stride, omega, s);
+    case LBGB_F64: return launch_collide<LBGB_F64>(f, n, chan_stride, omega, s);
+    case LBGB_F16DEV: return launch_collide<LBGB_F16DEV>(f, n, chan_stride, omega, s);
+    case LBGB_BF16DEV: return launch_collide<LBGB_BF16DEV>(f, n, chan_stride, omega, s);
+    }
+    return LBGB_EDTYPE;
+}
+
+extern "C" int lbgb_macroscopic(const void *f, void *rho, void *ux, void *uy, int64_t n, int64_t chan_stride,
+                                int dtype, void *stream) {
+    int rc = check_cells(f, n, chan_stride, dtype, "lbgb_macroscopic");
+    if (rc) return rc;
+    if (n == 0) return LBGB_OK;
+    cudaStream_t s = (cudaStream_t)stream;
+    const int g = grid_for(n, 256);
+    switch (dtype) {
+    case LBGB_F32:
+        k_macroscopic<LBGB_F32><<<g, 256, 0, s>>>((const float *)f, (float *)rho, (float *)ux, (float *)uy, n,
+                                                  chan_stride);
+        break;
+    case LBGB_F64:
+        k_macroscopic<LBGB_F64><<<g, 256, 0, s>>>((const double *)f, (double *)rho, (double *)ux, (double *)uy, n,
+                                                  chan_stride);
+        break;
+    case LBGB_F16DEV:
+        k_macroscopic<LBGB_F16DEV><<<g, 256, 0, s>>>((const unsigned short *)f, (float *)rho, (float *)ux,
+                                                     (float *)uy, n, chan_stride);
+        break;
+    case LBGB_BF16DEV:
+        k_macroscopic<LBGB_BF16DEV><<<g, 256, 0, s>>>((const unsigned short *)f, (float *)rho, (float *)ux,
+                                                      (float *)uy, n, chan_stride);
+        break;
+    }
+    return check_launch("k_macroscopic");
+}
+
+extern "C" size_t lbgb_mass_momentum_workspace_bytes(void) { return (size_t)RED_BLOCKS * 3 * sizeof(double); }
+
+extern "C" int lbgb_mass_momentum(const void *f, int64_t n, int64_t chan_stride, int dtype, double *out_dev,
+                                  void *workspace, size_t workspace_bytes, void *stream) {
+    int rc = check_cells(f, n, chan_stride, dtype, "lbgb_mass_momentum");
+    if (rc) return rc;
+    if (!out_dev) {
+        set_error("lbgb_mass_momentum: null output pointer");
+        return LBGB_EINVAL;
+    }
+    if (!workspace || workspace_bytes < lbgb_mass_momentum_workspace_bytes() || !aligned(workspace, 8)) {
+        set_error("lbgb_mass_momentum: workspace needs %zu bytes, 8-byte aligned (got %zu)",
+                  lbgb_mass_momentum_workspace_bytes(), workspace_bytes);
+        return LBGB_EWORKSPACE;
+    }
+    cudaStream_t s = (cudaStream_t)stream;
+    double *partial = static_cast<double *>(workspace);
+    switch (dtype) {
+    case LBGB_F32:
+        k_mass_momentum_partial<LBGB_F32><<<RED_BLOCKS, RED_THREADS, 0, s>>>((const float *)f, n, chan_stride, partial);
+        break;
+    case LBGB_F64:
+        k_mass_momentum_partial<LBGB_F64><<<RED_BLOCKS, RED_THREADS, 0, s>>>((const double *)f, n, chan_stride,
+                                                                             partial);
+        break;
+    case LBGB_F16DEV:
+        k_mass_momentum_partial<LBGB_F16DEV><<<RED_BLOCKS, RED_THREADS, 0, s>>>((const unsigned short *)f, n,
+                                                                                chan_stride, partial);
+        break;
+    case LBGB_BF16DEV:
+        k_mass_momentum_partial<LBGB_BF16DEV><<<RED_BLOCKS, RED_THREADS, 0, s>>>((const unsigned short *)f, n,
+                                                                                 chan_stride, partial);
+        break;
+    }
+    rc = check_launch("k_mass_momentum_partial");
+    if (rc) return rc;
+    k_sum_partials<<<1, RED_THREADS, 0, s>>>(partial, RED_BLOCKS, out_dev);
+    return check_launch("k_sum_partials");
+}
+
+extern "C" int lbgb_convert(const void *src, int src_dtype, int64_t src_stride, void *dst, int dst_dtype,
+                            int64_t dst_stride, int64_t n, void *stream) {
+    int rc = check_cells(src, n, src_stride, src_dtype, "lbgb_convert");
+    if (rc) return rc;
+    rc = check_cells(dst, n, dst_stride, dst_dtype, "lbgb_convert");
+    if (rc) return rc;
+    if (n == 0) return LBGB_OK;
+    cudaStream_t s = (cudaStream_t)stream;
+    switch (src_dtype) {
+    case LBGB_F32: return launch_convert_to<LBGB_F32>(src, src_stride, dst, dst_dtype, dst_stride, n, s);
+    case LBGB_F64: return launch_convert_to<LBGB_F64>(src, src_stride, dst, dst_dtype, dst_stride, n, s);
+    case LBGB_F16DEV: return launch_convert_to<LBGB_F16DEV>(src, src_stride, dst, dst_dtype, dst_stride, n, s);
+    case LBGB_BF16DEV: return launch_convert_to<LBGB_BF16DEV>(src, src_stride, dst, dst_dtype, dst_stride, n, s);
+    }
+    return LBGB_EDTYPE;
+}

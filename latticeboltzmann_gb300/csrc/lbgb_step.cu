@@ -1,0 +1,316 @@
+// Pull-scheme streaming (periodic, or cavity walls with a moving lid) with an
+// optional fused BGK collision: the hot path of liblbgb.
+//
+// Work decomposition.  A warp owns one "segment": 32*V consecutive cells of one
+// row k (V cells per lane, l fastest).  Every population is read exactly once
+// and written exactly once, so the kernel is a pure HBM stream: per cell
+// 9 loads and 9 stores of the storage type (72 B/cell in FP32, 36 B in 16-bit).
+//
+//  * Channels with cx != 0 read the same l range of row k -/+ 1: an aligned
+//    vector load.
+//  * Channels with cy != 0 need the lane's vector shifted by one cell along l.
+//    The lane loads its own aligned vector and takes the missing edge value
+//    from the neighbouring lane with a warp shuffle; only lanes at a segment
+//    or row edge issue one extra scalar load (the warp-level replacement of
+//    the reference's ghost-cell halo exchange, cavity_opt1.py:247-278).
+//  * Cavity walls (cavity_opt1.py:177-245): whole wall rows k = 0 and
+//    k = nx-1 are warp-uniform, so their bounce-back is a change of the
+//    source plane and row, taken by the whole warp.  The bottom and lid nodes
+//    (l = 0, l = ny-1) belong to single lanes, which patch their values with
+//    a few scalar loads, including the lid density that the reference reads
+//    across the periodic seam at the two lid corners.
+#include <stdio.h>
+
+#include "lbgb_common.cuh"
+
+namespace lbgb {
+
+constexpr unsigned FULL = 0xffffffffu;
+
+template <class C, int V>
+__device__ __forceinline__ void load_plane(const typename C::raw *__restrict__ src, size_t cs, int ny,
+                                           int ch_src, int ch_dec, int row, int l0, bool act,
+                                           typename C::real (&o)[V]) {
+    if (act) {
+        typename C::raw r[V];
+        ldv<typename C::raw, V>(src + (size_t)ch_src * cs + (size_t)row * ny + l0, r);
+#pragma unroll
+        for (int j = 0; j < V; ++j) o[j] = C::dec(r[j], ch_dec);
+    } else {
+#pragma unroll
+        for (int j = 0; j < V; ++j) o[j] = 0;
+    }
+}
+
+template <class C>
+__device__ __forceinline__ typename C::real load_one(const typename C::raw *__restrict__ src, size_t cs,
+                                                     int ny, int ch, int row, int l) {
+    return C::dec(ld1(src + (size_t)ch * cs + (size_t)row * ny + l), ch);
+}
+
+// o[j] <- value at l0+j-1 (channels moving in +y).
+template <class C, int V, int BC>
+__device__ __forceinline__ void shift_from_below(typename C::real (&o)[V], const typename C::raw *__restrict__ src,
+                                                 size_t cs, int ny, int ch, int row, int l0, int lane,
+                                                 bool act) {
+    typename C::real prev = __shfl_up_sync(FULL, o[V - 1], 1);
+    if (lane == 0 && act) {
+        if (l0 > 0)
+            prev = load_one<C>(src, cs, ny, ch, row, l0 - 1);
+        else if (BC == LBGB_PERIODIC)
+            prev = load_one<C>(src, cs, ny, ch, row, ny - 1);
+        // cavity, l0 == 0: bottom-wall bounce-back patched by the caller
+    }
+#pragma unroll
+    for (int j = V - 1; j > 0; --j) o[j] = o[j - 1];
+    o[0] = prev;
+}
+
+// o[j] <- value at l0+j+1 (channels moving in -y).
+template <class C, int V, int BC>
+__device__ __forceinline__ void shift_from_above(typename C::real (&o)[V], const typename C::raw *__restrict__ src,
+                                                 size_t cs, int ny, int ch, int row, int l0, int lane,
+                                                 bool act) {
+    typename C::real next = __shfl_down_sync(FULL, o[0], 1);
+    if (act && (lane == 31 || l0 + V >= ny)) {
+        if (l0 + V < ny)
+            next = load_one<C>(src, cs, ny, ch, row, l0 + V);
+        else if (BC == LBGB_PERIODIC)
+            next = load_one<C>(src, cs, ny, ch, row, 0);
+        // cavity, last node of the row: lid rule patched by the caller
+    }
+#pragma unroll
+    for (int j = 0; j < V - 1; ++j) o[j] = o[j + 1];
+    o[V - 1] = next;
+}
+
+// Pulls channel ch of V nodes (k, l0..l0+V-1) into o.  wall = the source row
+// lies beyond a cavity side wall: bounce back from the same node instead.
+template <class C, int V, int BC, int CH>
+__device__ __forceinline__ void pull_channel(typename C::real (&o)[V], const typename C::raw *__restrict__ src,
+                                             size_t cs, int ny, int k, int krow, bool wall, int l0, int lane,
+                                             bool act) {
+    if (wall) {
+        load_plane<C, V>(src, cs, ny, opp(CH), CH, k, l0, act, o);
+        return;
+    }
+    load_plane<C, V>(src, cs, ny, CH, CH, krow, l0, act, o);
+    if (cy(CH) > 0) shift_from_below<C, V, BC>(o, src, cs, ny, CH, krow, l0, lane, act);
+    if (cy(CH) < 0) shift_from_above<C, V, BC>(o, src, cs, ny, CH, krow, l0, lane, act);
+}
+
+template <int DT, int BC, bool COLLIDE, int V>
+__global__ void __launch_bounds__(256)
+k_step(const typename Codec<DT>::raw *__restrict__ src, typename Codec<DT>::raw *__restrict__ dst, int nx,
+       int ny, int segs, long long tasks, typename Codec<DT>::real omega, typename Codec<DT>::real u0) {
+    using C = Codec<DT>;
+    using real = typename C::real;
+    using raw = typename C::raw;
+    const int lane = threadIdx.x & 31;
+    const long long nwarps = ((long long)gridDim.x * blockDim.x) >> 5;
+    const size_t cs = (size_t)nx * ny;
+    for (long long t = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5; t < tasks; t += nwarps) {
+        const int k = (int)(t / segs);
+        const int l0 = (int)(t - (long long)k * segs) * (32 * V) + lane * V;
+        const bool act = l0 < ny;
+        int km = k - 1, kp = k + 1;
+        bool wl = false, wr = false;
+        if (BC == LBGB_PERIODIC) {
+            if (km < 0) km += nx;
+            if (kp >= nx) kp -= nx;
+        } else {
+            wl = (k == 0);
+            wr = (k == nx - 1);
+        }
+        real v[9][V];
+        pull_channel<C, V, BC, C0>(v[C0], src, cs, ny, k, k, false, l0, lane, act);
+        pull_channel<C, V, BC, CE>(v[CE], src, cs, ny, k, km, wl, l0, lane, act);
+        pull_channel<C, V, BC, CN>(v[CN], src, cs, ny, k, k, false, l0, lane, act);
+        pull_channel<C, V, BC, CW>(v[CW], src, cs, ny, k, kp, wr, l0, lane, act);
+        pull_channel<C, V, BC, CS>(v[CS], src, cs, ny, k, k, false, l0, lane, act);
+        pull_channel<C, V, BC, CNE>(v[CNE], src, cs, ny, k, km, wl, l0, lane, act);
+        pull_channel<C, V, BC, CNW>(v[CNW], src, cs, ny, k, kp, wr, l0, lane, act);
+        pull_channel<C, V, BC, CSW>(v[CSW], src, cs, ny, k, kp, wr, l0, lane, act);
+        pull_channel<C, V, BC, CSE>(v[CSE], src, cs, ny, k, km, wl, l0, lane, act);
+
+        if (BC == LBGB_CAVITY && act) {
+            if (l0 == 0) {
+                // bottom wall: N, NE, NW bounce back from the same node
+                v[CN][0] = load_one<C>(src, cs, ny, CS, k, 0);
+                v[CNE][0] = load_one<C>(src, cs, ny, CSW, k, 0);
+                v[CNW][0] = load_one<C>(src, cs, ny, CSE, k, 0);
+            }
+            if (l0 + V == ny) {
+                // lid: S bounces back; SE/SW get the Ladd term 6 w rho_lid u0,
+                // except at the corner where the side wall wins (plain bounce-back)
+                const int T = ny - 1;
+                const int kw = (k == 0) ? nx - 1 : k - 1;  // periodic neighbours, as
+                const int ke = (k == nx - 1) ? 0 : k + 1;  // the reference's roll reads them
+                const real gN = load_one<C>(src, cs, ny, CN, k, T);
+                const real gNW = load_one<C>(src, cs, ny, CNW, k, T);
+                const real gNE = load_one<C>(src, cs, ny, CNE, k, T);
+                const real rho_lid = gNW + gN + gNE + load_one<C>(src, cs, ny, CNW, ke, T - 1) +
+                                     load_one<C>(src, cs, ny, CN, k, T - 1) +
+                                     load_one<C>(src, cs, ny, CNE, kw, T - 1) +
+                                     load_one<C>(src, cs, ny, CW, ke, T) + load_one<C>(src, cs, ny, C0, k, T) +
+                                     load_one<C>(src, cs, ny, CE, kw, T);
+                const real lid = (real(6) * real(1.0 / 36.0)) * rho_lid * u0;
+                v[CS][V - 1] = gN;
+                v[CSE][V - 1] = (k == 0) ? gNW : gNW + lid;
+                v[CSW][V - 1] = (k == nx - 1) ? gNE : gNE - lid;
+            }
+        }
+
+        if (COLLIDE) {
+#pragma unroll
+            for (int j = 0; j < V; ++j) {
+                real f[9];
+#pragma unroll
+                for (int i = 0; i < 9; ++i) f[i] = v[i][j];
+                bgk_collide(f, omega);
+#pragma unroll
+                for (int i = 0; i < 9; ++i) v[i][j] = f[i];
+            }
+        }
+        if (act) {
+#pragma unroll
+            for (int i = 0; i < 9; ++i) {
+                raw r[V];
+#pragma unroll
+                for (int j = 0; j < V; ++j) r[j] = C::enc(v[i][j], i);
+                stv<raw, V>(dst + (size_t)i * cs + (size_t)k * ny + l0, r);
+            }
+        }
+    }
+}
+
+// ---------------------------------------------------------------- launch
+static int sm_count() {
+    static int n = 0;
+    if (n == 0) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+        if (n <= 0) n = 1;
+    }
+    return n;
+}
+
+template <int DT, int BC, bool COLLIDE, int V>
+static int launch_v(const void *src, void *dst, int nx, int ny, double omega, double u0, cudaStream_t s) {
+    using C = Codec<DT>;
+    const int threads = 256;
+    const int segs = (ny + 32 * V - 1) / (32 * V);
+    const long long tasks = (long long)nx * segs;
+    const long long warps_per_block = threads / 32;
+    long long blocks = (tasks + warps_per_block - 1) / warps_per_block;
+    // at most 16 resident-size waves of blocks; the rest is grid-stride
+    const long long cap = (long long)sm_count() * 8 * 16;
+    if (blocks > cap) blocks = cap;
+    k_step<DT, BC, COLLIDE, V><<<(unsigned)blocks, threads, 0, s>>>(
+        static_cast<const typename C::raw *>(src), static_cast<typename C::raw *>(dst), nx, ny, segs, tasks,
+        (typename C::real)omega, (typename C::real)u0);
+    return check_launch("k_step");
+}
+
+// Widest vector width that divides ny and keeps every row start aligned.
+template <int DT, int BC, bool COLLIDE>
+static int launch(const void *src, void *dst, int nx, int ny, double omega, double u0, cudaStream_t s) {
+    constexpr int VW = 16 / sizeof(typename Codec<DT>::raw);
+    const size_t al = VW * sizeof(typename Codec<DT>::raw);
+    if (ny % VW == 0 && aligned(src, al) && aligned(dst, al))
+        return launch_v<DT, BC, COLLIDE, VW>(src, dst, nx, ny, omega, u0, s);
+    return launch_v<DT, BC, COLLIDE, 1>(src, dst, nx, ny, omega, u0, s);
+}
+
+template <int BC, bool COLLIDE>
+static int dispatch(const void *src, void *dst, int nx, int ny, int dtype, double omega, double u0,
+                    cudaStream_t s) {
+    switch (dtype) {
+    case LBGB_F32: return launch<LBGB_F32, BC, COLLIDE>(src, dst, nx, ny, omega, u0, s);
+    case LBGB_F64: return launch<LBGB_F64, BC, COLLIDE>(src, dst, nx, ny, omega, u0, s);
+    case LBGB_F16DEV: return launch<LBGB_F16DEV, BC, COLLIDE>(src, dst, nx, ny, omega, u0, s);
+    case LBGB_BF16DEV: return launch<LBGB_BF16DEV, BC, COLLIDE>(src, dst, nx, ny, omega, u0, s);
+    default: set_error("unsupported storage code %d", dtype); return LBGB_EDTYPE;
+    }
+}
+
+static int check_grid(const void *src, void *dst, int nx, int ny, int dtype, int boundary, const char *what) {
+    if (raw_size(dtype) == 0) {
+        set_error("%s: unsupported storage code %d", what, dtype);
+        return LBGB_EDTYPE;
+    }
+    if (nx <= 0 || ny <= 0) {
+        set_error("%s: grid %d x %d must be positive", what, nx, ny);
+        return LBGB_EINVAL;
+    }
+    if (boundary == LBGB_CAVITY && (nx < 2 || ny < 2)) {
+        set_error("%s: the cavity needs nx >= 2 and ny >= 2 (got %d x %d)", what, nx, ny);
+        return LBGB_EINVAL;
+    }
+    if (boundary != LBGB_CAVITY && boundary != LBGB_PERIODIC) {
+        set_error("%s: unknown boundary code %d", what, boundary);
+        return LBGB_EINVAL;
+    }
+    if (!src || !dst) {
+        set_error("%s: null population pointer", what);
+        return LBGB_EINVAL;
+    }
+    const size_t bytes = 9 * (size_t)nx * ny * raw_size(dtype);
+    const char *a = static_cast<const char *>(src), *b = static_cast<const char *>(dst);
+    if (a < b + bytes && b < a + bytes) {
+        set_error("%s: src and dst overlap; streaming is out of place", what);
+        return LBGB_EINVAL;
+    }
+    if (!aligned(src, raw_size(dtype)) || !aligned(dst, raw_size(dtype))) {
+        set_error("%s: population pointers must be aligned to the element size", what);
+        return LBGB_EINVAL;
+    }
+    return LBGB_OK;
+}
+
+}  // namespace lbgb
+
+using namespace lbgb;
+
+extern "C" int lbgb_stream_periodic(const void *src, void *dst, int nx, int ny, int dtype, void *stream) {
+    int rc = check_grid(src, dst, nx, ny, dtype, LBGB_PERIODIC, "lbgb_stream_periodic");
+    if (rc) return rc;
+    return dispatch<LBGB_PERIODIC, false>(src, dst, nx, ny, dtype, 0.0, 0.0, (cudaStream_t)stream);
+}
+
+extern "C" int lbgb_stream_bounce_back(const void *src, void *dst, int nx, int ny, double u0, int dtype,
+                                       void *stream) {
+    int rc = check_grid(src, dst, nx, ny, dtype, LBGB_CAVITY, "lbgb_stream_bounce_back");
+    if (rc) return rc;
+    return dispatch<LBGB_CAVITY, false>(src, dst, nx, ny, dtype, 0.0, u0, (cudaStream_t)stream);
+}
+
+extern "C" int lbgb_step_fused(const void *src, void *dst, int nx, int ny, int boundary, double omega, double u0,
+                               int dtype, void *stream) {
+    int rc = check_grid(src, dst, nx, ny, dtype, boundary, "lbgb_step_fused");
+    if (rc) return rc;
+    if (boundary == LBGB_CAVITY)
+        return dispatch<LBGB_CAVITY, true>(src, dst, nx, ny, dtype, omega, u0, (cudaStream_t)stream);
+    return dispatch<LBGB_PERIODIC, true>(src, dst, nx, ny, dtype, omega, 0.0, (cudaStream_t)stream);
+}
+
+extern "C" int lbgb_run_fused(void *a, void *b, int nx, int ny, int boundary, double omega, double u0, int dtype,
+                              int nsteps, int *which, void *stream) {
+    if (nsteps < 0) {
+        set_error("lbgb_run_fused: nsteps must be >= 0");
+        return LBGB_EINVAL;
+    }
+    int rc = check_grid(a, b, nx, ny, dtype, boundary, "lbgb_run_fused");
+    if (rc) return rc;
+    void *src = a, *dst = b;
+    for (int s = 0; s < nsteps; ++s) {
+        rc = lbgb_step_fused(src, dst, nx, ny, boundary, omega, u0, dtype, stream);
+        if (rc) return rc;
+        void *t = src;
+        src = dst;
+        dst = t;
+    }
+    if (which) *which = (src == a) ? 0 : 1;
+    return LBGB_OK;
+}

@@ -1,0 +1,262 @@
+"""Device-resident D2Q9 solver around the fused stream-collide kernel.
+
+The reference's time loop calls ``stream_and_bounce_back`` then ``collide`` on
+one host array per step (simulators/parallel_lid_drive_cavity/cavity_opt2.py:
+272-283; periodic: simulators/serial_shear_wave/Python/shear_wave_opt2.py:
+94-99).  ``Lattice`` keeps two population buffers in HBM and advances them with
+one fused pull-stream + collide launch per step (ping-pong, no copies); the
+stored state after each step is post-collision, as in the reference.
+
+Storage: ``f32``/``f64`` store f; ``f16dev``/``bf16dev`` store f_i - w_i in 16
+bits with FP32 arithmetic (half the bytes per lattice update).
+"""
+
+import ctypes
+
+import torch
+
+from . import _lib
+from ._tensor import require_cuda
+
+_RAW = {"f32": torch.float32, "f64": torch.float64, "f16dev": torch.int16, "bf16dev": torch.int16}
+_REAL = {"f32": torch.float32, "f64": torch.float64, "f16dev": torch.float32, "bf16dev": torch.float32}
+
+
+def omega_from_reynolds(re, lid_velocity, length):
+    """Relaxation parameter for a cavity of side ``length`` at Reynolds number ``re``.
+
+    ``nu = u L / Re`` and ``omega = 1 / (3 nu + 1/2)``, i.e. the relation
+    ``omega = 2 Re / (6 L u + Re)`` of simulators/simple_flows/slidingLid.py:28.
+    """
+    return 2.0 * re / (6.0 * length * lid_velocity + re)
+
+
+def viscosity_from_omega(omega):
+    """Kinematic viscosity of the BGK lattice fluid, ``(1/omega - 1/2) / 3``."""
+    return (1.0 / omega - 0.5) / 3.0
+
+
+class Lattice:
+    """A ``(9, nx, ny)`` D2Q9 lattice resident on one GPU.
+
+    Parameters
+    ----------
+    nx, ny : int
+        Grid size (``ny`` is the fast axis; the cavity lid is at ``l = ny-1``).
+    omega : float
+        BGK relaxation parameter.
+    boundary : {"cavity", "periodic"}
+        ``cavity``: bounce-back on four walls, lid moving with ``u0`` in +x.
+    u0 : float
+        Lid velocity (cavity only).
+    storage : {"f32", "f64", "f16dev", "bf16dev"}
+    device : torch device (CUDA).
+    """
+
+    def __init__(self, nx, ny, omega, boundary="cavity", u0=0.1, storage="f32", device=None):
+        if storage not in _RAW:
+            raise ValueError("storage must be one of %s" % sorted(_RAW))
+        if boundary not in _lib.BOUNDARY_CODES:
+            raise ValueError("boundary must be 'cavity' or 'periodic'")
+        if nx <= 0 or ny <= 0:
+            raise ValueError("grid must be positive, got %d x %d" % (nx, ny))
+        if boundary == "cavity" and (nx < 2 or ny < 2):
+            raise ValueError("the cavity needs nx >= 2 and ny >= 2")
+        self.nx, self.ny = int(nx), int(ny)
+        self.omega = float(omega)
+        self.u0 = float(u0) if boundary == "cavity" else 0.0
+        self.boundary = boundary
+        self.storage = storage
+        self.code = _lib.STORAGE_CODES[storage]
+        self.bcode = _lib.BOUNDARY_CODES[boundary]
+        self.device = torch.device(device) if device is not None else torch.device("cuda", torch.cuda.current_device())
+        if self.device.type != "cuda":
+            raise TypeError("Lattice lives on a CUDA device (there is no CPU path)")
+        shape = (9, self.nx, self.ny)
+        self._buf = [torch.empty(shape, dtype=_RAW[storage], device=self.device),
+                     torch.empty(shape, dtype=_RAW[storage], device=self.device)]
+        self._cur = 0
+        self._ws = None
+        self.steps_taken = 0
+        self.equilibrium()
+
+    # ------------------------------------------------------------------ state
+    @property
+    def cells(self):
+        return self.nx * self.ny
+
+    @property
+    def bytes_per_cell_update(self):
+        """Algorithmic HBM bytes per cell and step: 9 loads + 9 stores."""
+        return 18 * self._buf[0].element_size()
+
+    @property
+    def state(self):
+        """The raw storage tensor holding the current populations."""
+        return self._buf[self._cur]
+
+    def _stream(self):
+        return torch.cuda.current_stream(self.device).cuda_stream
+
+    def load(self, f):
+        """Set the populations from a float tensor ``(9, nx, ny)`` on any device.
+
+        A host tensor of the storage's own dtype is copied straight into the
+        device state (asynchronously when it is pinned); anything else goes
+        through a conversion on the device.
+        """
+        f = torch.as_tensor(f)
+        if tuple(f.shape) != (9, self.nx, self.ny):
+            raise ValueError("expected populations of shape %s, got %s" % ((9, self.nx, self.ny), tuple(f.shape)))
+        if self.storage in ("f32", "f64") and f.dtype == self.state.dtype and f.is_contiguous():
+            self.state.copy_(f, non_blocking=f.device.type == "cpu" and f.is_pinned())
+            return self
+        src = f.to(device=self.device, dtype=_REAL[self.storage]).contiguous()
+        if self.storage in ("f32", "f64"):
+            self.state.copy_(src)
+        else:
+            _lib.call("lbgb_convert", src.data_ptr(), _lib.F32, self.cells, self.state.data_ptr(), self.code,
+                      self.cells, self.cells, self._stream())
+        return self
+
+    def equilibrium(self, rho=None, ux=None, uy=None):
+        """Set the populations to the equilibrium of (rho, ux, uy) (default: rest)."""
+        real = torch.float64 if self.storage == "f64" else torch.float32
+        shape = (self.nx, self.ny)
+
+        def field(v, default):
+            if v is None:
+                return torch.full(shape, default, dtype=real, device=self.device)
+            v = torch.as_tensor(v, dtype=real, device=self.device)
+            return v.expand(shape).contiguous()
+
+        r, x, y = field(rho, 1.0), field(ux, 0.0), field(uy, 0.0)
+        code = _lib.F64 if self.storage == "f64" else _lib.F32
+        if self.storage in ("f32", "f64"):
+            _lib.call("lbgb_equilibrium", r.data_ptr(), x.data_ptr(), y.data_ptr(), self.state.data_ptr(),
+                      self.cells, self.cells, code, self._stream())
+        else:
+            tmp = torch.empty((9, self.nx, self.ny), dtype=torch.float32, device=self.device)
+            _lib.call("lbgb_equilibrium", r.data_ptr(), x.data_ptr(), y.data_ptr(), tmp.data_ptr(),
+                      self.cells, self.cells, code, self._stream())
+            _lib.call("lbgb_convert", tmp.data_ptr(), _lib.F32, self.cells, self.state.data_ptr(), self.code,
+                      self.cells, self.cells, self._stream())
+        return self
+
+    def populations(self, dtype=None, out=None):
+        """The populations f as a float tensor ``(9, nx, ny)`` (decoded for 16-bit storage).
+
+        ``out``: a preallocated tensor (e.g. pinned host memory) of the
+        storage's dtype to copy into, asynchronously on the current stream.
+        """
+        if out is not None:
+            if self.storage not in ("f32", "f64") or out.dtype != self.state.dtype:
+                out.copy_(self.populations(dtype=out.dtype))
+            else:
+                out.copy_(self.state, non_blocking=out.device.type == "cpu" and out.is_pinned())
+            return out
+        if self.storage in ("f32", "f64") and dtype is None:
+            return self.state.clone()
+        dtype = dtype or torch.float32
+        out = torch.empty((9, self.nx, self.ny), dtype=dtype, device=self.device)
+        dst = _lib.F64 if dtype == torch.float64 else _lib.F32
+        _lib.call("lbgb_convert", self.state.data_ptr(), self.code, self.cells, out.data_ptr(), dst, self.cells,
+                  self.cells, self._stream())
+        return out
+
+    # ------------------------------------------------------------------ stepping
+    def step(self, n=1):
+        """Advance ``n`` time steps (one fused launch each)."""
+        if n <= 0:
+            return self
+        which = ctypes.c_int(0)
+        a, b = self._buf[self._cur], self._buf[1 - self._cur]
+        _lib.call("lbgb_run_fused", a.data_ptr(), b.data_ptr(), self.nx, self.ny, self.bcode, self.omega, self.u0,
+                  self.code, int(n), ctypes.byref(which), self._stream())
+        if which.value == 1:
+            self._cur = 1 - self._cur
+        self.steps_taken += n
+        return self
+
+    def capture(self, n):
+        """Capture ``n`` steps into a CUDA graph; returns a callable replaying them.
+
+        ``n`` must be even so that the state returns to the same buffer after
+        each replay (the graph bakes the buffer addresses in).
+        """
+        if n <= 0 or n % 2:
+            raise ValueError("capture: n must be a positive even number")
+        # load the kernel variant outside the capture: one step on a two-row
+        # copy with the same row length (same vector width, same template)
+        warm = [torch.zeros((9, 2, self.ny), dtype=_RAW[self.storage], device=self.device) for _ in range(2)]
+        _lib.call("lbgb_step_fused", warm[0].data_ptr(), warm[1].data_ptr(), 2, self.ny, self.bcode, self.omega,
+                  self.u0, self.code, self._stream())
+        torch.cuda.current_stream(self.device).synchronize()
+        s = torch.cuda.Stream(device=self.device)
+        s.wait_stream(torch.cuda.current_stream(self.device))
+        g = torch.cuda.CUDAGraph()
+        cur = self._cur
+        with torch.cuda.stream(s):
+            with torch.cuda.graph(g, stream=s):
+                self.step(n)
+        # capture recorded launches only; restore the bookkeeping
+        self._cur = cur
+        self.steps_taken -= n
+        torch.cuda.current_stream(self.device).wait_stream(s)
+        lattice = self
+
+        def replay():
+            g.replay()
+            lattice.steps_taken += n
+
+        replay.graph = g
+        return replay
+
+    # ------------------------------------------------------------------ diagnostics
+    def macroscopic(self):
+        """(rho, ux, uy), each ``(nx, ny)``, from the current populations."""
+        real = torch.float64 if self.storage == "f64" else torch.float32
+        rho = torch.empty((self.nx, self.ny), dtype=real, device=self.device)
+        ux = torch.empty_like(rho)
+        uy = torch.empty_like(rho)
+        _lib.call("lbgb_macroscopic", self.state.data_ptr(), rho.data_ptr(), ux.data_ptr(), uy.data_ptr(),
+                  self.cells, self.cells, self.code, self._stream())
+        return rho, ux, uy
+
+    def mass_momentum(self):
+        """Total (mass, x momentum, y momentum) as a float64 CUDA tensor, FP64 sums."""
+        if self._ws is None:
+            nbytes = _lib.load().lbgb_mass_momentum_workspace_bytes()
+            self._ws = torch.empty(nbytes // 8 + 1, dtype=torch.float64, device=self.device)
+        out = torch.empty(3, dtype=torch.float64, device=self.device)
+        _lib.call("lbgb_mass_momentum", self.state.data_ptr(), self.cells, self.cells, self.code, out.data_ptr(),
+                  self._ws.data_ptr(), self._ws.numel() * 8, self._stream())
+        return out
+
+
+def mass_momentum(f):
+    """Total (mass, x momentum, y momentum) of a float32/float64 ``(9, ...)`` CUDA tensor."""
+    from ._tensor import population_view, storage_code, stream_handle
+    n, cs = population_view(f, "mass_momentum")
+    code = storage_code(f, "mass_momentum")
+    nbytes = _lib.load().lbgb_mass_momentum_workspace_bytes()
+    ws = torch.empty(nbytes // 8 + 1, dtype=torch.float64, device=f.device)
+    out = torch.empty(3, dtype=torch.float64, device=f.device)
+    _lib.call("lbgb_mass_momentum", f.data_ptr(), n, cs, code, out.data_ptr(), ws.data_ptr(), ws.numel() * 8,
+              stream_handle(f))
+    return out
+
+
+def macroscopic(f):
+    """(rho, ux, uy) of a float32/float64 ``(9, nx, ny)`` or ``(9, N)`` CUDA tensor."""
+    from ._tensor import population_view, storage_code, stream_handle
+    n, cs = population_view(f, "macroscopic")
+    code = storage_code(f, "macroscopic")
+    shape = tuple(f.shape[1:])
+    rho = torch.empty(shape, dtype=f.dtype, device=f.device)
+    ux = torch.empty_like(rho)
+    uy = torch.empty_like(rho)
+    if n:
+        _lib.call("lbgb_macroscopic", f.data_ptr(), rho.data_ptr(), ux.data_ptr(), uy.data_ptr(), n, cs, code,
+                  stream_handle(f))
+    return rho, ux, uy

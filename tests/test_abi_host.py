@@ -1,0 +1,126 @@
+"""Host-side checks that need no GPU: the C ABI library loads and exports every
+symbol of include/lbgb.h, the Python signatures agree with the header, and
+the operators reject what the reference's pybind11 binding rejects."""
+
+import os
+import re
+
+import numpy as np
+import pytest
+import torch
+
+import latticeboltzmann_gb300 as PyLB
+from latticeboltzmann_gb300 import IO, _lib
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def header_symbols():
+    src = open(os.path.join(ROOT, "include", "lbgb.h")).read()
+    return re.findall(r"^LBGB_API\s+\w+\s+(lbgb_\w+)\s*\(", src, flags=re.M)
+
+
+@pytest.fixture(scope="module")
+def lib():
+    if not os.path.exists(_lib.LIB_PATH):
+        from latticeboltzmann_gb300 import _build
+        _build.build()
+    return _lib.load()
+
+
+def test_header_declares_entry_points():
+    names = header_symbols()
+    assert len(names) >= 12
+    assert set(names) == set(_lib.SIGNATURES), "Python signature table and header disagree"
+
+
+def test_library_exports_every_header_symbol(lib):
+    for name in header_symbols():
+        assert hasattr(lib, name), name
+
+
+def test_version_and_error_buffer(lib):
+    assert lib.lbgb_version() >= 10000
+    # an invalid call fails on the host before any CUDA work and sets a message
+    rc = lib.lbgb_stream_bounce_back(None, None, 1, 1, 0.1, 0, None)
+    assert rc == _lib.EINVAL
+    assert "cavity" in _lib.last_error()
+    rc = lib.lbgb_collide(None, 4, 4, 7, 1.0, None)
+    assert rc == _lib.EDTYPE
+    with pytest.raises(TypeError):
+        _lib.check(rc)
+
+
+def test_host_validation_before_any_launch(lib):
+    rc = lib.lbgb_step_fused(1 << 20, (1 << 20) + 64, 8, 8, _lib.PERIODIC, 1.0, 0.0, _lib.F32, None)
+    assert rc == _lib.EINVAL and "overlap" in _lib.last_error()
+    rc = lib.lbgb_mass_momentum(1 << 20, 16, 16, _lib.F32, 1 << 24, None, 0, None)
+    assert rc == _lib.EWORKSPACE
+    rc = lib.lbgb_collide(None, 16, 8, _lib.F32, 1.0, None)
+    assert rc == _lib.EINVAL
+
+
+def test_workspace_size_is_small(lib):
+    assert 0 < lib.lbgb_mass_momentum_workspace_bytes() <= 1 << 20
+
+
+@pytest.mark.parametrize("bad", [np.zeros((9, 16)), torch.zeros(9, 16), [0.0] * 9])
+def test_no_cpu_path(bad):
+    with pytest.raises(TypeError):
+        PyLB.collide(bad, 1.0)
+    with pytest.raises(TypeError):
+        PyLB.stream(bad)
+    with pytest.raises(TypeError):
+        PyLB.Streaming.stream_and_bounce_back(bad)
+
+
+def test_c_ic_matches_reference_layout():
+    assert PyLB.Streaming.c_ic.shape == (9, 2)
+    assert PyLB.Streaming.c_ic[5].tolist() == [1, 1]
+    assert PyLB.Streaming.c_ic[8].tolist() == [1, -1]
+
+
+def test_reynolds_relation():
+    # omega = 2 Re / (6 L u + Re)  <=>  nu = u L / Re
+    om = PyLB.omega_from_reynolds(1000, 0.1, 300)
+    assert abs(PyLB.viscosity_from_omega(om) - 0.1 * 300 / 1000) < 1e-15
+
+
+def reference_header(dtype, shape):
+    # the padding rule of PyLB/IO.py:55-61, restated
+    from numpy.lib.format import dtype_to_descr, magic
+    m = magic(1, 0)
+    d = str({"descr": dtype_to_descr(np.dtype(dtype)), "fortran_order": False, "shape": shape})
+    while (len(d) + len(m) + 2) % 16 != 15:
+        d += " "
+    d += "\n"
+    return m + np.int16(len(d)).tobytes() + d.encode("latin-1")
+
+
+@pytest.mark.parametrize("dtype,shape", [(np.float64, (300, 300)), (np.float32, (7, 5)), (np.float32, (0, 3))])
+def test_npy_header_layout(dtype, shape):
+    h = IO.npy_header(dtype, shape)
+    assert h == reference_header(dtype, shape)
+    assert len(h) % 16 == 0
+
+
+def test_save_npy_round_trip(tmp_path):
+    a = np.arange(35, dtype=np.float32).reshape(7, 5) / 3
+    fn = str(tmp_path / "ux.npy")
+    IO.save_mpiio(None, fn, a)
+    b = np.load(fn)
+    np.testing.assert_array_equal(a, b)
+
+    class OneRank:
+        def Get_size(self):
+            return 1
+
+    IO.save_mpiio(OneRank(), fn, a.astype(np.float64))
+    assert np.load(fn).dtype == np.float64
+
+    class TwoRanks:
+        def Get_size(self):
+            return 2
+
+    with pytest.raises(NotImplementedError):
+        IO.save_mpiio(TwoRanks(), fn, a)

@@ -1,0 +1,111 @@
+"""Precision of the fused solver against float64 runs of the oracle.
+
+Stated tolerances (lid-driven cavity 64 x 64, omega = 1.7, u0 = 0.1, from rest,
+1000 steps; relative L2 error of the velocity field against the float64
+oracle):
+
+* f64 storage:     populations within 1e-12 absolute of the float64 oracle.
+* f32 storage:     rel-L2(u) <= 1e-5, and no worse than 1.5x the error of the
+                   reference's own float32 arithmetic (cavity_opt1.py run with
+                   dtype=float32, reproduced bit-exactly by oracle/d2q9.py).
+                   The floor is FP32 rounding inside the collision; the
+                   reference's float32 path measures about 6e-6 here.
+* f16dev storage:  rel-L2(u) <= 2e-3    (half deviations f_i - w_i)
+* bf16dev storage: rel-L2(u) <= 1.5e-2  (bfloat16 deviations)
+"""
+
+import numpy as np
+import pytest
+import torch
+
+import latticeboltzmann_gb300 as PyLB
+from oracle import d2q9 as oracle
+from oracle import port
+
+pytestmark = pytest.mark.gpu
+
+NX, NY, OMEGA, U0, STEPS = 64, 64, 1.7, 0.1, 1000
+
+
+def rel_l2_u(f, f_ref):
+    _, ux, uy = oracle.macroscopic(np.asarray(f, dtype=np.float64))
+    _, rx, ry = oracle.macroscopic(f_ref)
+    return np.sqrt(((ux - rx) ** 2 + (uy - ry) ** 2).sum() / (rx ** 2 + ry ** 2).sum())
+
+
+@pytest.fixture(scope="module")
+def ref64():
+    f = oracle.equilibrium(np.ones((NX, NY)), np.zeros((NX, NY)), np.zeros((NX, NY)))
+    return port.cavity_run(f, OMEGA, U0, STEPS, nthreads=0)
+
+
+@pytest.fixture(scope="module")
+def ref32_error(ref64):
+    # the reference's own float32 arithmetic (numpy, cavity_opt1.py order)
+    one = np.ones((NX, NY), np.float32)
+    zero = np.zeros((NX, NY), np.float32)
+    f = oracle.equilibrium(one, zero, zero)
+    om = np.array(OMEGA, dtype=np.float32)
+    for _ in range(STEPS):
+        oracle.cavity_step(f, om, U0)
+    return rel_l2_u(f, ref64)
+
+
+def run(storage, cuda, steps=STEPS, nx=NX, ny=NY, omega=OMEGA):
+    lat = PyLB.Lattice(nx, ny, omega, boundary="cavity", u0=U0, storage=storage, device=cuda)
+    lat.step(steps)
+    return lat
+
+
+def test_f64_matches_oracle(cuda, ref64):
+    lat = run("f64", cuda)
+    assert np.abs(lat.populations().cpu().numpy() - ref64).max() < 1e-12
+
+
+def test_f32_error_bound(cuda, ref64, ref32_error):
+    lat = run("f32", cuda)
+    err = rel_l2_u(lat.populations().cpu().numpy(), ref64)
+    assert err <= 1e-5, err
+    assert err <= 1.5 * ref32_error, (err, ref32_error)
+
+
+@pytest.mark.parametrize("storage,tol", [("f16dev", 2e-3), ("bf16dev", 1.5e-2)])
+def test_16bit_deviation_storage_error_bound(cuda, ref64, storage, tol):
+    lat = run(storage, cuda)
+    f = lat.populations(torch.float64).cpu().numpy()
+    err = rel_l2_u(f, ref64)
+    assert err <= tol, (storage, err)
+    # mass drift of the 16-bit run tracks the float64 run's (the lid injects mass)
+    m_ref = ref64.sum() - NX * NY
+    m = float(lat.mass_momentum()[0]) - NX * NY
+    assert abs(m - m_ref) <= 0.05 * abs(m_ref) + 1e-3
+
+
+@pytest.mark.parametrize("storage", ["f32", "f16dev", "bf16dev"])
+def test_resting_walls_conserve_mass(cuda, storage):
+    lat = PyLB.Lattice(48, 40, 1.2, boundary="cavity", u0=0.0, storage=storage, device=cuda)
+    rng = np.random.default_rng(3)
+    rho = torch.from_numpy(1 + 0.01 * rng.standard_normal((48, 40))).to(cuda)
+    lat.equilibrium(rho=rho)
+    m0 = float(lat.mass_momentum()[0])
+    lat.step(500)
+    m1 = float(lat.mass_momentum()[0])
+    tol = {"f32": 2e-3, "f16dev": 2e-2, "bf16dev": 0.2}[storage]
+    assert abs(m1 - m0) < tol, (storage, m1 - m0)
+
+
+def test_shear_wave_viscosity(cuda):
+    """Velocity shear wave on a periodic lattice decays at nu = (1/omega - 1/2)/3."""
+    nx, ny, omega, steps = 64, 32, 1.0, 400
+    f0 = oracle.shear_wave_init(nx, ny, amplitude=0.01, along="y")
+    lat = PyLB.Lattice(nx, ny, omega, boundary="periodic", storage="f64", device=cuda).load(torch.from_numpy(f0))
+    k = 2 * np.pi / nx
+    x = np.arange(nx)
+    amps = []
+    for _ in range(steps // 20):
+        lat.step(20)
+        _, _, uy = lat.macroscopic()
+        amps.append((uy.cpu().numpy()[:, ny // 2] * np.sin(k * x)).sum() * 2 / nx)
+    t = 20 * np.arange(1, len(amps) + 1)
+    nu = -np.polyfit(t, np.log(amps), 1)[0] / k ** 2
+    assert abs(nu - PyLB.viscosity_from_omega(omega)) / PyLB.viscosity_from_omega(omega) < 0.02

@@ -1,0 +1,105 @@
+"""The device-resident solver: fused steps, CUDA-graph replay, storage round trips,
+vector-width dispatch (row lengths that are and are not multiples of the vector
+width) and full-size properties at the benchmark's grid."""
+
+import numpy as np
+import pytest
+import torch
+
+import latticeboltzmann_gb300 as PyLB
+from oracle import d2q9 as oracle
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.mark.parametrize("storage", ["f32", "f64", "f16dev", "bf16dev"])
+@pytest.mark.parametrize("boundary", ["cavity", "periodic"])
+def test_graph_replay_equals_eager(cuda, storage, boundary):
+    a = PyLB.Lattice(96, 72, 1.6, boundary=boundary, u0=0.1, storage=storage, device=cuda)
+    b = PyLB.Lattice(96, 72, 1.6, boundary=boundary, u0=0.1, storage=storage, device=cuda)
+    replay = b.capture(10)
+    for _ in range(3):
+        replay()
+    a.step(30)
+    torch.cuda.synchronize()
+    assert a.steps_taken == b.steps_taken == 30
+    assert torch.equal(a.state, b.state)
+
+
+@pytest.mark.parametrize("storage", ["f32", "f16dev", "bf16dev"])
+@pytest.mark.parametrize("ny", [16, 17, 24, 31, 128, 200])
+def test_vector_and_scalar_paths_agree(cuda, storage, ny):
+    """Row lengths that are not multiples of the vector width take the scalar
+    kernel; both must match the float64 oracle equally well."""
+    nx = 21
+    rng = np.random.default_rng(ny)
+    rho = 1 + 0.02 * rng.standard_normal((nx, ny))
+    ux = 0.03 * rng.standard_normal((nx, ny))
+    uy = 0.03 * rng.standard_normal((nx, ny))
+    f0 = oracle.equilibrium(rho, ux, uy)
+    ref = f0.copy()
+    for _ in range(8):
+        oracle.cavity_step(ref, 1.4, 0.1)
+    lat = PyLB.Lattice(nx, ny, 1.4, boundary="cavity", u0=0.1, storage=storage, device=cuda)
+    lat.load(torch.from_numpy(f0))
+    lat.step(8)
+    err = np.abs(lat.populations(torch.float64).cpu().numpy() - ref).max()
+    tol = {"f32": 2e-6, "f16dev": 2e-4, "bf16dev": 2e-3}[storage]
+    assert err < tol, err
+
+
+def test_storage_round_trip(cuda):
+    rng = np.random.default_rng(1)
+    f = oracle.equilibrium(1 + 0.01 * rng.standard_normal((40, 48)), 0.02 * rng.standard_normal((40, 48)),
+                           0.02 * rng.standard_normal((40, 48)))
+    for storage, tol in (("f32", 1e-7), ("f16dev", 3e-6), ("bf16dev", 3e-5)):
+        lat = PyLB.Lattice(40, 48, 1.0, boundary="periodic", storage=storage, device=cuda).load(torch.from_numpy(f))
+        back = lat.populations(torch.float64).cpu().numpy()
+        assert np.abs(back - f).max() < tol, storage
+
+
+def test_equilibrium_initialisation_is_exact_at_rest(cuda):
+    lat = PyLB.Lattice(33, 20, 1.0, boundary="cavity", storage="f64", device=cuda)
+    f = lat.populations().cpu().numpy()
+    assert np.abs(f - oracle.W_I[:, None, None]).max() == 0
+    rho, ux, uy = lat.macroscopic()
+    assert float(rho.min()) == 1.0 and float(ux.abs().max()) == 0.0
+
+
+def test_bad_configuration_rejected(cuda):
+    with pytest.raises(ValueError):
+        PyLB.Lattice(1, 8, 1.0, boundary="cavity", device=cuda)
+    with pytest.raises(ValueError):
+        PyLB.Lattice(8, 8, 1.0, storage="f8", device=cuda)
+    lat = PyLB.Lattice(8, 8, 1.0, device=cuda)
+    with pytest.raises(ValueError):
+        lat.capture(3)
+    with pytest.raises(ValueError):
+        lat.load(torch.zeros(9, 8, 9))
+
+
+@pytest.mark.parametrize("storage", ["f32", "f16dev"])
+def test_full_size_cavity_properties(cuda, storage):
+    """Size-independent properties at the benchmark grid (8192^2).
+
+    * With a resting lid the rest state is an exact fixed point (bit-exact).
+    * One step from rest with a moving lid: interior nodes stay at rest, the
+      lid row gains x momentum 2 * u0/6 per interior column and u0/6 at each
+      corner column (where the side wall overrides one Ladd term), i.e.
+      (u0/3)(n-1) in total; mass and y momentum do not change.
+    """
+    n = 8192
+    lat = PyLB.Lattice(n, n, 1.7, boundary="cavity", u0=0.0, storage=storage, device=cuda)
+    s0 = lat.state.clone()
+    lat.step(2)
+    assert torch.equal(lat.state, s0)
+    del s0, lat
+    u0 = 0.1
+    lat = PyLB.Lattice(n, n, 1.7, boundary="cavity", u0=u0, storage=storage, device=cuda)
+    m0 = float(lat.mass_momentum()[0])
+    lat.step(1)
+    mass, px, py = lat.mass_momentum().cpu().numpy()
+    rel = 1e-6 if storage == "f32" else 2e-3
+    assert abs(mass - m0) < 1e-3
+    assert abs(px - u0 / 3 * (n - 1)) < rel * u0 / 3 * n
+    assert abs(py) < 1e-3
