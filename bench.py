@@ -42,7 +42,7 @@ UNIT = "MLUPS"
 def parse(argv=None):
     p = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
     p.add_argument("--gpus", type=int, default=1)
-    p.add_argument("--steps", type=int, default=50)
+    p.add_argument("--steps", type=int, default=1000)
     p.add_argument("--warmup", type=int, default=5)
     p.add_argument("--impl", choices=["ours", "reference"], default="ours")
     p.add_argument("--nx", type=int, default=8192)
@@ -55,6 +55,9 @@ def parse(argv=None):
     p.add_argument("--cpu-seconds", type=float, default=10.0, help="bound of the CPU-baseline sample")
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-e2e", action="store_true")
+    p.add_argument("--kernel", choices=["auto", "register", "pipelined"], default="auto",
+                   help="step kernel: shared-memory pipelined, register/shuffle, or automatic choice")
+    p.add_argument("--stages", type=int, default=0, help="pipeline stages (0: library default)")
     return p.parse_args(argv)
 
 
@@ -283,7 +286,11 @@ def run_ours(args):
     dev = torch.device("cuda", d.local_rank)
     torch.cuda.set_device(dev)
     import latticeboltzmann_gb300 as PyLB
+    from latticeboltzmann_gb300 import _lib
 
+    _lib.set_tuning(_lib.TUNE_KERNEL, _lib.KERNELS[args.kernel])
+    if args.stages:
+        _lib.set_tuning(_lib.TUNE_STAGES, args.stages)
     lat = PyLB.Lattice(args.nx, args.ny, args.omega, boundary=args.boundary, u0=args.u0, storage=args.storage,
                        device=dev)
     stream = torch.cuda.current_stream(dev)
@@ -304,6 +311,7 @@ def run_ours(args):
     torch.cuda.synchronize(dev)
     d.barrier()
     clk = clocks.stop() if d.rank == 0 else None
+    _lib.device_status()  # raises if a bounded device-side wait gave up
     per_launch_ms = [ev[i].elapsed_time(ev[i + 1]) for i in range(args.steps)]
     total_s = ev[0].elapsed_time(ev[-1]) / 1e3
     mlups, t_max = aggregate_mlups(lat.cells, args.steps, total_s, d, dev)

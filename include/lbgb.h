@@ -126,6 +126,28 @@ LBGB_API int lbgb_mass_momentum(const void *f, int64_t n, int64_t chan_stride, i
 LBGB_API int lbgb_convert(const void *src, int src_dtype, int64_t src_stride, void *dst,
                  int dst_dtype, int64_t dst_stride, int64_t n, void *stream);
 
+/* Launch tuning (process-wide; used by the autotuner and the tests).
+ *   LBGB_TUNE_KERNEL          0 auto, 1 register kernel, 2 pipelined kernel
+ *   LBGB_TUNE_STAGES          shared-memory stages of the pipelined kernel
+ *   LBGB_TUNE_WAIT_LIMIT      tries per bounded device-side wait
+ *   LBGB_TUNE_PIPE_MIN_CELLS  auto: lattices with fewer cells use the register kernel
+ *   LBGB_TUNE_TEST_STALL_PRODUCER  test hook: the pipelined kernel's producer
+ *                             delivers nothing, so its consumers' bounded
+ *                             waits expire (exercises the timeout path)
+ * No counterpart in the reference (it has no GPU path). */
+#define LBGB_TUNE_KERNEL 0
+#define LBGB_TUNE_STAGES 1
+#define LBGB_TUNE_WAIT_LIMIT 2
+#define LBGB_TUNE_PIPE_MIN_CELLS 3
+#define LBGB_TUNE_TEST_STALL_PRODUCER 4
+LBGB_API int lbgb_set_tuning(int key, long long value);
+LBGB_API long long lbgb_get_tuning(int key);
+
+/* Synchronizes the device and reports its status word: LBGB_OK, or
+ * LBGB_ETIMEOUT if a bounded wait inside a pipelined kernel gave up since
+ * the last reset (reset != 0 clears it).  No counterpart in the reference. */
+LBGB_API int lbgb_device_status(int reset);
+
 #ifdef __cplusplus
 }
 #endif

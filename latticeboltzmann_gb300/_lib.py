@@ -53,7 +53,13 @@ SIGNATURES = {
     "lbgb_mass_momentum_workspace_bytes": (_SZ, []),
     "lbgb_mass_momentum": (_I, [_P, _I64, _I64, _I, _P, _P, _SZ, _P]),
     "lbgb_convert": (_I, [_P, _I, _I64, _P, _I, _I64, _I64, _P]),
+    "lbgb_set_tuning": (_I, [_I, ctypes.c_longlong]),
+    "lbgb_get_tuning": (ctypes.c_longlong, [_I]),
+    "lbgb_device_status": (_I, [_I]),
 }
+
+TUNE_KERNEL, TUNE_STAGES, TUNE_WAIT_LIMIT, TUNE_PIPE_MIN_CELLS, TUNE_TEST_STALL_PRODUCER = 0, 1, 2, 3, 4
+KERNELS = {"auto": 0, "register": 1, "pipelined": 2}
 
 
 def load(path=LIB_PATH):
@@ -101,3 +107,16 @@ def check(rc, what=""):
 
 def call(name, *args):
     check(getattr(load(), name)(*args), name)
+
+
+def set_tuning(key, value):
+    call("lbgb_set_tuning", key, int(value))
+
+
+def get_tuning(key):
+    return load().lbgb_get_tuning(key)
+
+
+def device_status(reset=True):
+    """Synchronize and raise LBGBTimeout if a bounded device-side wait gave up."""
+    check(load().lbgb_device_status(1 if reset else 0), "lbgb_device_status")

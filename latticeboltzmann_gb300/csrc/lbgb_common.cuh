@@ -52,22 +52,18 @@ template <> struct Codec<LBGB_F64> {
 template <> struct Codec<LBGB_F16DEV> {
     using raw = unsigned short;
     using real = float;
-    static __device__ __forceinline__ real dec(raw x, int i) {
-        return __half2float(__ushort_as_half(x)) + wgt<float>(i);
-    }
-    static __device__ __forceinline__ raw enc(real x, int i) {
-        return __half_as_ushort(__float2half_rn(x - wgt<float>(i)));
-    }
+    static __device__ __forceinline__ real dec_h(raw x) { return __half2float(__ushort_as_half(x)); }
+    static __device__ __forceinline__ raw enc_h(real h) { return __half_as_ushort(__float2half_rn(h)); }
+    static __device__ __forceinline__ real dec(raw x, int i) { return dec_h(x) + wgt<float>(i); }
+    static __device__ __forceinline__ raw enc(real x, int i) { return enc_h(x - wgt<float>(i)); }
 };
 template <> struct Codec<LBGB_BF16DEV> {
     using raw = unsigned short;
     using real = float;
-    static __device__ __forceinline__ real dec(raw x, int i) {
-        return __bfloat162float(__ushort_as_bfloat16(x)) + wgt<float>(i);
-    }
-    static __device__ __forceinline__ raw enc(real x, int i) {
-        return __bfloat16_as_ushort(__float2bfloat16_rn(x - wgt<float>(i)));
-    }
+    static __device__ __forceinline__ real dec_h(raw x) { return __bfloat162float(__ushort_as_bfloat16(x)); }
+    static __device__ __forceinline__ raw enc_h(real h) { return __bfloat16_as_ushort(__float2bfloat16_rn(h)); }
+    static __device__ __forceinline__ real dec(raw x, int i) { return dec_h(x) + wgt<float>(i); }
+    static __device__ __forceinline__ raw enc(real x, int i) { return enc_h(x - wgt<float>(i)); }
 };
 
 // ---------------------------------------------------------------- memory
@@ -121,12 +117,15 @@ __device__ __forceinline__ void stv(RAW *p, const RAW (&v)[V]) {
 //   f_i += omega (w_i rho (1 + 3 c.u + 9/2 (c.u)^2 - 3/2 u^2) - f_i),
 // in the formulation of c/d2q9.h:59-81,121-131: rho = sum f, u = sum c f / rho,
 // ux, uy scaled by 3, uu = (ux^2 + uy^2)/6, feq_i = w_i rho (1 + cu + cu^2/2 - uu).
+__device__ __forceinline__ float recip(float x) { return __frcp_rn(x); }
+__device__ __forceinline__ double recip(double x) { return __drcp_rn(x); }
+
 template <class R>
 __device__ __forceinline__ void bgk_collide(R (&f)[9], R omega, R &rho_out, R &ux_out, R &uy_out) {
     R rho = f[0];
 #pragma unroll
     for (int i = 1; i < 9; ++i) rho += f[i];
-    const R inv = R(1) / rho;
+    const R inv = recip(rho);
     R ux = (f[1] - f[3] + f[5] - f[6] - f[7] + f[8]) * inv;
     R uy = (f[2] - f[4] + f[5] + f[6] - f[7] - f[8]) * inv;
     ux_out = ux;
@@ -180,6 +179,56 @@ __device__ __forceinline__ void equilibrium1(R rho, R ux, R uy, R (&feq)[9]) {
     feq[6] = w5 * (base + cu6 + h6);
     feq[7] = w5 * (base - cu5 + h5);
     feq[8] = w5 * (base - cu6 + h6);
+}
+
+// ---------------------------------------------------------------- conservation
+// BGK conserves mass exactly; rounding the nine relaxed values does not, and in
+// a slowly varying flow the same rounding repeats step after step and adds up
+// (the reference's own float32 path drifts by ~1e-2 in 500 steps of a 48x40
+// box with resting walls).  The rest population is therefore written last as
+// the node's pre-collision mass minus the eight stored moving populations, so
+// that the mass survives the collision up to the rounding of that one value:
+//  * FP32: f_0' = f_0 + sum_{i>0} (f_i - f_i'), the relaxed amounts of the
+//    moving populations summed as small numbers (exactly zero at rest, so
+//    the rest state stays a fixed point; resting-wall drift ~5e-6 instead
+//    of ~1e-2, for 16 additions);
+//  * half deviations: h_0 = sum_i h_i(before) - sum_{i>0} h_i(stored), the
+//    stored values decoded back (drift 7e-5 instead of 3e-2; moving-lid mass
+//    error against FP64 5x smaller);
+//  * bfloat16 deviations are rounded as they are: with 8 significant bits
+//    the correction made the moving-lid mass error larger, not smaller.
+template <int DT>
+__device__ __forceinline__ void collide_encode(typename Codec<DT>::real (&f)[9], typename Codec<DT>::real omega,
+                                               typename Codec<DT>::raw (&out)[9]) {
+    using C = Codec<DT>;
+    using real = typename C::real;
+    if constexpr (DT == LBGB_F32) {
+        real pre[9];
+#pragma unroll
+        for (int i = 0; i < 9; ++i) pre[i] = f[i];
+        bgk_collide(f, omega);
+        real d = pre[1] - f[1];
+#pragma unroll
+        for (int i = 2; i < 9; ++i) d += pre[i] - f[i];
+        f[0] = pre[0] + d;
+#pragma unroll
+        for (int i = 0; i < 9; ++i) out[i] = f[i];
+    } else if constexpr (DT == LBGB_F16DEV) {
+        real dm = f[0] - wgt<real>(0);
+#pragma unroll
+        for (int i = 1; i < 9; ++i) dm += f[i] - wgt<real>(i);
+        bgk_collide(f, omega);
+#pragma unroll
+        for (int i = 1; i < 9; ++i) {
+            out[i] = C::enc(f[i], i);
+            dm -= C::dec_h(out[i]);
+        }
+        out[0] = C::enc_h(dm);
+    } else {
+        bgk_collide(f, omega);
+#pragma unroll
+        for (int i = 0; i < 9; ++i) out[i] = C::enc(f[i], i);
+    }
 }
 
 // ---------------------------------------------------------------- host side

@@ -74,26 +74,23 @@ __global__ void k_collide(typename Codec<DT>::raw *__restrict__ f, int64_t n, in
 #pragma unroll
                 for (int j = 0; j < V; ++j) v[i][j] = j < cnt ? C::dec(f[i * cs + c0 + j], i) : real(1.0 / 9.0);
         }
+        raw out[9][V];
 #pragma unroll
         for (int j = 0; j < V; ++j) {
             real x[9];
+            raw r[9];
 #pragma unroll
             for (int i = 0; i < 9; ++i) x[i] = v[i][j];
-            bgk_collide(x, omega);
+            collide_encode<DT>(x, omega, r);
 #pragma unroll
-            for (int i = 0; i < 9; ++i) v[i][j] = x[i];
+            for (int i = 0; i < 9; ++i) out[i][j] = r[i];
         }
         if (cnt == V) {
 #pragma unroll
-            for (int i = 0; i < 9; ++i) {
-                raw r[V];
-#pragma unroll
-                for (int j = 0; j < V; ++j) r[j] = C::enc(v[i][j], i);
-                stv<raw, V>(f + i * cs + c0, r);
-            }
+            for (int i = 0; i < 9; ++i) stv<raw, V>(f + i * cs + c0, out[i]);
         } else {
             for (int i = 0; i < 9; ++i)
-                for (int j = 0; j < cnt; ++j) f[i * cs + c0 + j] = C::enc(v[i][j], i);
+                for (int j = 0; j < cnt; ++j) f[i * cs + c0 + j] = out[i][j];
         }
     }
 }

@@ -1,0 +1,257 @@
+// Warp-specialised, shared-memory-pipelined variant of the pull step.
+//
+// One persistent CTA per SM.  Warp NCW (the producer, one thread) streams the
+// source data of each tile into a ring of shared-memory stages with bulk
+// asynchronous copies (cp.async.bulk, completion counted on an mbarrier);
+// warps 0..NCW-1 (the consumers) gather every population of their cells from
+// the stage, release it, collide and store straight to global memory.
+//
+// A tile is L = NCW*32*NC consecutive cells of one row k (NC = cells per
+// consumer thread = one 16-byte vector).  For channel i the producer copies
+// row k - cx_i (or, at a cavity side wall, the opposite channel of row k),
+// columns [l0 - HALO, l0 + L + HALO) clipped to the row, HALO = one 16-byte
+// vector: the one-cell neighbours along l that the cy != 0 channels pull are
+// then in shared memory.  Only the cells of the first and last column of a
+// row fetch their wrap-around or wall values from global memory.
+//
+// With ~37 KB per stage and 5 stages about 185 KB per SM are in flight,
+// independent of how long the consumers spend in the collision.
+//
+// Every mbarrier wait is bounded.  A wait that gives up records a code in a
+// device-side status word and makes its warp leave the tile loop; the
+// producer then waits (bounded again) for the copies it has issued before it
+// exits, so no copy can land in the shared memory of a finished CTA.
+#pragma once
+
+#include "lbgb_common.cuh"
+
+namespace lbgb {
+
+__device__ __forceinline__ uint32_t smem_addr(const void *p) {
+    return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+__device__ __forceinline__ void mbar_init(uint64_t *bar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void fence_mbar_init() {
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+__device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t *bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)), "r"(bytes)
+                 : "memory");
+}
+__device__ __forceinline__ void mbar_arrive(uint64_t *bar) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_addr(bar)) : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity) {
+    uint32_t done;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(done)
+        : "r"(smem_addr(bar)), "r"(parity)
+        : "memory");
+    return done != 0;
+}
+// Waits for the phase of the given parity; false if `limit` tries pass first.
+__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity, long long limit) {
+    for (long long n = 0; n < limit; ++n)
+        if (mbar_try_wait(bar, parity)) return true;
+    return false;
+}
+// Bulk asynchronous copy global -> shared, completion counted on `bar`.
+__device__ __forceinline__ void bulk_copy_g2s(void *dst, const void *src, uint32_t bytes, uint64_t *bar) {
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                     smem_addr(dst)),
+                 "l"(src), "r"(bytes), "r"(smem_addr(bar))
+                 : "memory");
+}
+
+// device-side status word of the pipelined kernels (0 = fine)
+__device__ int g_pipe_status;
+
+constexpr int PIPE_CONSUMER_WARPS = 8;
+constexpr long long PIPE_DRAIN_LIMIT = 1ll << 22;
+
+__device__ __forceinline__ void pipe_report(int code) { atomicCAS(&g_pipe_status, 0, code); }
+
+template <class RAW>
+struct PipeGeom {
+    static constexpr int NC = 16 / (int)sizeof(RAW);           // cells per consumer thread
+    static constexpr int HALO = NC;                            // one 16-byte vector each side
+    static constexpr int L = PIPE_CONSUMER_WARPS * 32 * NC;    // cells per tile
+    static constexpr int SLOT = L + 2 * HALO;                  // elements per channel slot
+    static constexpr size_t STAGE_BYTES = 9ull * SLOT * sizeof(RAW);
+};
+
+template <int DT, int BC, bool COLLIDE>
+__global__ void __launch_bounds__((PIPE_CONSUMER_WARPS + 1) * 32, 1)
+k_step_pipe(const typename Codec<DT>::raw *__restrict__ src, typename Codec<DT>::raw *__restrict__ dst, int nx,
+            int ny, int tiles_per_row, int total_tiles, int stages, typename Codec<DT>::real omega,
+            typename Codec<DT>::real u0, long long wait_limit, int stall_producer) {
+    using C = Codec<DT>;
+    using raw = typename C::raw;
+    using real = typename C::real;
+    using G = PipeGeom<raw>;
+    constexpr int NC = G::NC, HALO = G::HALO, L = G::L, SLOT = G::SLOT, NCW = PIPE_CONSUMER_WARPS;
+
+    extern __shared__ __align__(128) unsigned char smem[];
+    raw *slots = reinterpret_cast<raw *>(smem);
+    uint64_t *full = reinterpret_cast<uint64_t *>(smem + (size_t)stages * G::STAGE_BYTES);
+    uint64_t *empty = full + stages;
+
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const size_t cs = (size_t)nx * ny;
+
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < stages; ++s) {
+            mbar_init(&full[s], 1);
+            mbar_init(&empty[s], NCW * 32);
+        }
+        fence_mbar_init();
+    }
+    __syncthreads();
+
+    if (warp == NCW) {
+        // ------------------------------------------------------------ producer
+        if (lane != 0) return;
+        // test hook for the failure path: a producer that never delivers lets
+        // the consumers' bounded waits run out (nothing is in flight)
+        if (stall_producer) return;
+        int issued = 0;
+        for (int tile = blockIdx.x; tile < total_tiles; tile += gridDim.x) {
+            const int s = issued % stages;
+            const uint32_t ph = (uint32_t)(issued / stages) & 1u;
+            if (!mbar_wait(&empty[s], ph ^ 1u, wait_limit)) {
+                pipe_report(1);
+                break;
+            }
+            const int k = tile / tiles_per_row;
+            const int l0 = (tile - k * tiles_per_row) * L;
+            const int c0 = max(l0 - HALO, 0), c1 = min(l0 + L + HALO, ny);
+            const uint32_t bytes = (uint32_t)(c1 - c0) * (uint32_t)sizeof(raw);
+            mbar_arrive_expect_tx(&full[s], 9u * bytes);
+            raw *stage = slots + (size_t)s * 9 * SLOT;
+#pragma unroll
+            for (int i = 0; i < 9; ++i) {
+                int ch = i, row = k - cx(i);
+                if (BC == LBGB_PERIODIC) {
+                    row = row < 0 ? row + nx : (row >= nx ? row - nx : row);
+                } else if (row < 0 || row >= nx) {
+                    ch = opp(i);
+                    row = k;
+                }
+                bulk_copy_g2s(stage + i * SLOT + (c0 - (l0 - HALO)), src + (size_t)ch * cs + (size_t)row * ny + c0,
+                              bytes, &full[s]);
+            }
+            ++issued;
+        }
+        // drain: the copies of the last stages issued must land before exit
+        for (int j = max(0, issued - stages); j < issued; ++j)
+            mbar_wait(&full[j % stages], (uint32_t)(j / stages) & 1u, PIPE_DRAIN_LIMIT);
+        return;
+    }
+
+    // ---------------------------------------------------------------- consumers
+    const int t = threadIdx.x;  // 0 .. NCW*32-1
+    int it = 0;
+    for (int tile = blockIdx.x; tile < total_tiles; tile += gridDim.x, ++it) {
+        const int s = it % stages;
+        const uint32_t ph = (uint32_t)(it / stages) & 1u;
+        if (!mbar_wait(&full[s], ph, wait_limit)) {
+            pipe_report(2);
+            break;
+        }
+        const int k = tile / tiles_per_row;
+        const int l0 = (tile - k * tiles_per_row) * L;
+        const int c = l0 + t * NC;  // first cell of this thread
+        const bool act = c < ny;
+        const raw *stage = slots + (size_t)s * 9 * SLOT;
+        const bool wl = (BC == LBGB_CAVITY) && k == 0;
+        const bool wr = (BC == LBGB_CAVITY) && k == nx - 1;
+        real v[9][NC];
+        if (act) {
+#pragma unroll
+            for (int i = 0; i < 9; ++i) {
+                const raw *sl = stage + i * SLOT + HALO + t * NC;
+                raw r[NC];
+                {
+                    const uint4 x = *reinterpret_cast<const uint4 *>(sl);
+                    memcpy(r, &x, 16);
+                }
+#pragma unroll
+                for (int j = 0; j < NC; ++j) v[i][j] = C::dec(r[j], i);
+                const bool wall = (cx(i) > 0 && wl) || (cx(i) < 0 && wr);
+                if (wall || cy(i) == 0) continue;
+                int row = k - cx(i);
+                if (BC == LBGB_PERIODIC) row = row < 0 ? row + nx : (row >= nx ? row - nx : row);
+                if (cy(i) > 0) {
+                    real prev = 0;
+                    if (c > 0)
+                        prev = C::dec(sl[-1], i);
+                    else if (BC == LBGB_PERIODIC)
+                        prev = C::dec(ld1(src + (size_t)i * cs + (size_t)row * ny + (ny - 1)), i);
+#pragma unroll
+                    for (int j = NC - 1; j > 0; --j) v[i][j] = v[i][j - 1];
+                    v[i][0] = prev;
+                } else {
+                    real next = 0;
+                    if (c + NC < ny)
+                        next = C::dec(sl[NC], i);
+                    else if (BC == LBGB_PERIODIC)
+                        next = C::dec(ld1(src + (size_t)i * cs + (size_t)row * ny), i);
+#pragma unroll
+                    for (int j = 0; j < NC - 1; ++j) v[i][j] = v[i][j + 1];
+                    v[i][NC - 1] = next;
+                }
+            }
+        }
+        mbar_arrive(&empty[s]);  // this thread is done with the stage
+        if (!act) continue;
+
+        if (BC == LBGB_CAVITY) {
+            auto g = [&](int ch, int row, int l) { return C::dec(ld1(src + (size_t)ch * cs + (size_t)row * ny + l), ch); };
+            if (c == 0) {
+                v[CN][0] = g(CS, k, 0);
+                v[CNE][0] = g(CSW, k, 0);
+                v[CNW][0] = g(CSE, k, 0);
+            }
+            if (c + NC == ny) {
+                const int T = ny - 1;
+                const int kw = (k == 0) ? nx - 1 : k - 1;
+                const int ke = (k == nx - 1) ? 0 : k + 1;
+                const real gN = g(CN, k, T), gNW = g(CNW, k, T), gNE = g(CNE, k, T);
+                const real rho_lid = gNW + gN + gNE + g(CNW, ke, T - 1) + g(CN, k, T - 1) + g(CNE, kw, T - 1) +
+                                     g(CW, ke, T) + g(C0, k, T) + g(CE, kw, T);
+                const real lid = (real(6) * real(1.0 / 36.0)) * rho_lid * u0;
+                v[CS][NC - 1] = gN;
+                v[CSE][NC - 1] = (k == 0) ? gNW : gNW + lid;
+                v[CSW][NC - 1] = (k == nx - 1) ? gNE : gNE - lid;
+            }
+        }
+
+        raw out[9][NC];
+        if (COLLIDE) {
+#pragma unroll
+            for (int j = 0; j < NC; ++j) {
+                real f[9];
+                raw r[9];
+#pragma unroll
+                for (int i = 0; i < 9; ++i) f[i] = v[i][j];
+                collide_encode<DT>(f, omega, r);
+#pragma unroll
+                for (int i = 0; i < 9; ++i) out[i][j] = r[i];
+            }
+        } else {
+#pragma unroll
+            for (int i = 0; i < 9; ++i)
+#pragma unroll
+                for (int j = 0; j < NC; ++j) out[i][j] = C::enc(v[i][j], i);
+        }
+#pragma unroll
+        for (int i = 0; i < 9; ++i) stv<raw, NC>(dst + (size_t)i * cs + (size_t)k * ny + c, out[i]);
+    }
+}
+
+}  // namespace lbgb

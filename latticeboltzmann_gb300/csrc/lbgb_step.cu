@@ -19,9 +19,11 @@
 //    (l = 0, l = ny-1) belong to single lanes, which patch their values with
 //    a few scalar loads, including the lid density that the reference reads
 //    across the periodic seam at the two lid corners.
+#include <limits.h>
 #include <stdio.h>
 
 #include "lbgb_common.cuh"
+#include "lbgb_pipe.cuh"
 
 namespace lbgb {
 
@@ -99,8 +101,13 @@ __device__ __forceinline__ void pull_channel(typename C::real (&o)[V], const typ
     if (cy(CH) < 0) shift_from_above<C, V, BC>(o, src, cs, ny, CH, krow, l0, lane, act);
 }
 
+// Resident blocks per SM the register allocation must allow: the 8-cell
+// 16-bit variant needs ~110 registers, the others ~80.
+template <int DT, int V>
+constexpr int min_blocks() { return (sizeof(typename Codec<DT>::raw) == 2 && V == 8) ? 2 : 3; }
+
 template <int DT, int BC, bool COLLIDE, int V>
-__global__ void __launch_bounds__(256)
+__global__ void __launch_bounds__(256, min_blocks<DT, V>())
 k_step(const typename Codec<DT>::raw *__restrict__ src, typename Codec<DT>::raw *__restrict__ dst, int nx,
        int ny, int segs, long long tasks, typename Codec<DT>::real omega, typename Codec<DT>::real u0) {
     using C = Codec<DT>;
@@ -161,25 +168,27 @@ k_step(const typename Codec<DT>::raw *__restrict__ src, typename Codec<DT>::raw 
             }
         }
 
+        raw out[9][V];
         if (COLLIDE) {
 #pragma unroll
             for (int j = 0; j < V; ++j) {
                 real f[9];
+                raw r[9];
 #pragma unroll
                 for (int i = 0; i < 9; ++i) f[i] = v[i][j];
-                bgk_collide(f, omega);
+                collide_encode<DT>(f, omega, r);
 #pragma unroll
-                for (int i = 0; i < 9; ++i) v[i][j] = f[i];
+                for (int i = 0; i < 9; ++i) out[i][j] = r[i];
             }
+        } else {
+#pragma unroll
+            for (int i = 0; i < 9; ++i)
+#pragma unroll
+                for (int j = 0; j < V; ++j) out[i][j] = C::enc(v[i][j], i);
         }
         if (act) {
 #pragma unroll
-            for (int i = 0; i < 9; ++i) {
-                raw r[V];
-#pragma unroll
-                for (int j = 0; j < V; ++j) r[j] = C::enc(v[i][j], i);
-                stv<raw, V>(dst + (size_t)i * cs + (size_t)k * ny + l0, r);
-            }
+            for (int i = 0; i < 9; ++i) stv<raw, V>(dst + (size_t)i * cs + (size_t)k * ny + l0, out[i]);
         }
     }
 }
@@ -213,13 +222,70 @@ static int launch_v(const void *src, void *dst, int nx, int ny, double omega, do
     return check_launch("k_step");
 }
 
-// Widest vector width that divides ny and keeps every row start aligned.
+// ---------------------------------------------------------------- tuning
+struct Tuning {
+    long long kernel = 0;                // 0 auto, 1 register kernel, 2 pipelined kernel
+    long long stages = 2;                // pipeline depth (shared-memory stages)
+    long long wait_limit = 1ll << 22;    // tries per bounded mbarrier wait
+    long long pipe_min_cells = 1 << 16;  // auto: smaller lattices use the register kernel
+    long long stall_producer = 0;        // test hook: the producer delivers nothing
+};
+static Tuning g_tune;
+
+static int max_dyn_smem() {
+    static int v = 0;
+    if (v == 0) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&v, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+        if (v <= 0) v = 48 * 1024;
+    }
+    return v;
+}
+
+template <int DT, int BC, bool COLLIDE>
+static int launch_pipe(const void *src, void *dst, int nx, int ny, double omega, double u0, cudaStream_t s) {
+    using raw = typename Codec<DT>::raw;
+    using G = PipeGeom<raw>;
+    const long long tpr = (ny + G::L - 1) / G::L;
+    const long long total = (long long)nx * tpr;
+    const int smax = max_dyn_smem();
+    const int fit = (int)((smax - 256) / (G::STAGE_BYTES + 16));
+    int stages = (int)g_tune.stages;
+    if (stages > fit) stages = fit;
+    if (stages < 2 || total > INT_MAX) return 1;  // caller falls back to the register kernel
+    const size_t smem = (size_t)stages * G::STAGE_BYTES + 16 * (size_t)stages;
+    static bool attr = false;  // one per template instance
+    if (!attr) {
+        cudaError_t e = cudaFuncSetAttribute(k_step_pipe<DT, BC, COLLIDE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             smax);
+        if (e != cudaSuccess) {
+            set_error("k_step_pipe: cannot reserve %d bytes of shared memory: %s", smax, cudaGetErrorString(e));
+            return LBGB_ECUDA;
+        }
+        attr = true;
+    }
+    const int grid = (int)(total < sm_count() ? total : sm_count());
+    k_step_pipe<DT, BC, COLLIDE><<<grid, (PIPE_CONSUMER_WARPS + 1) * 32, smem, s>>>(
+        static_cast<const raw *>(src), static_cast<raw *>(dst), nx, ny, (int)tpr, (int)total, stages,
+        (typename Codec<DT>::real)omega, (typename Codec<DT>::real)u0, g_tune.wait_limit, (int)g_tune.stall_producer);
+    return check_launch("k_step_pipe");
+}
+
+// Pipelined kernel for lattices whose rows hold whole 16-byte vectors (large
+// lattices, or when forced); otherwise the register kernel with the widest
+// vector width that divides ny and keeps every row start aligned.
 template <int DT, int BC, bool COLLIDE>
 static int launch(const void *src, void *dst, int nx, int ny, double omega, double u0, cudaStream_t s) {
     constexpr int VW = 16 / sizeof(typename Codec<DT>::raw);
-    const size_t al = VW * sizeof(typename Codec<DT>::raw);
-    if (ny % VW == 0 && aligned(src, al) && aligned(dst, al))
-        return launch_v<DT, BC, COLLIDE, VW>(src, dst, nx, ny, omega, u0, s);
+    const bool vec_ok = ny % VW == 0 && aligned(src, 16) && aligned(dst, 16);
+    const bool want_pipe = g_tune.kernel == 2 ||
+                           (g_tune.kernel == 0 && (long long)nx * ny >= g_tune.pipe_min_cells);
+    if (vec_ok && want_pipe) {
+        const int rc = launch_pipe<DT, BC, COLLIDE>(src, dst, nx, ny, omega, u0, s);
+        if (rc <= 0) return rc;
+    }
+    if (vec_ok) return launch_v<DT, BC, COLLIDE, VW>(src, dst, nx, ny, omega, u0, s);
     return launch_v<DT, BC, COLLIDE, 1>(src, dst, nx, ny, omega, u0, s);
 }
 
@@ -312,5 +378,68 @@ extern "C" int lbgb_run_fused(void *a, void *b, int nx, int ny, int boundary, do
         dst = t;
     }
     if (which) *which = (src == a) ? 0 : 1;
+    return LBGB_OK;
+}
+
+extern "C" int lbgb_set_tuning(int key, long long value) {
+    switch (key) {
+    case LBGB_TUNE_KERNEL:
+        if (value < 0 || value > 2) break;
+        g_tune.kernel = value;
+        return LBGB_OK;
+    case LBGB_TUNE_STAGES:
+        if (value < 2 || value > 64) break;
+        g_tune.stages = value;
+        return LBGB_OK;
+    case LBGB_TUNE_WAIT_LIMIT:
+        if (value < 1) break;
+        g_tune.wait_limit = value;
+        return LBGB_OK;
+    case LBGB_TUNE_PIPE_MIN_CELLS:
+        if (value < 0) break;
+        g_tune.pipe_min_cells = value;
+        return LBGB_OK;
+    case LBGB_TUNE_TEST_STALL_PRODUCER:
+        g_tune.stall_producer = value ? 1 : 0;
+        return LBGB_OK;
+    default:
+        set_error("lbgb_set_tuning: unknown key %d", key);
+        return LBGB_EINVAL;
+    }
+    set_error("lbgb_set_tuning: value %lld out of range for key %d", value, key);
+    return LBGB_EINVAL;
+}
+
+extern "C" long long lbgb_get_tuning(int key) {
+    switch (key) {
+    case LBGB_TUNE_KERNEL: return g_tune.kernel;
+    case LBGB_TUNE_STAGES: return g_tune.stages;
+    case LBGB_TUNE_WAIT_LIMIT: return g_tune.wait_limit;
+    case LBGB_TUNE_PIPE_MIN_CELLS: return g_tune.pipe_min_cells;
+    case LBGB_TUNE_TEST_STALL_PRODUCER: return g_tune.stall_producer;
+    }
+    return -1;
+}
+
+extern "C" int lbgb_device_status(int reset) {
+    cudaError_t e = cudaDeviceSynchronize();
+    if (e != cudaSuccess) {
+        set_error("lbgb_device_status: %s", cudaGetErrorString(e));
+        return LBGB_ECUDA;
+    }
+    int v = 0;
+    e = cudaMemcpyFromSymbol(&v, g_pipe_status, sizeof(int));
+    if (e == cudaSuccess && reset) {
+        const int zero = 0;
+        e = cudaMemcpyToSymbol(g_pipe_status, &zero, sizeof(int));
+    }
+    if (e != cudaSuccess) {
+        set_error("lbgb_device_status: %s", cudaGetErrorString(e));
+        return LBGB_ECUDA;
+    }
+    if (v != 0) {
+        set_error("a bounded device-side wait gave up (site %d)", v);
+        return LBGB_ETIMEOUT;
+    }
     return LBGB_OK;
 }

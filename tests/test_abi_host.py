@@ -17,7 +17,7 @@ ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 
 def header_symbols():
     src = open(os.path.join(ROOT, "include", "lbgb.h")).read()
-    return re.findall(r"^LBGB_API\s+\w+\s+(lbgb_\w+)\s*\(", src, flags=re.M)
+    return re.findall(r"^LBGB_API\s+[\w\s*]*?\b(lbgb_\w+)\s*\(", src, flags=re.M)
 
 
 @pytest.fixture(scope="module")

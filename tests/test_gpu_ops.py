@@ -65,7 +65,9 @@ def test_collide_ragged_and_strided(cuda, n, dtype):
         oracle.collide_cxx(ref, 1.3)
     g = T(f, cuda)
     PyLB.collide(g, 1.3)
-    tol = 1e-15 if dtype == np.float64 else 3e-7
+    # float32: the rest population is written as rho - sum of the others,
+    # a few ulps of 1 away from the native kernel's value
+    tol = 1e-15 if dtype == np.float64 else 6e-7
     if n:
         assert np.abs(g.cpu().numpy() - ref).max() < tol
     # channel rows spaced wider than N (a view into a bigger buffer), odd stride

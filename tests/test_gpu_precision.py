@@ -69,20 +69,31 @@ def test_f32_error_bound(cuda, ref64, ref32_error):
     assert err <= 1.5 * ref32_error, (err, ref32_error)
 
 
-@pytest.mark.parametrize("storage,tol", [("f16dev", 2e-3), ("bf16dev", 1.5e-2)])
-def test_16bit_deviation_storage_error_bound(cuda, ref64, storage, tol):
+@pytest.mark.parametrize("storage,tol,mtol", [("f16dev", 2e-3, 0.1), ("bf16dev", 1.5e-2, 0.3)])
+def test_16bit_deviation_storage_error_bound(cuda, ref64, storage, tol, mtol):
+    """16-bit deviation storage: velocity error and mass drift against float64.
+
+    The reference's moving lid injects mass (0.70 in this run); the 16-bit runs
+    must reproduce that drift within 10% (half, whose rest population absorbs
+    each node's rounding residual; CPU emulation: 5%) or 30% (bfloat16,
+    rounded as is; CPU emulation: 21%)."""
     lat = run(storage, cuda)
     f = lat.populations(torch.float64).cpu().numpy()
     err = rel_l2_u(f, ref64)
     assert err <= tol, (storage, err)
-    # mass drift of the 16-bit run tracks the float64 run's (the lid injects mass)
     m_ref = ref64.sum() - NX * NY
     m = float(lat.mass_momentum()[0]) - NX * NY
-    assert abs(m - m_ref) <= 0.05 * abs(m_ref) + 1e-3
+    assert abs(m - m_ref) <= mtol * abs(m_ref), (m, m_ref)
 
 
 @pytest.mark.parametrize("storage", ["f32", "f16dev", "bf16dev"])
 def test_resting_walls_conserve_mass(cuda, storage):
+    """With resting walls the cavity conserves mass exactly in exact arithmetic.
+
+    The reference's own float32 arithmetic drifts by about 1e-2 here (numpy
+    order) or 1.6e-3 (native C++ order); the moment-preserving store keeps
+    the drift at the rounding of one population per node and step.
+    """
     lat = PyLB.Lattice(48, 40, 1.2, boundary="cavity", u0=0.0, storage=storage, device=cuda)
     rng = np.random.default_rng(3)
     rho = torch.from_numpy(1 + 0.01 * rng.standard_normal((48, 40))).to(cuda)
@@ -90,7 +101,8 @@ def test_resting_walls_conserve_mass(cuda, storage):
     m0 = float(lat.mass_momentum()[0])
     lat.step(500)
     m1 = float(lat.mass_momentum()[0])
-    tol = {"f32": 2e-3, "f16dev": 2e-2, "bf16dev": 0.2}[storage]
+    # CPU emulation of the same arithmetic: f32 5e-6, f16dev 7e-5, bf16dev 1.9e-2
+    tol = {"f32": 1e-4, "f16dev": 1e-3, "bf16dev": 4e-2}[storage]
     assert abs(m1 - m0) < tol, (storage, m1 - m0)
 
 

@@ -52,7 +52,8 @@ def test_storage_round_trip(cuda):
     rng = np.random.default_rng(1)
     f = oracle.equilibrium(1 + 0.01 * rng.standard_normal((40, 48)), 0.02 * rng.standard_normal((40, 48)),
                            0.02 * rng.standard_normal((40, 48)))
-    for storage, tol in (("f32", 1e-7), ("f16dev", 3e-6), ("bf16dev", 3e-5)):
+    # half an ulp of |h| < 2^-5: 2^-17 in half, 2^-14 in bfloat16; f32: 2^-25 of f < 1
+    for storage, tol in (("f32", 3e-8), ("f16dev", 2.0 ** -17), ("bf16dev", 2.0 ** -14)):
         lat = PyLB.Lattice(40, 48, 1.0, boundary="periodic", storage=storage, device=cuda).load(torch.from_numpy(f))
         back = lat.populations(torch.float64).cpu().numpy()
         assert np.abs(back - f).max() < tol, storage
@@ -63,7 +64,10 @@ def test_equilibrium_initialisation_is_exact_at_rest(cuda):
     f = lat.populations().cpu().numpy()
     assert np.abs(f - oracle.W_I[:, None, None]).max() == 0
     rho, ux, uy = lat.macroscopic()
-    assert float(rho.min()) == 1.0 and float(ux.abs().max()) == 0.0
+    w_sum = 0.0
+    for w in oracle.W_I:  # the float64 weights do not sum to exactly 1
+        w_sum += w
+    assert float(rho.min()) == float(rho.max()) == w_sum and float(ux.abs().max()) == 0.0
 
 
 def test_bad_configuration_rejected(cuda):
@@ -100,6 +104,11 @@ def test_full_size_cavity_properties(cuda, storage):
     lat.step(1)
     mass, px, py = lat.mass_momentum().cpu().numpy()
     rel = 1e-6 if storage == "f32" else 2e-3
-    assert abs(mass - m0) < 1e-3
+    # 16-bit: every lid cell carries the same state, so the rounding of its
+    # rest population (the only value not conserved exactly) repeats across
+    # the 8192 columns: bound 8192 * half an ulp of |h_0| < 2^-9
+    assert abs(mass - m0) < (1e-3 if storage == "f32" else n * 2.0 ** -21)
     assert abs(px - u0 / 3 * (n - 1)) < rel * u0 / 3 * n
-    assert abs(py) < 1e-3
+    # y momentum is zero in exact arithmetic; 16-bit rounding of the six
+    # channels with cy != 0 repeats in every lid column: <= n * 6 * 2^-17
+    assert abs(py) < (1e-3 if storage == "f32" else n * 6 * 2.0 ** -17)
