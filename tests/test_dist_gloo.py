@@ -1,0 +1,60 @@
+"""Multi-rank path of bench.py on CPU (gloo, world size 2).
+
+The lattice does not shard across GPUs here: N ranks run N independent
+replicas and the whole-job throughput is all ranks' cell updates over the
+slowest rank's time.  These tests run that aggregation with real gloo ranks.
+"""
+
+import os
+import socket
+
+import pytest
+import torch.multiprocessing as mp
+
+
+def _free_port():
+    with socket.socket() as s:
+        s.bind(("127.0.0.1", 0))
+        return s.getsockname()[1]
+
+
+def _worker(rank, world, port, results):
+    os.environ.update({"MASTER_ADDR": "127.0.0.1", "MASTER_PORT": str(port), "RANK": str(rank),
+                       "WORLD_SIZE": str(world), "LOCAL_RANK": str(rank)})
+    import bench
+    d = bench.Dist(backend="gloo")
+    cells = 1000 * (rank + 1)          # ranks may hold different lattices
+    seconds = 2.0 if rank == 0 else 4.0  # rank 1 is the slow one
+    mlups, t = bench.aggregate_mlups(cells, 10, seconds, d)
+    d.barrier()
+    results[rank] = (mlups, t)
+    d.close()
+
+
+@pytest.mark.timeout(120)
+def test_replica_aggregation_two_ranks():
+    ctx = mp.get_context("spawn")
+    manager = ctx.Manager()
+    results = manager.dict()
+    port = _free_port()
+    procs = [ctx.Process(target=_worker, args=(r, 2, port, results)) for r in range(2)]
+    for p in procs:
+        p.start()
+    for p in procs:
+        p.join(90)
+        assert p.exitcode == 0
+    expected = (1000 + 2000) * 10 / 4.0 / 1e6
+    for r in range(2):
+        mlups, t = results[r]
+        assert t == 4.0
+        assert abs(mlups - expected) < 1e-12
+
+
+def test_single_process_needs_no_process_group(monkeypatch):
+    for k in ("WORLD_SIZE", "RANK", "LOCAL_RANK"):
+        monkeypatch.delenv(k, raising=False)
+    import bench
+    d = bench.Dist()
+    assert d.world == 1 and d.dist is None
+    mlups, t = bench.aggregate_mlups(2_000_000, 5, 0.5, d)
+    assert t == 0.5 and abs(mlups - 20.0) < 1e-12
