@@ -121,6 +121,22 @@ LBGB_API int lbgb_mass_momentum(const void *f, int64_t n, int64_t chan_stride, i
                        double *out_dev, void *workspace, size_t workspace_bytes,
                        void *stream);
 
+/* Allocation-free variant of lbgb_mass_momentum, for callers that may not
+ * allocate device memory (a code embedded in an application whose memory
+ * manager owns the GPU, or a time loop in which device allocations are
+ * forbidden) and therefore cannot pass a workspace.  Same result (FP64 sums;
+ * a different but fixed summation order), with the partial sums kept in an
+ * array built into the library (1.5 MiB, held on every GPU that loads the
+ * library until the process exits).  n must not exceed
+ * LBGB_NOALLOC_MAX_CELLS (LBGB_EINVAL otherwise).  The first call on a device
+ * looks up the array's device address with that device current; make that
+ * first call before any stream capture.  All calls share the array: calls
+ * whose kernels overlap on the GPU race and must be ordered (one stream, or
+ * events).  No counterpart in the reference (it has no GPU path). */
+#define LBGB_NOALLOC_MAX_CELLS 268435456LL
+LBGB_API int lbgb_mass_momentum_noalloc(const void *f, int64_t n, int64_t chan_stride, int dtype,
+                                        double *out_dev, void *stream);
+
 /* Converts populations between storage codes (n cells, channel strides
  * src_stride / dst_stride): e.g. F32 -> F16DEV stores f_i - w_i in half. */
 LBGB_API int lbgb_convert(const void *src, int src_dtype, int64_t src_stride, void *dst,

@@ -52,6 +52,7 @@ SIGNATURES = {
     "lbgb_macroscopic": (_I, [_P, _P, _P, _P, _I64, _I64, _I, _P]),
     "lbgb_mass_momentum_workspace_bytes": (_SZ, []),
     "lbgb_mass_momentum": (_I, [_P, _I64, _I64, _I, _P, _P, _SZ, _P]),
+    "lbgb_mass_momentum_noalloc": (_I, [_P, _I64, _I64, _I, _P, _P]),
     "lbgb_convert": (_I, [_P, _I, _I64, _P, _I, _I64, _I64, _P]),
     "lbgb_set_tuning": (_I, [_I, ctypes.c_longlong]),
     "lbgb_get_tuning": (ctypes.c_longlong, [_I]),
@@ -60,6 +61,7 @@ SIGNATURES = {
 
 TUNE_KERNEL, TUNE_STAGES, TUNE_WAIT_LIMIT, TUNE_PIPE_MIN_CELLS, TUNE_TEST_STALL_PRODUCER = 0, 1, 2, 3, 4
 KERNELS = {"auto": 0, "register": 1, "pipelined": 2}
+NOALLOC_MAX_CELLS = 268435456
 
 
 def load(path=LIB_PATH):

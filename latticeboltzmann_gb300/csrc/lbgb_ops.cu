@@ -4,6 +4,8 @@
 #include <stdarg.h>
 #include <stdio.h>
 
+#include <mutex>
+
 #include "lbgb_common.cuh"
 
 namespace lbgb {
@@ -379,4 +381,97 @@ extern "C" int lbgb_convert(const void *src, int src_dtype, int64_t src_stride, 
     case LBGB_BF16DEV: return launch_convert_to<LBGB_BF16DEV>(src, src_stride, dst, dst_dtype, dst_stride, n, s);
     }
     return LBGB_EDTYPE;
+}
+
+// ---------------------------------------------------------------- allocation-free reduction
+// lbgb_mass_momentum_noalloc is for callers that are not allowed to allocate
+// device memory at all -- for example a simulation code embedded in a larger
+// application whose memory manager owns the whole GPU, or a time loop where a
+// device allocation (which can synchronise the device and can fail when memory
+// is short) is forbidden between steps -- and so cannot provide the workspace
+// that lbgb_mass_momentum asks for.  It runs the same two kernels, with the
+// per-block partial sums kept in the file-scope array below instead of a
+// caller's workspace.
+//
+// Limits and sharing:
+//  * one partial per 4096 cells, at most LBGB_NOALLOC_MAX_CELLS cells (the
+//    array holds 65536 partials = 1.5 MiB; every GPU that loads this library
+//    holds it until the process exits);
+//  * every call uses the same array: each block overwrites its own partial
+//    before the second kernel reads it, so nothing has to start at zero, but
+//    calls whose kernels overlap on the GPU (different streams without
+//    ordering) race on the array and give wrong sums.
+constexpr int NOALLOC_CELLS_PER_BLOCK = RED_THREADS * 16;
+constexpr int NOALLOC_MAX_BLOCKS = (int)(LBGB_NOALLOC_MAX_CELLS / NOALLOC_CELLS_PER_BLOCK);
+static __device__ __align__(256) double g_noalloc_partials[NOALLOC_MAX_BLOCKS * 3];
+
+// Device address of the array, looked up once per device with that device
+// current.  A host-side use of the symbol itself would be a host stand-in,
+// not a device address, and must never be handed to a kernel.
+static double *noalloc_partials(int *rc) {
+    constexpr int MAX_DEV = 64;
+    static double *ptr[MAX_DEV] = {};
+    static std::mutex mu;
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess || dev < 0 || dev >= MAX_DEV) {
+        set_error("lbgb_mass_momentum_noalloc: no usable current device (%s)",
+                  e != cudaSuccess ? cudaGetErrorString(e) : "device index out of range");
+        *rc = LBGB_ECUDA;
+        return nullptr;
+    }
+    std::lock_guard<std::mutex> lock(mu);
+    if (!ptr[dev]) {
+        void *p = nullptr;
+        e = cudaGetSymbolAddress(&p, g_noalloc_partials);
+        if (e != cudaSuccess || !p) {
+            set_error("lbgb_mass_momentum_noalloc: cudaGetSymbolAddress failed: %s", cudaGetErrorString(e));
+            *rc = LBGB_ECUDA;
+            return nullptr;
+        }
+        ptr[dev] = static_cast<double *>(p);
+    }
+    *rc = LBGB_OK;
+    return ptr[dev];
+}
+
+extern "C" int lbgb_mass_momentum_noalloc(const void *f, int64_t n, int64_t chan_stride, int dtype, double *out_dev,
+                                         void *stream) {
+    int rc = check_cells(f, n, chan_stride, dtype, "lbgb_mass_momentum_noalloc");
+    if (rc) return rc;
+    if (!out_dev) {
+        set_error("lbgb_mass_momentum_noalloc: null output pointer");
+        return LBGB_EINVAL;
+    }
+    if (n > LBGB_NOALLOC_MAX_CELLS) {
+        set_error("lbgb_mass_momentum_noalloc: %lld cells exceed the built-in scratch limit of %lld cells; "
+                  "use lbgb_mass_momentum with a workspace",
+                  (long long)n, (long long)LBGB_NOALLOC_MAX_CELLS);
+        return LBGB_EINVAL;
+    }
+    double *partial = noalloc_partials(&rc);
+    if (!partial) return rc;
+    const int nblocks = n > 0 ? (int)((n + NOALLOC_CELLS_PER_BLOCK - 1) / NOALLOC_CELLS_PER_BLOCK) : 1;
+    cudaStream_t s = (cudaStream_t)stream;
+    switch (dtype) {
+    case LBGB_F32:
+        k_mass_momentum_partial<LBGB_F32><<<nblocks, RED_THREADS, 0, s>>>((const float *)f, n, chan_stride, partial);
+        break;
+    case LBGB_F64:
+        k_mass_momentum_partial<LBGB_F64><<<nblocks, RED_THREADS, 0, s>>>((const double *)f, n, chan_stride,
+                                                                          partial);
+        break;
+    case LBGB_F16DEV:
+        k_mass_momentum_partial<LBGB_F16DEV><<<nblocks, RED_THREADS, 0, s>>>((const unsigned short *)f, n,
+                                                                             chan_stride, partial);
+        break;
+    case LBGB_BF16DEV:
+        k_mass_momentum_partial<LBGB_BF16DEV><<<nblocks, RED_THREADS, 0, s>>>((const unsigned short *)f, n,
+                                                                              chan_stride, partial);
+        break;
+    }
+    rc = check_launch("k_mass_momentum_partial (no-alloc)");
+    if (rc) return rc;
+    k_sum_partials<<<1, RED_THREADS, 0, s>>>(partial, nblocks, out_dev);
+    return check_launch("k_sum_partials (no-alloc)");
 }
