@@ -58,6 +58,8 @@ def parse(argv=None):
     p.add_argument("--kernel", choices=["auto", "register", "pipelined"], default="auto",
                    help="step kernel: shared-memory pipelined, register/shuffle, or automatic choice")
     p.add_argument("--stages", type=int, default=0, help="pipeline stages (0: library default)")
+    p.add_argument("--rounding", choices=["nearest", "stochastic"], default="nearest",
+                   help="rounding of 16-bit storage")
     return p.parse_args(argv)
 
 
@@ -292,7 +294,7 @@ def run_ours(args):
     if args.stages:
         _lib.set_tuning(_lib.TUNE_STAGES, args.stages)
     lat = PyLB.Lattice(args.nx, args.ny, args.omega, boundary=args.boundary, u0=args.u0, storage=args.storage,
-                       device=dev)
+                       device=dev, rounding=args.rounding)
     stream = torch.cuda.current_stream(dev)
     for _ in range(args.warmup):
         lat.step(1)

@@ -17,8 +17,9 @@
  * SW(-1,-1), SE(1,-1)  (PyLB/Streaming.py:28-29).
  *
  * Storage codes (dtype): LBGB_F32 and LBGB_F64 store f itself;
- * LBGB_F16DEV / LBGB_BF16DEV store the deviation h_i = f_i - w_i as IEEE half
- * or bfloat16; all arithmetic on those is FP32.
+ * LBGB_F16DEV stores the deviation h_i = f_i - w_i scaled by 2^14 as IEEE half
+ * (the scale keeps small deviations out of half's subnormal range),
+ * LBGB_BF16DEV stores h_i as bfloat16; all arithmetic on those is FP32.
  */
 #ifndef LBGB_H
 #define LBGB_H
@@ -102,6 +103,21 @@ LBGB_API int lbgb_step_fused(const void *src, void *dst, int nx, int ny, int bou
 LBGB_API int lbgb_run_fused(void *a, void *b, int nx, int ny, int boundary,
                    double omega, double u0, int dtype, int nsteps, int *which,
                    void *stream);
+
+/* As lbgb_run_fused, with stochastic rounding of the 16-bit storage codes
+ * (LBGB_F16DEV, LBGB_BF16DEV; other codes run lbgb_run_fused).  Every stored
+ * value is rounded up or down at random with the probabilities that make the
+ * rounding unbiased, and the rest population keeps each node's mass, so that
+ * rounding errors no longer add up step after step in slowly varying flows.
+ * The random bits are a hash of (seed, step, cell, channel): results are
+ * reproducible.  step_counter: device pointer to one unsigned 64-bit step
+ * index, read by every step and advanced by one after it (on the stream), so
+ * that graph replays keep drawing fresh bits.  No counterpart in the
+ * reference (it has no reduced-precision storage). */
+LBGB_API int lbgb_run_fused_sr(void *a, void *b, int nx, int ny, int boundary,
+                               double omega, double u0, int dtype, int nsteps,
+                               unsigned int seed, unsigned long long *step_counter,
+                               int *which, void *stream);
 
 /* Density and velocity of every cell (the diagnostics of cavity_opt2.py:280-281
  * and cavity_opt1.py:154-156).  rho/ux/uy are float for the F32/F16DEV/BF16DEV

@@ -49,6 +49,7 @@ SIGNATURES = {
     "lbgb_stream_bounce_back": (_I, [_P, _P, _I, _I, _D, _I, _P]),
     "lbgb_step_fused": (_I, [_P, _P, _I, _I, _I, _D, _D, _I, _P]),
     "lbgb_run_fused": (_I, [_P, _P, _I, _I, _I, _D, _D, _I, _I, ctypes.POINTER(_I), _P]),
+    "lbgb_run_fused_sr": (_I, [_P, _P, _I, _I, _I, _D, _D, _I, _I, ctypes.c_uint, _P, ctypes.POINTER(_I), _P]),
     "lbgb_macroscopic": (_I, [_P, _P, _P, _P, _I64, _I64, _I, _P]),
     "lbgb_mass_momentum_workspace_bytes": (_SZ, []),
     "lbgb_mass_momentum": (_I, [_P, _I64, _I64, _I, _P, _P, _SZ, _P]),

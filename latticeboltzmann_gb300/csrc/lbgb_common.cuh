@@ -49,12 +49,21 @@ template <> struct Codec<LBGB_F64> {
     static __device__ __forceinline__ real dec(raw x, int) { return x; }
     static __device__ __forceinline__ raw enc(real x, int) { return x; }
 };
+// Half deviations are stored scaled by 2^14: deviations down to ~4e-9 stay
+// in half's normal range (full 11-bit precision instead of the coarse
+// subnormal grid below 6e-5), and |f - w| < 4 still fits.  Scaling by a power
+// of two is exact in both directions.
+constexpr float F16_SCALE = 16384.0f;
+constexpr float F16_UNSCALE = 1.0f / 16384.0f;
+
 template <> struct Codec<LBGB_F16DEV> {
     using raw = unsigned short;
     using real = float;
-    static __device__ __forceinline__ real dec_h(raw x) { return __half2float(__ushort_as_half(x)); }
-    static __device__ __forceinline__ raw enc_h(real h) { return __half_as_ushort(__float2half_rn(h)); }
-    static __device__ __forceinline__ real dec(raw x, int i) { return dec_h(x) + wgt<float>(i); }
+    static __device__ __forceinline__ real dec_h(raw x) { return __half2float(__ushort_as_half(x)) * F16_UNSCALE; }
+    static __device__ __forceinline__ raw enc_h(real h) { return __half_as_ushort(__float2half_rn(h * F16_SCALE)); }
+    static __device__ __forceinline__ real dec(raw x, int i) {
+        return fmaf(__half2float(__ushort_as_half(x)), F16_UNSCALE, wgt<float>(i));
+    }
     static __device__ __forceinline__ raw enc(real x, int i) { return enc_h(x - wgt<float>(i)); }
 };
 template <> struct Codec<LBGB_BF16DEV> {
@@ -110,6 +119,127 @@ __device__ __forceinline__ void stv(RAW *p, const RAW (&v)[V]) {
     T x;
     memcpy(&x, v, sizeof(T));
     st_cs(reinterpret_cast<T *>(p), x);
+}
+
+// ---------------------------------------------------------------- packets
+// A packet is the N consecutive cells of one channel that one thread moves as
+// one 8- or 16-byte vector.  The 16-bit routines convert two values per
+// instruction where the hardware allows (half2 -> float2, float2 -> half2 /
+// bfloat162); bfloat16 -> float is a 16-bit shift.
+template <int DT, int N>
+struct Packet {
+    using raw = typename Codec<DT>::raw;
+    using real = typename Codec<DT>::real;
+    static constexpr int BYTES = N * (int)sizeof(raw);
+    static constexpr int WORDS = BYTES / 4;
+    using vec = typename VecBits<BYTES>::t;
+
+    // values f = h + w (16-bit codecs; w = 0 gives the deviations) or f
+    static __device__ __forceinline__ void dec(const vec &x, real w, real (&o)[N]) {
+        uint32_t wd[WORDS];
+        memcpy(wd, &x, BYTES);
+        if constexpr (DT == LBGB_F32) {
+#pragma unroll
+            for (int q = 0; q < N; ++q) o[q] = __uint_as_float(wd[q]);
+        } else if constexpr (DT == LBGB_F64) {
+#pragma unroll
+            for (int q = 0; q < N; ++q) o[q] = __hiloint2double((int)wd[2 * q + 1], (int)wd[2 * q]);
+        } else {
+#pragma unroll
+            for (int q = 0; q < WORDS; ++q) {
+                if constexpr (DT == LBGB_F16DEV) {
+                    const float2 p = __half22float2(*reinterpret_cast<const __half2 *>(&wd[q]));
+                    o[2 * q] = fmaf(p.x, F16_UNSCALE, w);
+                    o[2 * q + 1] = fmaf(p.y, F16_UNSCALE, w);
+                } else {
+                    o[2 * q] = __uint_as_float(wd[q] << 16) + w;
+                    o[2 * q + 1] = __uint_as_float(wd[q] & 0xffff0000u) + w;
+                }
+            }
+        }
+    }
+    // one stored element plus w
+    static __device__ __forceinline__ real dec1(raw x, real w) {
+        if constexpr (DT == LBGB_F16DEV)
+            return fmaf(__half2float(__ushort_as_half(x)), F16_UNSCALE, w);
+        else if constexpr (DT == LBGB_BF16DEV)
+            return __uint_as_float((uint32_t)x << 16) + w;
+        else
+            return x;
+    }
+    // packs N deviations of a 16-bit codec, two per conversion
+    static __device__ __forceinline__ vec enc_h(const real (&h)[N]) {
+        uint32_t wd[WORDS];
+#pragma unroll
+        for (int q = 0; q < WORDS; ++q) {
+            if constexpr (DT == LBGB_F16DEV) {
+                const __half2 p = __floats2half2_rn(h[2 * q] * F16_SCALE, h[2 * q + 1] * F16_SCALE);
+                wd[q] = *reinterpret_cast<const uint32_t *>(&p);
+            } else {
+                const __nv_bfloat162 p = __floats2bfloat162_rn(h[2 * q], h[2 * q + 1]);
+                wd[q] = *reinterpret_cast<const uint32_t *>(&p);
+            }
+        }
+        vec x;
+        memcpy(&x, wd, BYTES);
+        return x;
+    }
+};
+
+
+
+// ---------------------------------------------------------------- stochastic rounding
+// Rounding a slowly varying field to 16 bits repeats the same error at every
+// step, so the errors add up linearly (mass and momentum drift).  Stochastic
+// rounding -- round up with probability equal to the discarded fraction --
+// makes every rounding unbiased, and the accumulated error a random walk.
+// The random bits are a counter-based hash of (seed, step, cell, channel), so
+// every kernel variant rounds every value identically.  Two neighbouring
+// cells (2m, 2m+1) of a channel share one 32-bit hash: 16 bits each.
+__device__ __forceinline__ uint32_t mix32(uint32_t x) {
+    // integer finaliser with the constants of the public-domain "lowbias32"
+    // from C. Wellons' hash-prospector
+    x ^= x >> 16;
+    x *= 0x7feb352du;
+    x ^= x >> 15;
+    x *= 0x846ca68bu;
+    x ^= x >> 16;
+    return x;
+}
+__device__ __forceinline__ uint32_t sr_step_key(uint32_t seed, unsigned long long step) {
+    return mix32(seed ^ mix32((uint32_t)step * 0x9e3779b9u + (uint32_t)(step >> 32)));
+}
+__device__ __forceinline__ uint32_t sr_pair_bits(uint32_t key, uint32_t even_cell, int ch) {
+    return mix32((even_cell * 9u + (uint32_t)ch) ^ key);
+}
+// f (FP32) -> 16-bit pattern with stochastic rounding, r = 16 random bits
+template <int DT>
+__device__ __forceinline__ uint32_t sr_round16(float h, uint32_t r) {
+    if constexpr (DT == LBGB_BF16DEV) {
+        return (__float_as_uint(h) + r) >> 16;
+    } else {
+        // keep half's 10 mantissa bits of the scaled value; the result is
+        // exactly representable, so the final conversion does not round
+        const float x = __uint_as_float((__float_as_uint(h * F16_SCALE) + (r >> 3)) & 0xffffe000u);
+        return __half_as_ushort(__float2half_rn(x));
+    }
+}
+
+// packs N deviations of a 16-bit codec with stochastic rounding; cell0 (even)
+// is the global index of the packet's first cell
+template <int DT, int N>
+__device__ __forceinline__ typename Packet<DT, N>::vec enc_h_sr(const float (&h)[N], uint32_t key, uint32_t cell0,
+                                                              int ch) {
+    using P = Packet<DT, N>;
+    uint32_t wd[P::WORDS];
+#pragma unroll
+    for (int q = 0; q < P::WORDS; ++q) {
+        const uint32_t r = sr_pair_bits(key, cell0 + 2 * q, ch);
+        wd[q] = sr_round16<DT>(h[2 * q], r & 0xffffu) | (sr_round16<DT>(h[2 * q + 1], r >> 16) << 16);
+    }
+    typename P::vec x;
+    memcpy(&x, wd, P::BYTES);
+    return x;
 }
 
 // ---------------------------------------------------------------- collision
@@ -229,6 +359,26 @@ __device__ __forceinline__ void collide_encode(typename Codec<DT>::real (&f)[9],
 #pragma unroll
         for (int i = 0; i < 9; ++i) out[i] = C::enc(f[i], i);
     }
+}
+
+// 16-bit storage with stochastic rounding (see above): the moving populations
+// are rounded stochastically, then the rest population carries the node's
+// remaining mass (for both 16-bit codecs) and is rounded stochastically too.
+template <int DT>
+__device__ __forceinline__ void collide_encode_sr(float (&f)[9], float omega, unsigned short (&out)[9], uint32_t key,
+                                                  uint32_t cell) {
+    float dm = f[0] - wgt<float>(0);
+#pragma unroll
+    for (int i = 1; i < 9; ++i) dm += f[i] - wgt<float>(i);
+    bgk_collide(f, omega);
+#pragma unroll
+    for (int i = 1; i < 9; ++i) {
+        const uint32_t r = sr_pair_bits(key, cell & ~1u, i);
+        out[i] = (unsigned short)sr_round16<DT>(f[i] - wgt<float>(i), (cell & 1u) ? (r >> 16) : (r & 0xffffu));
+        dm -= Codec<DT>::dec_h(out[i]);
+    }
+    const uint32_t r = sr_pair_bits(key, cell & ~1u, 0);
+    out[0] = (unsigned short)sr_round16<DT>(dm, (cell & 1u) ? (r >> 16) : (r & 0xffffu));
 }
 
 // ---------------------------------------------------------------- host side

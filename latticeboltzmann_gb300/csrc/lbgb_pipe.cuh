@@ -71,30 +71,43 @@ __device__ __forceinline__ void bulk_copy_g2s(void *dst, const void *src, uint32
 // device-side status word of the pipelined kernels (0 = fine)
 __device__ int g_pipe_status;
 
-constexpr int PIPE_CONSUMER_WARPS = 8;
 constexpr long long PIPE_DRAIN_LIMIT = 1ll << 22;
 
 __device__ __forceinline__ void pipe_report(int code) { atomicCAS(&g_pipe_status, 0, code); }
 
-template <class RAW>
+// Tile geometry: NCW consumer warps, NC cells per consumer thread (one 8- or
+// 16-byte packet per channel), a 16-byte halo on each side of the row segment
+// (bulk copies start and end on 16-byte boundaries).
+template <class RAW, int NCW_, int NC_>
 struct PipeGeom {
-    static constexpr int NC = 16 / (int)sizeof(RAW);           // cells per consumer thread
-    static constexpr int HALO = NC;                            // one 16-byte vector each side
-    static constexpr int L = PIPE_CONSUMER_WARPS * 32 * NC;    // cells per tile
+    static constexpr int NCW = NCW_;
+    static constexpr int NC = NC_;
+    static constexpr int HALO = 16 / (int)sizeof(RAW);
+    static constexpr int L = NCW * 32 * NC;                    // cells per tile
     static constexpr int SLOT = L + 2 * HALO;                  // elements per channel slot
     static constexpr size_t STAGE_BYTES = 9ull * SLOT * sizeof(RAW);
 };
 
-template <int DT, int BC, bool COLLIDE>
-__global__ void __launch_bounds__((PIPE_CONSUMER_WARPS + 1) * 32, 1)
+// Shapes per storage code: FP32 8 warps x 4 cells, FP64 8 x 2; the 16-bit
+// codecs have twice the cells per byte, so twice the consumer warps (16) with
+// 4 cells each.
+template <int DT> struct PipeShape { static constexpr int NCW = 8, NC = 4; };
+template <> struct PipeShape<LBGB_F64> { static constexpr int NCW = 8, NC = 2; };
+template <> struct PipeShape<LBGB_F16DEV> { static constexpr int NCW = 16, NC = 4; };
+template <> struct PipeShape<LBGB_BF16DEV> { static constexpr int NCW = 16, NC = 4; };
+
+template <int DT, int BC, bool COLLIDE, int NCW_, int NC_, bool SRND>
+__global__ void __launch_bounds__((NCW_ + 1) * 32, 1)
 k_step_pipe(const typename Codec<DT>::raw *__restrict__ src, typename Codec<DT>::raw *__restrict__ dst, int nx,
             int ny, int tiles_per_row, int total_tiles, int stages, typename Codec<DT>::real omega,
-            typename Codec<DT>::real u0, long long wait_limit, int stall_producer) {
+            typename Codec<DT>::real u0, long long wait_limit, int stall_producer,
+            const unsigned long long *__restrict__ sr_step, uint32_t sr_seed) {
     using C = Codec<DT>;
     using raw = typename C::raw;
     using real = typename C::real;
-    using G = PipeGeom<raw>;
-    constexpr int NC = G::NC, HALO = G::HALO, L = G::L, SLOT = G::SLOT, NCW = PIPE_CONSUMER_WARPS;
+    using G = PipeGeom<raw, NCW_, NC_>;
+    using P = Packet<DT, NC_>;
+    constexpr int NC = G::NC, HALO = G::HALO, L = G::L, SLOT = G::SLOT, NCW = G::NCW;
 
     extern __shared__ __align__(128) unsigned char smem[];
     raw *slots = reinterpret_cast<raw *>(smem);
@@ -175,13 +188,7 @@ k_step_pipe(const typename Codec<DT>::raw *__restrict__ src, typename Codec<DT>:
 #pragma unroll
             for (int i = 0; i < 9; ++i) {
                 const raw *sl = stage + i * SLOT + HALO + t * NC;
-                raw r[NC];
-                {
-                    const uint4 x = *reinterpret_cast<const uint4 *>(sl);
-                    memcpy(r, &x, 16);
-                }
-#pragma unroll
-                for (int j = 0; j < NC; ++j) v[i][j] = C::dec(r[j], i);
+                P::dec(*reinterpret_cast<const typename P::vec *>(sl), wgt<real>(i), v[i]);
                 const bool wall = (cx(i) > 0 && wl) || (cx(i) < 0 && wr);
                 if (wall || cy(i) == 0) continue;
                 int row = k - cx(i);
@@ -189,7 +196,7 @@ k_step_pipe(const typename Codec<DT>::raw *__restrict__ src, typename Codec<DT>:
                 if (cy(i) > 0) {
                     real prev = 0;
                     if (c > 0)
-                        prev = C::dec(sl[-1], i);
+                        prev = P::dec1(sl[-1], wgt<real>(i));
                     else if (BC == LBGB_PERIODIC)
                         prev = C::dec(ld1(src + (size_t)i * cs + (size_t)row * ny + (ny - 1)), i);
 #pragma unroll
@@ -198,7 +205,7 @@ k_step_pipe(const typename Codec<DT>::raw *__restrict__ src, typename Codec<DT>:
                 } else {
                     real next = 0;
                     if (c + NC < ny)
-                        next = C::dec(sl[NC], i);
+                        next = P::dec1(sl[NC], wgt<real>(i));
                     else if (BC == LBGB_PERIODIC)
                         next = C::dec(ld1(src + (size_t)i * cs + (size_t)row * ny), i);
 #pragma unroll
@@ -231,26 +238,81 @@ k_step_pipe(const typename Codec<DT>::raw *__restrict__ src, typename Codec<DT>:
             }
         }
 
-        raw out[9][NC];
-        if (COLLIDE) {
+        raw *out_row = dst + (size_t)k * ny + c;
+        if constexpr (COLLIDE && sizeof(raw) == 2) {
+            // 16-bit deviations: collide in FP32, pack two values per
+            // conversion.  Round to nearest: half storage writes the rest
+            // population last so that each node keeps its mass (see
+            // collide_encode).  Stochastic rounding (sr_step set): both codecs
+            // round every value stochastically and keep the mass the same way
+            // (see collide_encode_sr).
+            constexpr bool sr = SRND;
+            constexpr bool keep_mass = SRND || DT == LBGB_F16DEV;
+            real hpost[9][NC];
+            real dm[NC];
 #pragma unroll
             for (int j = 0; j < NC; ++j) {
                 real f[9];
-                raw r[9];
 #pragma unroll
                 for (int i = 0; i < 9; ++i) f[i] = v[i][j];
-                collide_encode<DT>(f, omega, r);
+                if constexpr (keep_mass) {
+                    dm[j] = f[0] - wgt<real>(0);
 #pragma unroll
-                for (int i = 0; i < 9; ++i) out[i][j] = r[i];
+                    for (int i = 1; i < 9; ++i) dm[j] += f[i] - wgt<real>(i);
+                }
+                bgk_collide(f, omega);
+#pragma unroll
+                for (int i = 0; i < 9; ++i) hpost[i][j] = f[i] - wgt<real>(i);
             }
+            uint32_t key = 0u;
+            if constexpr (SRND) key = sr_step_key(sr_seed, *sr_step);
+            const uint32_t cell0 = (uint32_t)((size_t)k * ny + c);
+            typename P::vec pk[9];
+#pragma unroll
+            for (int i = 1; i < 9; ++i) {
+                if constexpr (sr)
+                    pk[i] = enc_h_sr<DT, NC>(hpost[i], key, cell0, i);
+                else
+                    pk[i] = P::enc_h(hpost[i]);
+                if constexpr (keep_mass) {
+                    real y[NC];
+                    P::dec(pk[i], real(0), y);
+#pragma unroll
+                    for (int j = 0; j < NC; ++j) dm[j] -= y[j];
+                }
+            }
+            if constexpr (keep_mass) {
+#pragma unroll
+                for (int j = 0; j < NC; ++j) hpost[0][j] = dm[j];
+            }
+            if constexpr (sr)
+                pk[0] = enc_h_sr<DT, NC>(hpost[0], key, cell0, 0);
+            else
+                pk[0] = P::enc_h(hpost[0]);
+#pragma unroll
+            for (int i = 0; i < 9; ++i) st_cs(reinterpret_cast<typename P::vec *>(out_row + (size_t)i * cs), pk[i]);
         } else {
+            raw out[9][NC];
+            if (COLLIDE) {
 #pragma unroll
-            for (int i = 0; i < 9; ++i)
+                for (int j = 0; j < NC; ++j) {
+                    real f[9];
+                    raw r[9];
 #pragma unroll
-                for (int j = 0; j < NC; ++j) out[i][j] = C::enc(v[i][j], i);
+                    for (int i = 0; i < 9; ++i) f[i] = v[i][j];
+                    collide_encode<DT>(f, omega, r);
+#pragma unroll
+                    for (int i = 0; i < 9; ++i) out[i][j] = r[i];
+                }
+            } else {
+#pragma unroll
+                for (int i = 0; i < 9; ++i)
+#pragma unroll
+                    for (int j = 0; j < NC; ++j) out[i][j] = C::enc(v[i][j], i);
+            }
+#pragma unroll
+            for (int i = 0; i < 9; ++i) stv<raw, NC>(out_row + (size_t)i * cs, out[i]);
         }
-#pragma unroll
-        for (int i = 0; i < 9; ++i) stv<raw, NC>(dst + (size_t)i * cs + (size_t)k * ny + c, out[i]);
     }
 }
 

@@ -109,7 +109,8 @@ constexpr int min_blocks() { return (sizeof(typename Codec<DT>::raw) == 2 && V =
 template <int DT, int BC, bool COLLIDE, int V>
 __global__ void __launch_bounds__(256, min_blocks<DT, V>())
 k_step(const typename Codec<DT>::raw *__restrict__ src, typename Codec<DT>::raw *__restrict__ dst, int nx,
-       int ny, int segs, long long tasks, typename Codec<DT>::real omega, typename Codec<DT>::real u0) {
+       int ny, int segs, long long tasks, typename Codec<DT>::real omega, typename Codec<DT>::real u0,
+       const unsigned long long *__restrict__ sr_step, uint32_t sr_seed) {
     using C = Codec<DT>;
     using real = typename C::real;
     using raw = typename C::raw;
@@ -170,13 +171,24 @@ k_step(const typename Codec<DT>::raw *__restrict__ src, typename Codec<DT>::raw 
 
         raw out[9][V];
         if (COLLIDE) {
+            uint32_t key = 0;
+            if constexpr (sizeof(raw) == 2) {
+                if (sr_step) key = sr_step_key(sr_seed, *sr_step);
+            }
 #pragma unroll
             for (int j = 0; j < V; ++j) {
                 real f[9];
                 raw r[9];
 #pragma unroll
                 for (int i = 0; i < 9; ++i) f[i] = v[i][j];
-                collide_encode<DT>(f, omega, r);
+                if constexpr (sizeof(raw) == 2) {
+                    if (sr_step)
+                        collide_encode_sr<DT>(f, omega, r, key, (uint32_t)((size_t)k * ny + l0 + j));
+                    else
+                        collide_encode<DT>(f, omega, r);
+                } else {
+                    collide_encode<DT>(f, omega, r);
+                }
 #pragma unroll
                 for (int i = 0; i < 9; ++i) out[i][j] = r[i];
             }
@@ -205,8 +217,14 @@ static int sm_count() {
     return n;
 }
 
+struct SR {
+    const unsigned long long *step = nullptr;  // device step counter; null: round to nearest
+    uint32_t seed = 0;
+};
+
 template <int DT, int BC, bool COLLIDE, int V>
-static int launch_v(const void *src, void *dst, int nx, int ny, double omega, double u0, cudaStream_t s) {
+static int launch_v(const void *src, void *dst, int nx, int ny, double omega, double u0, cudaStream_t s,
+                    SR sr = SR()) {
     using C = Codec<DT>;
     const int threads = 256;
     const int segs = (ny + 32 * V - 1) / (32 * V);
@@ -218,7 +236,7 @@ static int launch_v(const void *src, void *dst, int nx, int ny, double omega, do
     if (blocks > cap) blocks = cap;
     k_step<DT, BC, COLLIDE, V><<<(unsigned)blocks, threads, 0, s>>>(
         static_cast<const typename C::raw *>(src), static_cast<typename C::raw *>(dst), nx, ny, segs, tasks,
-        (typename C::real)omega, (typename C::real)u0);
+        (typename C::real)omega, (typename C::real)u0, sr.step, sr.seed);
     return check_launch("k_step");
 }
 
@@ -244,9 +262,11 @@ static int max_dyn_smem() {
 }
 
 template <int DT, int BC, bool COLLIDE>
-static int launch_pipe(const void *src, void *dst, int nx, int ny, double omega, double u0, cudaStream_t s) {
+static int launch_pipe(const void *src, void *dst, int nx, int ny, double omega, double u0, cudaStream_t s,
+                       SR sr) {
     using raw = typename Codec<DT>::raw;
-    using G = PipeGeom<raw>;
+    using SH = PipeShape<DT>;
+    using G = PipeGeom<raw, SH::NCW, SH::NC>;
     const long long tpr = (ny + G::L - 1) / G::L;
     const long long total = (long long)nx * tpr;
     const int smax = max_dyn_smem();
@@ -255,20 +275,28 @@ static int launch_pipe(const void *src, void *dst, int nx, int ny, double omega,
     if (stages > fit) stages = fit;
     if (stages < 2 || total > INT_MAX) return 1;  // caller falls back to the register kernel
     const size_t smem = (size_t)stages * G::STAGE_BYTES + 16 * (size_t)stages;
-    static bool attr = false;  // one per template instance
-    if (!attr) {
-        cudaError_t e = cudaFuncSetAttribute(k_step_pipe<DT, BC, COLLIDE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                             smax);
-        if (e != cudaSuccess) {
-            set_error("k_step_pipe: cannot reserve %d bytes of shared memory: %s", smax, cudaGetErrorString(e));
-            return LBGB_ECUDA;
-        }
-        attr = true;
-    }
     const int grid = (int)(total < sm_count() ? total : sm_count());
-    k_step_pipe<DT, BC, COLLIDE><<<grid, (PIPE_CONSUMER_WARPS + 1) * 32, smem, s>>>(
-        static_cast<const raw *>(src), static_cast<raw *>(dst), nx, ny, (int)tpr, (int)total, stages,
-        (typename Codec<DT>::real)omega, (typename Codec<DT>::real)u0, g_tune.wait_limit, (int)g_tune.stall_producer);
+    const bool srnd = sizeof(raw) == 2 && COLLIDE && sr.step != nullptr;
+    // the dynamic shared-memory limit is raised once per kernel variant
+    static bool attr_set[2] = {false, false};
+    auto go = [&](auto kernel, int variant) -> int {
+        if (!attr_set[variant]) {
+            cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smax);
+            if (e != cudaSuccess) {
+                set_error("k_step_pipe: cannot reserve %d bytes of shared memory: %s", smax, cudaGetErrorString(e));
+                return LBGB_ECUDA;
+            }
+            attr_set[variant] = true;
+        }
+        kernel<<<grid, (SH::NCW + 1) * 32, smem, s>>>(
+            static_cast<const raw *>(src), static_cast<raw *>(dst), nx, ny, (int)tpr, (int)total, stages,
+            (typename Codec<DT>::real)omega, (typename Codec<DT>::real)u0, g_tune.wait_limit,
+            (int)g_tune.stall_producer, sr.step, sr.seed);
+        return LBGB_OK;
+    };
+    const int rc = srnd ? go(k_step_pipe<DT, BC, COLLIDE, SH::NCW, SH::NC, sizeof(raw) == 2 && COLLIDE>, 1)
+                        : go(k_step_pipe<DT, BC, COLLIDE, SH::NCW, SH::NC, false>, 0);
+    if (rc) return rc;
     return check_launch("k_step_pipe");
 }
 
@@ -276,27 +304,28 @@ static int launch_pipe(const void *src, void *dst, int nx, int ny, double omega,
 // lattices, or when forced); otherwise the register kernel with the widest
 // vector width that divides ny and keeps every row start aligned.
 template <int DT, int BC, bool COLLIDE>
-static int launch(const void *src, void *dst, int nx, int ny, double omega, double u0, cudaStream_t s) {
+static int launch(const void *src, void *dst, int nx, int ny, double omega, double u0, cudaStream_t s,
+                  SR sr = SR()) {
     constexpr int VW = 16 / sizeof(typename Codec<DT>::raw);
     const bool vec_ok = ny % VW == 0 && aligned(src, 16) && aligned(dst, 16);
     const bool want_pipe = g_tune.kernel == 2 ||
                            (g_tune.kernel == 0 && (long long)nx * ny >= g_tune.pipe_min_cells);
     if (vec_ok && want_pipe) {
-        const int rc = launch_pipe<DT, BC, COLLIDE>(src, dst, nx, ny, omega, u0, s);
+        const int rc = launch_pipe<DT, BC, COLLIDE>(src, dst, nx, ny, omega, u0, s, sr);
         if (rc <= 0) return rc;
     }
-    if (vec_ok) return launch_v<DT, BC, COLLIDE, VW>(src, dst, nx, ny, omega, u0, s);
-    return launch_v<DT, BC, COLLIDE, 1>(src, dst, nx, ny, omega, u0, s);
+    if (vec_ok) return launch_v<DT, BC, COLLIDE, VW>(src, dst, nx, ny, omega, u0, s, sr);
+    return launch_v<DT, BC, COLLIDE, 1>(src, dst, nx, ny, omega, u0, s, sr);
 }
 
 template <int BC, bool COLLIDE>
 static int dispatch(const void *src, void *dst, int nx, int ny, int dtype, double omega, double u0,
-                    cudaStream_t s) {
+                    cudaStream_t s, SR sr = SR()) {
     switch (dtype) {
     case LBGB_F32: return launch<LBGB_F32, BC, COLLIDE>(src, dst, nx, ny, omega, u0, s);
     case LBGB_F64: return launch<LBGB_F64, BC, COLLIDE>(src, dst, nx, ny, omega, u0, s);
-    case LBGB_F16DEV: return launch<LBGB_F16DEV, BC, COLLIDE>(src, dst, nx, ny, omega, u0, s);
-    case LBGB_BF16DEV: return launch<LBGB_BF16DEV, BC, COLLIDE>(src, dst, nx, ny, omega, u0, s);
+    case LBGB_F16DEV: return launch<LBGB_F16DEV, BC, COLLIDE>(src, dst, nx, ny, omega, u0, s, sr);
+    case LBGB_BF16DEV: return launch<LBGB_BF16DEV, BC, COLLIDE>(src, dst, nx, ny, omega, u0, s, sr);
     default: set_error("unsupported storage code %d", dtype); return LBGB_EDTYPE;
     }
 }
@@ -372,6 +401,46 @@ extern "C" int lbgb_run_fused(void *a, void *b, int nx, int ny, int boundary, do
     void *src = a, *dst = b;
     for (int s = 0; s < nsteps; ++s) {
         rc = lbgb_step_fused(src, dst, nx, ny, boundary, omega, u0, dtype, stream);
+        if (rc) return rc;
+        void *t = src;
+        src = dst;
+        dst = t;
+    }
+    if (which) *which = (src == a) ? 0 : 1;
+    return LBGB_OK;
+}
+
+namespace lbgb {
+__global__ void k_bump_step(unsigned long long *ctr) { *ctr += 1; }
+}  // namespace lbgb
+
+extern "C" int lbgb_run_fused_sr(void *a, void *b, int nx, int ny, int boundary, double omega, double u0, int dtype,
+                                 int nsteps, unsigned int seed, unsigned long long *step_counter, int *which,
+                                 void *stream) {
+    if (dtype != LBGB_F16DEV && dtype != LBGB_BF16DEV)
+        return lbgb_run_fused(a, b, nx, ny, boundary, omega, u0, dtype, nsteps, which, stream);
+    if (nsteps < 0) {
+        set_error("lbgb_run_fused_sr: nsteps must be >= 0");
+        return LBGB_EINVAL;
+    }
+    if (!step_counter || !aligned(step_counter, 8)) {
+        set_error("lbgb_run_fused_sr: step_counter must be an 8-byte aligned device pointer");
+        return LBGB_EINVAL;
+    }
+    int rc = check_grid(a, b, nx, ny, dtype, boundary, "lbgb_run_fused_sr");
+    if (rc) return rc;
+    cudaStream_t s = (cudaStream_t)stream;
+    SR sr;
+    sr.step = step_counter;
+    sr.seed = seed;
+    void *src = a, *dst = b;
+    for (int i = 0; i < nsteps; ++i) {
+        rc = boundary == LBGB_CAVITY
+                 ? dispatch<LBGB_CAVITY, true>(src, dst, nx, ny, dtype, omega, u0, s, sr)
+                 : dispatch<LBGB_PERIODIC, true>(src, dst, nx, ny, dtype, omega, 0.0, s, sr);
+        if (rc) return rc;
+        k_bump_step<<<1, 1, 0, s>>>(step_counter);
+        rc = check_launch("k_bump_step");
         if (rc) return rc;
         void *t = src;
         src = dst;

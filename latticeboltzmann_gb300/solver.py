@@ -51,9 +51,16 @@ class Lattice:
         Lid velocity (cavity only).
     storage : {"f32", "f64", "f16dev", "bf16dev"}
     device : torch device (CUDA).
+    rounding : {"nearest", "stochastic"}
+        How 16-bit storage rounds (FP32/FP64 ignore it).  Stochastic rounding
+        is unbiased, so rounding errors do not add up in slowly varying flows;
+        its random bits are a hash of (seed, step, cell, channel).
+    seed : int
+        Seed of the stochastic rounding.
     """
 
-    def __init__(self, nx, ny, omega, boundary="cavity", u0=0.1, storage="f32", device=None):
+    def __init__(self, nx, ny, omega, boundary="cavity", u0=0.1, storage="f32", device=None, rounding="nearest",
+                 seed=0):
         if storage not in _RAW:
             raise ValueError("storage must be one of %s" % sorted(_RAW))
         if boundary not in _lib.BOUNDARY_CODES:
@@ -78,6 +85,12 @@ class Lattice:
         self._cur = 0
         self._ws = None
         self.steps_taken = 0
+        if rounding not in ("nearest", "stochastic"):
+            raise ValueError("rounding must be 'nearest' or 'stochastic'")
+        self.rounding = rounding
+        self.seed = int(seed) & 0xffffffff
+        # device step index read by stochastic rounding (advanced on the device)
+        self._step_ctr = torch.zeros(1, dtype=torch.int64, device=self.device)
         self.equilibrium()
 
     # ------------------------------------------------------------------ state
@@ -171,8 +184,13 @@ class Lattice:
             return self
         which = ctypes.c_int(0)
         a, b = self._buf[self._cur], self._buf[1 - self._cur]
-        _lib.call("lbgb_run_fused", a.data_ptr(), b.data_ptr(), self.nx, self.ny, self.bcode, self.omega, self.u0,
-                  self.code, int(n), ctypes.byref(which), self._stream())
+        if self.rounding == "stochastic" and self.storage in ("f16dev", "bf16dev"):
+            _lib.call("lbgb_run_fused_sr", a.data_ptr(), b.data_ptr(), self.nx, self.ny, self.bcode, self.omega,
+                      self.u0, self.code, int(n), self.seed, self._step_ctr.data_ptr(), ctypes.byref(which),
+                      self._stream())
+        else:
+            _lib.call("lbgb_run_fused", a.data_ptr(), b.data_ptr(), self.nx, self.ny, self.bcode, self.omega,
+                      self.u0, self.code, int(n), ctypes.byref(which), self._stream())
         if which.value == 1:
             self._cur = 1 - self._cur
         self.steps_taken += n
@@ -191,6 +209,11 @@ class Lattice:
         warm = [torch.zeros((9, 2, self.ny), dtype=_RAW[self.storage], device=self.device) for _ in range(2)]
         _lib.call("lbgb_step_fused", warm[0].data_ptr(), warm[1].data_ptr(), 2, self.ny, self.bcode, self.omega,
                   self.u0, self.code, self._stream())
+        if self.rounding == "stochastic" and self.storage in ("f16dev", "bf16dev"):
+            ctr = torch.zeros(1, dtype=torch.int64, device=self.device)
+            _lib.call("lbgb_run_fused_sr", warm[0].data_ptr(), warm[1].data_ptr(), 2, self.ny, self.bcode,
+                      self.omega, self.u0, self.code, 1, self.seed, ctr.data_ptr(), ctypes.byref(ctypes.c_int(0)),
+                      self._stream())
         torch.cuda.current_stream(self.device).synchronize()
         s = torch.cuda.Stream(device=self.device)
         s.wait_stream(torch.cuda.current_stream(self.device))
