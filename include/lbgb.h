@@ -158,6 +158,41 @@ LBGB_API int lbgb_mass_momentum_noalloc(const void *f, int64_t n, int64_t chan_s
 LBGB_API int lbgb_convert(const void *src, int src_dtype, int64_t src_stride, void *dst,
                  int dst_dtype, int64_t dst_stride, int64_t n, void *stream);
 
+/* Batched lattices: many independent (9, nx, ny) lattices of uneven size in
+ * one population buffer, advanced by one launch per step over a packed task
+ * queue.  One table entry per instance (device memory, 8-byte aligned): */
+typedef struct {
+    long long offset;        /* element offset of the instance in the buffer */
+    int nx, ny;              /* its grid */
+    double omega, u0;        /* relaxation parameter, lid velocity (cavity) */
+    int vec;                 /* cells per lane: 16/sizeof(element) if its rows hold whole
+                                16-byte vectors (and offset is a multiple of it), else 1 */
+    unsigned int cell_base;  /* index of its first cell among all instances */
+} lbgb_batch_instance;
+
+/* One fused step of every instance, src -> dst (same layout).  tasks: device
+ * array of n_tasks int4.  Segment tasks (flat = 0) are {instance, first row,
+ * first column, unused}: one warp's work is rows_per_task rows of a
+ * 32*vec-cell row segment.  Flat tasks (flat = 1) are {instance, unused,
+ * first cell, unused}: lane j takes cells first + 32 r + j of the flattened
+ * grid for r < rows_per_task (every lane busy, however short the rows).
+ * total_elems bounds every access (entries that do not fit are skipped).
+ * threads: multiple of 32 up to 256; blocks: persistent grid size.
+ * Replaces the reference's loop over independent runs of
+ * simulators/serial_shear_wave/Python/shear_wave_opt2.py:94-99 (one process
+ * per run) with one launch. */
+LBGB_API int lbgb_batch_step(const void *src, void *dst, long long total_elems,
+                             const void *instances, int n_instances, const void *tasks,
+                             long long n_tasks, int rows_per_task, int boundary, int dtype,
+                             int threads, int blocks, int flat, void *stream);
+
+/* Per-instance amplitude of the shear mode u_x ~ sin(2 pi l / ny):
+ * out_dev[b] = 2/(nx ny) sum_{k,l} u_x(k,l) sin(2 pi l / ny), in FP64.
+ * The decay diagnostic of shear_wave_opt1.py:174 / shear_wave_decay.py:155-158. */
+LBGB_API int lbgb_batch_shear_amplitude(const void *f, long long total_elems,
+                                        const void *instances, int n_instances, int dtype,
+                                        double *out_dev, void *stream);
+
 /* Launch tuning (process-wide; used by the autotuner and the tests).
  *   LBGB_TUNE_KERNEL          0 auto, 1 register kernel, 2 pipelined kernel
  *   LBGB_TUNE_STAGES          shared-memory stages of the pipelined kernel

@@ -55,6 +55,8 @@ SIGNATURES = {
     "lbgb_mass_momentum": (_I, [_P, _I64, _I64, _I, _P, _P, _SZ, _P]),
     "lbgb_mass_momentum_noalloc": (_I, [_P, _I64, _I64, _I, _P, _P]),
     "lbgb_convert": (_I, [_P, _I, _I64, _P, _I, _I64, _I64, _P]),
+    "lbgb_batch_step": (_I, [_P, _P, ctypes.c_longlong, _P, _I, _P, ctypes.c_longlong, _I, _I, _I, _I, _I, _I, _P]),
+    "lbgb_batch_shear_amplitude": (_I, [_P, ctypes.c_longlong, _P, _I, _I, _P, _P]),
     "lbgb_set_tuning": (_I, [_I, ctypes.c_longlong]),
     "lbgb_get_tuning": (ctypes.c_longlong, [_I]),
     "lbgb_device_status": (_I, [_I]),

@@ -106,102 +106,115 @@ __device__ __forceinline__ void pull_channel(typename C::real (&o)[V], const typ
 template <int DT, int V>
 constexpr int min_blocks() { return (sizeof(typename Codec<DT>::raw) == 2 && V == 8) ? 2 : 3; }
 
+// One warp segment of one row: lane `lane` owns cells (k, l0 .. l0+V-1) of a
+// (9, nx, ny) lattice at src/dst.  Shared by the single-lattice kernel and
+// the batched multi-lattice kernel.
+template <int DT, int BC, bool COLLIDE, int V>
+__device__ __forceinline__ void step_segment(const typename Codec<DT>::raw *__restrict__ src,
+                                             typename Codec<DT>::raw *__restrict__ dst, int nx, int ny, int k,
+                                             int l0, int lane, typename Codec<DT>::real omega,
+                                             typename Codec<DT>::real u0,
+                                             const unsigned long long *__restrict__ sr_step, uint32_t sr_seed,
+                                             uint32_t cell_base) {
+    using C = Codec<DT>;
+    using real = typename C::real;
+    using raw = typename C::raw;
+    const size_t cs = (size_t)nx * ny;
+    const bool act = l0 < ny;
+    int km = k - 1, kp = k + 1;
+    bool wl = false, wr = false;
+    if (BC == LBGB_PERIODIC) {
+        if (km < 0) km += nx;
+        if (kp >= nx) kp -= nx;
+    } else {
+        wl = (k == 0);
+        wr = (k == nx - 1);
+    }
+    real v[9][V];
+    pull_channel<C, V, BC, C0>(v[C0], src, cs, ny, k, k, false, l0, lane, act);
+    pull_channel<C, V, BC, CE>(v[CE], src, cs, ny, k, km, wl, l0, lane, act);
+    pull_channel<C, V, BC, CN>(v[CN], src, cs, ny, k, k, false, l0, lane, act);
+    pull_channel<C, V, BC, CW>(v[CW], src, cs, ny, k, kp, wr, l0, lane, act);
+    pull_channel<C, V, BC, CS>(v[CS], src, cs, ny, k, k, false, l0, lane, act);
+    pull_channel<C, V, BC, CNE>(v[CNE], src, cs, ny, k, km, wl, l0, lane, act);
+    pull_channel<C, V, BC, CNW>(v[CNW], src, cs, ny, k, kp, wr, l0, lane, act);
+    pull_channel<C, V, BC, CSW>(v[CSW], src, cs, ny, k, kp, wr, l0, lane, act);
+    pull_channel<C, V, BC, CSE>(v[CSE], src, cs, ny, k, km, wl, l0, lane, act);
+
+    if (BC == LBGB_CAVITY && act) {
+        if (l0 == 0) {
+            // bottom wall: N, NE, NW bounce back from the same node
+            v[CN][0] = load_one<C>(src, cs, ny, CS, k, 0);
+            v[CNE][0] = load_one<C>(src, cs, ny, CSW, k, 0);
+            v[CNW][0] = load_one<C>(src, cs, ny, CSE, k, 0);
+        }
+        if (l0 + V == ny) {
+            // lid: S bounces back; SE/SW get the Ladd term 6 w rho_lid u0,
+            // except at the corner where the side wall wins (plain bounce-back)
+            const int T = ny - 1;
+            const int kw = (k == 0) ? nx - 1 : k - 1;  // periodic neighbours, as
+            const int ke = (k == nx - 1) ? 0 : k + 1;  // the reference's roll reads them
+            const real gN = load_one<C>(src, cs, ny, CN, k, T);
+            const real gNW = load_one<C>(src, cs, ny, CNW, k, T);
+            const real gNE = load_one<C>(src, cs, ny, CNE, k, T);
+            const real rho_lid = gNW + gN + gNE + load_one<C>(src, cs, ny, CNW, ke, T - 1) +
+                                 load_one<C>(src, cs, ny, CN, k, T - 1) +
+                                 load_one<C>(src, cs, ny, CNE, kw, T - 1) +
+                                 load_one<C>(src, cs, ny, CW, ke, T) + load_one<C>(src, cs, ny, C0, k, T) +
+                                 load_one<C>(src, cs, ny, CE, kw, T);
+            const real lid = (real(6) * real(1.0 / 36.0)) * rho_lid * u0;
+            v[CS][V - 1] = gN;
+            v[CSE][V - 1] = (k == 0) ? gNW : gNW + lid;
+            v[CSW][V - 1] = (k == nx - 1) ? gNE : gNE - lid;
+        }
+    }
+
+    raw out[9][V];
+    if (COLLIDE) {
+        uint32_t key = 0;
+        if constexpr (sizeof(raw) == 2) {
+            if (sr_step) key = sr_step_key(sr_seed, *sr_step);
+        }
+#pragma unroll
+        for (int j = 0; j < V; ++j) {
+            real f[9];
+            raw r[9];
+#pragma unroll
+            for (int i = 0; i < 9; ++i) f[i] = v[i][j];
+            if constexpr (sizeof(raw) == 2) {
+                if (sr_step)
+                    collide_encode_sr<DT>(f, omega, r, key, cell_base + (uint32_t)((size_t)k * ny + l0 + j));
+                else
+                    collide_encode<DT>(f, omega, r);
+            } else {
+                collide_encode<DT>(f, omega, r);
+            }
+#pragma unroll
+            for (int i = 0; i < 9; ++i) out[i][j] = r[i];
+        }
+    } else {
+#pragma unroll
+        for (int i = 0; i < 9; ++i)
+#pragma unroll
+            for (int j = 0; j < V; ++j) out[i][j] = C::enc(v[i][j], i);
+    }
+    if (act) {
+#pragma unroll
+        for (int i = 0; i < 9; ++i) stv<raw, V>(dst + (size_t)i * cs + (size_t)k * ny + l0, out[i]);
+    }
+}
+
 template <int DT, int BC, bool COLLIDE, int V>
 __global__ void __launch_bounds__(256, min_blocks<DT, V>())
 k_step(const typename Codec<DT>::raw *__restrict__ src, typename Codec<DT>::raw *__restrict__ dst, int nx,
        int ny, int segs, long long tasks, typename Codec<DT>::real omega, typename Codec<DT>::real u0,
        const unsigned long long *__restrict__ sr_step, uint32_t sr_seed) {
-    using C = Codec<DT>;
-    using real = typename C::real;
-    using raw = typename C::raw;
     const int lane = threadIdx.x & 31;
     const long long nwarps = ((long long)gridDim.x * blockDim.x) >> 5;
-    const size_t cs = (size_t)nx * ny;
     for (long long t = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5; t < tasks; t += nwarps) {
         const int k = (int)(t / segs);
         const int l0 = (int)(t - (long long)k * segs) * (32 * V) + lane * V;
-        const bool act = l0 < ny;
-        int km = k - 1, kp = k + 1;
-        bool wl = false, wr = false;
-        if (BC == LBGB_PERIODIC) {
-            if (km < 0) km += nx;
-            if (kp >= nx) kp -= nx;
-        } else {
-            wl = (k == 0);
-            wr = (k == nx - 1);
-        }
-        real v[9][V];
-        pull_channel<C, V, BC, C0>(v[C0], src, cs, ny, k, k, false, l0, lane, act);
-        pull_channel<C, V, BC, CE>(v[CE], src, cs, ny, k, km, wl, l0, lane, act);
-        pull_channel<C, V, BC, CN>(v[CN], src, cs, ny, k, k, false, l0, lane, act);
-        pull_channel<C, V, BC, CW>(v[CW], src, cs, ny, k, kp, wr, l0, lane, act);
-        pull_channel<C, V, BC, CS>(v[CS], src, cs, ny, k, k, false, l0, lane, act);
-        pull_channel<C, V, BC, CNE>(v[CNE], src, cs, ny, k, km, wl, l0, lane, act);
-        pull_channel<C, V, BC, CNW>(v[CNW], src, cs, ny, k, kp, wr, l0, lane, act);
-        pull_channel<C, V, BC, CSW>(v[CSW], src, cs, ny, k, kp, wr, l0, lane, act);
-        pull_channel<C, V, BC, CSE>(v[CSE], src, cs, ny, k, km, wl, l0, lane, act);
-
-        if (BC == LBGB_CAVITY && act) {
-            if (l0 == 0) {
-                // bottom wall: N, NE, NW bounce back from the same node
-                v[CN][0] = load_one<C>(src, cs, ny, CS, k, 0);
-                v[CNE][0] = load_one<C>(src, cs, ny, CSW, k, 0);
-                v[CNW][0] = load_one<C>(src, cs, ny, CSE, k, 0);
-            }
-            if (l0 + V == ny) {
-                // lid: S bounces back; SE/SW get the Ladd term 6 w rho_lid u0,
-                // except at the corner where the side wall wins (plain bounce-back)
-                const int T = ny - 1;
-                const int kw = (k == 0) ? nx - 1 : k - 1;  // periodic neighbours, as
-                const int ke = (k == nx - 1) ? 0 : k + 1;  // the reference's roll reads them
-                const real gN = load_one<C>(src, cs, ny, CN, k, T);
-                const real gNW = load_one<C>(src, cs, ny, CNW, k, T);
-                const real gNE = load_one<C>(src, cs, ny, CNE, k, T);
-                const real rho_lid = gNW + gN + gNE + load_one<C>(src, cs, ny, CNW, ke, T - 1) +
-                                     load_one<C>(src, cs, ny, CN, k, T - 1) +
-                                     load_one<C>(src, cs, ny, CNE, kw, T - 1) +
-                                     load_one<C>(src, cs, ny, CW, ke, T) + load_one<C>(src, cs, ny, C0, k, T) +
-                                     load_one<C>(src, cs, ny, CE, kw, T);
-                const real lid = (real(6) * real(1.0 / 36.0)) * rho_lid * u0;
-                v[CS][V - 1] = gN;
-                v[CSE][V - 1] = (k == 0) ? gNW : gNW + lid;
-                v[CSW][V - 1] = (k == nx - 1) ? gNE : gNE - lid;
-            }
-        }
-
-        raw out[9][V];
-        if (COLLIDE) {
-            uint32_t key = 0;
-            if constexpr (sizeof(raw) == 2) {
-                if (sr_step) key = sr_step_key(sr_seed, *sr_step);
-            }
-#pragma unroll
-            for (int j = 0; j < V; ++j) {
-                real f[9];
-                raw r[9];
-#pragma unroll
-                for (int i = 0; i < 9; ++i) f[i] = v[i][j];
-                if constexpr (sizeof(raw) == 2) {
-                    if (sr_step)
-                        collide_encode_sr<DT>(f, omega, r, key, (uint32_t)((size_t)k * ny + l0 + j));
-                    else
-                        collide_encode<DT>(f, omega, r);
-                } else {
-                    collide_encode<DT>(f, omega, r);
-                }
-#pragma unroll
-                for (int i = 0; i < 9; ++i) out[i][j] = r[i];
-            }
-        } else {
-#pragma unroll
-            for (int i = 0; i < 9; ++i)
-#pragma unroll
-                for (int j = 0; j < V; ++j) out[i][j] = C::enc(v[i][j], i);
-        }
-        if (act) {
-#pragma unroll
-            for (int i = 0; i < 9; ++i) stv<raw, V>(dst + (size_t)i * cs + (size_t)k * ny + l0, out[i]);
-        }
+        step_segment<DT, BC, COLLIDE, V>(src, dst, nx, ny, k, l0, lane, omega, u0, sr_step, sr_seed, 0u);
     }
 }
 
@@ -413,6 +426,8 @@ extern "C" int lbgb_run_fused(void *a, void *b, int nx, int ny, int boundary, do
 namespace lbgb {
 __global__ void k_bump_step(unsigned long long *ctr) { *ctr += 1; }
 }  // namespace lbgb
+
+#include "lbgb_batch.cuh"
 
 extern "C" int lbgb_run_fused_sr(void *a, void *b, int nx, int ny, int boundary, double omega, double u0, int dtype,
                                  int nsteps, unsigned int seed, unsigned long long *step_counter, int *which,

@@ -1,0 +1,111 @@
+"""Batched uneven lattices (one launch per step over a packed task queue)."""
+
+import math
+
+import numpy as np
+import pytest
+import torch
+
+from latticeboltzmann_gb300 import batch as B
+from latticeboltzmann_gb300 import _lib
+from oracle import d2q9 as oracle
+from oracle import port
+
+pytestmark = pytest.mark.gpu
+
+
+def test_batch_matches_oracle_per_instance(cuda):
+    """Every instance of an uneven FP64 batch equals its own oracle run."""
+    sizes = [(32, 16), (17, 40), (64, 33), (5, 8), (40, 130), (3, 3)]
+    omegas = [0.5, 1.0, 1.7, 1.2, 0.9, 1.4]
+    bl = B.BatchedLattice(sizes, omegas, storage="f64", device=cuda).shear_wave(0.05)
+    for cfg in ({"vector": True, "rows": 1, "threads": 256, "blocks": 64},
+                {"vector": False, "rows": 3, "threads": 128, "blocks": 7},
+                {"flat": True, "vector": False, "rows": 1, "threads": 256, "blocks": 5},
+                {"flat": True, "vector": False, "rows": 4, "threads": 64, "blocks": 300}):
+        b2 = B.BatchedLattice(sizes, omegas, storage="f64", device=cuda).shear_wave(0.05)
+        b2.step(25, cfg)
+        for b, (nx, ny) in enumerate(sizes):
+            f = oracle.equilibrium(np.ones((nx, ny)), (0.05 * np.sin(2 * np.pi * np.arange(ny) / ny))[None, :]
+                                   * np.ones((nx, 1)), np.zeros((nx, ny)))
+            port.periodic_run(f, omegas[b], 25, nthreads=1)
+            assert np.abs(b2.populations(b).cpu().numpy() - f).max() < 1e-13, (b, cfg)
+    del bl
+
+
+def test_batch_cavity_and_storages_against_single_lattice(cuda):
+    """A batch of cavities equals the same cavities run one by one (same kernel code)."""
+    import latticeboltzmann_gb300 as PyLB
+    sizes = [(24, 16), (33, 40), (8, 64)]
+    for storage in ("f32", "f16dev", "bf16dev"):
+        bl = B.BatchedLattice(sizes, [1.3, 1.6, 0.8], boundary="cavity", u0=0.1, storage=storage, device=cuda)
+        bl.equilibrium(lambda b: (1.0, 0.0, 0.0))
+        flat = B.BatchedLattice(sizes, [1.3, 1.6, 0.8], boundary="cavity", u0=0.1, storage=storage, device=cuda)
+        flat.equilibrium(lambda b: (1.0, 0.0, 0.0))
+        bl.step(12, {"flat": False, "vector": True, "rows": 2, "threads": 256, "blocks": 40})
+        flat.step(12, {"flat": True, "vector": False, "rows": 2, "threads": 128, "blocks": 40})
+        _lib.set_tuning(_lib.TUNE_KERNEL, _lib.KERNELS["register"])
+        try:
+            for b, (nx, ny) in enumerate(sizes):
+                lat = PyLB.Lattice(nx, ny, [1.3, 1.6, 0.8][b], boundary="cavity", u0=0.1, storage=storage,
+                                   device=cuda)
+                lat.step(12)
+                assert torch.equal(lat.populations(torch.float64), bl.populations(b)), (storage, b)
+                assert torch.equal(lat.populations(torch.float64), flat.populations(b)), (storage, b)
+        finally:
+            _lib.set_tuning(_lib.TUNE_KERNEL, _lib.KERNELS["auto"])
+
+
+def test_batch_graph_replay_and_autotune(cuda):
+    sizes, om = B.random_shear_batch(24, seed=3, nx_range=(8, 128), ny_range=(8, 96))
+    a = B.BatchedLattice(sizes, om, storage="f32", device=cuda).shear_wave()
+    b = B.BatchedLattice(sizes, om, storage="f32", device=cuda).shear_wave()
+    best, timings = b.autotune(steps=2, warmup=1)
+    assert len(timings) == len(b.candidates()) and best in [dict(k) for k in timings]
+    assert b.steps_taken == 0
+    replay = b.capture(4)
+    for _ in range(3):
+        replay()
+    a.step(12)
+    torch.cuda.synchronize()
+    assert a.steps_taken == b.steps_taken == 12
+    for i in range(len(sizes)):
+        assert torch.equal(a.populations(i), b.populations(i))
+
+
+def test_shear_amplitude_and_viscosity(cuda):
+    """Config-4 style study on a small uneven batch.
+
+    * The fitted viscosity of the smallest instances equals the fit of the
+      FP64 oracle's run of the same instance within 1e-3 (the FP32 batch vs
+      the reference algorithm).
+    * Where the wave is well resolved (nu k^2 < 0.005 per step) the fit agrees
+      with (1/omega - 1/2)/3 within 3%.  For short, strongly damped waves the
+      lattice's own dispersion departs from the continuum value (ny = 16,
+      omega = 0.3: -45% in the FP64 oracle as well), so theory is not the
+      check there.
+    """
+    every, steps = 10, 1000
+    res = B.shear_study(n=48, steps=steps, every=every, seed=5, device=cuda, tune=False)
+    nu_fit, nu_th = res["nu_fit"], res["nu_theory"]
+    assert np.abs(res["amplitudes"][0] - 0.05).max() < 1e-6
+    ny = np.array([s[1] for s in res["sizes"]])
+    k2nu = (2 * np.pi / ny) ** 2 * nu_th
+    resolved = (k2nu < 0.005) & np.isfinite(nu_fit)
+    assert resolved.sum() >= 10
+    assert np.abs(nu_fit[resolved] / nu_th[resolved] - 1).max() < 0.03
+    cells = np.array([a * b for a, b in res["sizes"]])
+    for b in np.argsort(cells)[:4]:
+        nx, nyb = res["sizes"][b]
+        f = oracle.equilibrium(np.ones((nx, nyb)), (0.05 * np.sin(2 * np.pi * np.arange(nyb) / nyb))[None, :]
+                               * np.ones((nx, 1)), np.zeros((nx, nyb)))
+        kk = 2 * np.pi / nyb
+        amps = [0.05]
+        for _ in range(steps // every):
+            port.periodic_run(f, res["omegas"][b], every, nthreads=1)
+            _, ux, _ = oracle.macroscopic(f)
+            amps.append((ux * np.sin(kk * np.arange(nyb))[None, :]).sum() * 2 / (nx * nyb))
+        ref = B.fit_viscosity(res["times"], amps, nyb)
+        if np.isfinite(ref):
+            assert abs(nu_fit[b] / ref - 1) < 1e-3, (b, nu_fit[b], ref)
+        assert np.abs(res["amplitudes"][:, b] - np.array(amps)).max() < 2e-6
