@@ -43,7 +43,8 @@ extern "C" {
 #define LBGB_BF16DEV 3
 
 #define LBGB_PERIODIC 0
-#define LBGB_CAVITY 1
+#define LBGB_CAVITY 1       /* the reference's lid: 6 w rho_lid u0 with its rho_lid, side walls win at the corners */
+#define LBGB_CAVITY_LADD 2  /* standard Ladd moving wall, wall density 1, at every lid node (steady-state studies) */
 
 #define LBGB_OK 0
 #define LBGB_EINVAL (-1)   /* bad size, pointer or option */
@@ -192,6 +193,61 @@ LBGB_API int lbgb_batch_step(const void *src, void *dst, long long total_elems,
 LBGB_API int lbgb_batch_shear_amplitude(const void *f, long long total_elems,
                                         const void *instances, int n_instances, int dtype,
                                         double *out_dev, void *stream);
+
+/* Steady-state monitor of a batch: out_dev[b] = max over the cells of
+ * instance b of |u - u_prev| (x and y components, FP32), then u_prev <- u.
+ * u_prev: 2 floats per cell, instances back to back at 2*cell_base.
+ * Called every m steps it gives the criterion max|u^(n+m) - u^n| of the
+ * steady-cavity data set.  No counterpart in the reference. */
+LBGB_API int lbgb_batch_velocity_change(const void *f, long long total_elems,
+                                        const void *instances, int n_instances, int dtype,
+                                        float *u_prev, long long total_cells, float *out_dev,
+                                        void *stream);
+
+/* BF16 GEMM with FP32 accumulation: C = alpha * A * B + beta * C for `batch`
+ * independent problems.  A (m x k) and B (k x n) are BF16, C FP32; element
+ * (i, j) of X is X[i * x_rs + j * x_cs] and problem z starts at z * x_bs, so
+ * any transposed or strided view works.  engine: 0/2 tensor cores
+ * (tcgen05.mma, accumulator in tensor memory), 1 CUDA-core reference.  Used
+ * by the Fourier-neural-operator surrogate; no counterpart in the reference. */
+LBGB_API int lbgb_gemm_bf16(int m, int n, int k, const void *A, long long a_rs, long long a_cs,
+                            long long a_bs, const void *B, long long b_rs, long long b_cs,
+                            long long b_bs, float *C, long long c_rs, long long c_cs, long long c_bs,
+                            int batch, float alpha, float beta, int engine, void *stream);
+
+/* Synchronizes and reports whether a bounded wait in the tensor-core GEMM gave
+ * up since the last reset (LBGB_ETIMEOUT).  No counterpart in the reference. */
+LBGB_API int lbgb_gemm_status(int reset);
+
+/* Element-wise and mode-mixing kernels of the Fourier-neural-operator
+ * surrogate (activations channel-major: (channels, cols)).  No counterpart in
+ * the reference.
+ *   to_bf16      y = bf16(x)
+ *   bias_act     z += bias[c] (+ extra); v = act(z) (0 identity, 1 GELU), fp32 and/or bf16
+ *   gelu_back    dz = dy * GELU'(z) (and its bf16 copy)
+ *   row_sum      db[c] = sum_j dy[c, j]
+ *   mix          y[o,b,q] = sum_c x[c,b,q] R[c,o,q] (complex, BF16 weights)
+ *   mix_back     its gradients with respect to x and R
+ *   mse          partial sums of (y - t)^2 and d = 2 (y - t) / n
+ *   adam         Adam step on FP32 weights, refreshing their BF16 copy
+ *   sum_splits   out = beta out + sum of S split-K partial results */
+LBGB_API int lbgb_fno_to_bf16(const float *x, void *y, long long n, void *stream);
+LBGB_API int lbgb_fno_bias_act(float *z, const float *bias, const float *extra, float *v, void *vb,
+                               int channels, long long cols, int act, void *stream);
+LBGB_API int lbgb_fno_gelu_back(const float *dy, const float *z, float *dz, void *dzb, long long n,
+                                void *stream);
+LBGB_API int lbgb_fno_row_sum(const float *dy, float *db, int channels, long long cols, void *stream);
+LBGB_API int lbgb_fno_mix(const float *xr, const float *xi, const void *Rr, const void *Ri, float *yr,
+                          float *yi, int C, int O, int B, int Q, void *stream);
+LBGB_API int lbgb_fno_mix_back(const float *dyr, const float *dyi, const float *xr, const float *xi,
+                               const void *Rr, const void *Ri, float *dxr, float *dxi, float *dRr,
+                               float *dRi, int C, int O, int B, int Q, void *stream);
+LBGB_API int lbgb_fno_mse(const float *y, const float *t, float *d, double *partials, int nparts,
+                          long long n, void *stream);
+LBGB_API int lbgb_fno_adam(float *w, const float *g, float *m, float *v, void *wb, long long n, float lr,
+                           float b1, float b2, float eps, int step, float weight_decay, void *stream);
+LBGB_API int lbgb_fno_sum_splits(const float *parts, float *out, int S, long long n, float beta,
+                                 void *stream);
 
 /* Launch tuning (process-wide; used by the autotuner and the tests).
  *   LBGB_TUNE_KERNEL          0 auto, 1 register kernel, 2 pipelined kernel

@@ -14,12 +14,12 @@ LIB_PATH = os.path.join(HERE, "liblbgb.so")
 # storage codes
 F32, F64, F16DEV, BF16DEV = 0, 1, 2, 3
 # boundary codes
-PERIODIC, CAVITY = 0, 1
+PERIODIC, CAVITY, CAVITY_LADD = 0, 1, 2
 # return codes
 OK, EINVAL, EDTYPE, ECUDA, EWORKSPACE, ETIMEOUT = 0, -1, -2, -3, -4, -5
 
 STORAGE_CODES = {"f32": F32, "f64": F64, "f16dev": F16DEV, "bf16dev": BF16DEV}
-BOUNDARY_CODES = {"periodic": PERIODIC, "cavity": CAVITY}
+BOUNDARY_CODES = {"periodic": PERIODIC, "cavity": CAVITY, "cavity-ladd": CAVITY_LADD}
 
 
 class LBGBError(RuntimeError):
@@ -57,6 +57,21 @@ SIGNATURES = {
     "lbgb_convert": (_I, [_P, _I, _I64, _P, _I, _I64, _I64, _P]),
     "lbgb_batch_step": (_I, [_P, _P, ctypes.c_longlong, _P, _I, _P, ctypes.c_longlong, _I, _I, _I, _I, _I, _I, _P]),
     "lbgb_batch_shear_amplitude": (_I, [_P, ctypes.c_longlong, _P, _I, _I, _P, _P]),
+    "lbgb_batch_velocity_change": (_I, [_P, ctypes.c_longlong, _P, _I, _I, _P, ctypes.c_longlong, _P, _P]),
+    "lbgb_gemm_bf16": (_I, [_I, _I, _I, _P, ctypes.c_longlong, ctypes.c_longlong, ctypes.c_longlong, _P,
+                            ctypes.c_longlong, ctypes.c_longlong, ctypes.c_longlong, _P, ctypes.c_longlong,
+                            ctypes.c_longlong, ctypes.c_longlong, _I, ctypes.c_float, ctypes.c_float, _I, _P]),
+    "lbgb_gemm_status": (_I, [_I]),
+    "lbgb_fno_to_bf16": (_I, [_P, _P, ctypes.c_longlong, _P]),
+    "lbgb_fno_bias_act": (_I, [_P, _P, _P, _P, _P, _I, ctypes.c_longlong, _I, _P]),
+    "lbgb_fno_gelu_back": (_I, [_P, _P, _P, _P, ctypes.c_longlong, _P]),
+    "lbgb_fno_row_sum": (_I, [_P, _P, _I, ctypes.c_longlong, _P]),
+    "lbgb_fno_mix": (_I, [_P, _P, _P, _P, _P, _P, _I, _I, _I, _I, _P]),
+    "lbgb_fno_mix_back": (_I, [_P, _P, _P, _P, _P, _P, _P, _P, _P, _P, _I, _I, _I, _I, _P]),
+    "lbgb_fno_mse": (_I, [_P, _P, _P, _P, _I, ctypes.c_longlong, _P]),
+    "lbgb_fno_adam": (_I, [_P, _P, _P, _P, _P, ctypes.c_longlong, ctypes.c_float, ctypes.c_float, ctypes.c_float,
+                           ctypes.c_float, _I, ctypes.c_float, _P]),
+    "lbgb_fno_sum_splits": (_I, [_P, _P, _I, ctypes.c_longlong, ctypes.c_float, _P]),
     "lbgb_set_tuning": (_I, [_I, ctypes.c_longlong]),
     "lbgb_get_tuning": (ctypes.c_longlong, [_I]),
     "lbgb_device_status": (_I, [_I]),

@@ -33,8 +33,9 @@ def _sm_count(device):
 class BatchedLattice:
     """Independent lattices ``sizes[b] = (nx_b, ny_b)`` with relaxation ``omegas[b]``.
 
-    boundary: "periodic" (the default; shear-wave studies) or "cavity" (lid
-    velocity ``u0`` for every instance).  storage as for ``Lattice``.
+    boundary: "periodic" (the default; shear-wave studies), "cavity" (the
+    reference's lid) or "cavity-ladd" (wall-density-1 lid, steady states);
+    lid velocity ``u0``, a scalar or one per instance.  storage as for ``Lattice``.
     """
 
     def __init__(self, sizes, omegas, boundary="periodic", u0=0.0, storage="f32", device=None):
@@ -43,27 +44,29 @@ class BatchedLattice:
         if storage not in _RAW:
             raise ValueError("storage must be one of %s" % sorted(_RAW))
         if boundary not in _lib.BOUNDARY_CODES:
-            raise ValueError("boundary must be 'cavity' or 'periodic'")
+            raise ValueError("boundary must be one of %s" % sorted(_lib.BOUNDARY_CODES))
         self.device = torch.device(device) if device is not None else torch.device("cuda", torch.cuda.current_device())
         if self.device.type != "cuda":
             raise TypeError("BatchedLattice lives on a CUDA device (there is no CPU path)")
         self.sizes = [(int(a), int(b)) for a, b in sizes]
         for nx, ny in self.sizes:
-            if nx <= 0 or ny <= 0 or (boundary == "cavity" and (nx < 2 or ny < 2)):
+            if nx <= 0 or ny <= 0 or (boundary != "periodic" and (nx < 2 or ny < 2)):
                 raise ValueError("invalid instance size %dx%d" % (nx, ny))
         self.omegas = np.asarray(omegas, dtype=np.float64)
         self.n = len(self.sizes)
         self.boundary, self.storage = boundary, storage
         self.code = _lib.STORAGE_CODES[storage]
         self.bcode = _lib.BOUNDARY_CODES[boundary]
-        self.u0 = float(u0) if boundary == "cavity" else 0.0
+        u0s = np.broadcast_to(np.asarray(u0, dtype=np.float64), (self.n,)) if boundary != "periodic" \
+            else np.zeros(self.n)
+        self.u0s = np.array(u0s, dtype=np.float64)
         raw = _RAW[storage]
         es = torch.empty(0, dtype=raw).element_size()
         self.vw = 16 // es
         table = np.zeros(self.n, dtype=INSTANCE_DTYPE)
         off, cell = 0, 0
         for b, (nx, ny) in enumerate(self.sizes):
-            table[b] = (off, nx, ny, self.omegas[b], self.u0, self.vw if ny % self.vw == 0 else 1, cell)
+            table[b] = (off, nx, ny, self.omegas[b], self.u0s[b], self.vw if ny % self.vw == 0 else 1, cell)
             off += -(-9 * nx * ny // self.vw) * self.vw  # next instance starts on a 16-byte boundary
             cell += nx * ny
         self.total = off
@@ -77,6 +80,8 @@ class BatchedLattice:
         self.config = {"flat": True, "vector": False, "rows": 2, "threads": 256, "blocks": n_sm * 8}
         self._tasks = {}
         self._amp = torch.empty(self.n, dtype=torch.float64, device=self.device)
+        self.active = np.ones(self.n, dtype=bool)  # instances that still advance
+        self._u_prev = None
 
     # ------------------------------------------------------------ tables and queues
     def _table(self, vector):
@@ -94,7 +99,7 @@ class BatchedLattice:
         of a 32*V-cell segment.  Flat tasks: (instance, 0, first cell, 0), one
         warp per 32*``rows`` consecutive cells of the flattened grid.
         """
-        key = (bool(vector), int(rows), bool(flat))
+        key = (bool(vector), int(rows), bool(flat), None)
         if key not in self._tasks:
             parts = []
             for b, (nx, ny) in enumerate(self.sizes):
@@ -170,9 +175,35 @@ class BatchedLattice:
         return out
 
     # ------------------------------------------------------------ stepping
+    def set_active(self, mask):
+        """Advance only the instances where ``mask`` is true (the others keep
+        their state: their tasks leave the queue)."""
+        mask = np.asarray(mask, dtype=bool).copy()
+        other = self._buf[1 - self._cur]
+        for b in np.nonzero(self.active & ~mask)[0]:
+            # both ping-pong buffers hold the frozen state from now on
+            self._slice(int(b), other).copy_(self._slice(int(b)))
+        self.active = mask
+        self._tasks = {k: v for k, v in self._tasks.items() if k[3] is None}
+
+    def _queue(self, cfg):
+        flat = bool(cfg.get("flat", False))
+        full = self.task_queue(cfg["vector"], cfg["rows"], flat)
+        if self.active.all():
+            return full
+        key = (bool(cfg["vector"]), int(cfg["rows"]), flat, self.active.tobytes())
+        if key not in self._tasks:
+            keep = torch.from_numpy(self.active).to(self.device)[full[:, 0].long()]
+            self._tasks[key] = full[keep].contiguous()
+        return self._tasks[key]
+
     def _launch(self, src, dst, cfg):
         flat = bool(cfg.get("flat", False))
-        tasks = self.task_queue(cfg["vector"], cfg["rows"], flat)
+        tasks = self._queue(cfg)
+        if tasks.shape[0] == 0:
+            # nothing advances: keep the ping-pong consistent with a copy
+            dst.copy_(src)
+            return
         _lib.call("lbgb_batch_step", src.data_ptr(), dst.data_ptr(), self.total, self._table(cfg["vector"]).data_ptr(),
                   self.n, tasks.data_ptr(), tasks.shape[0], cfg["rows"], self.bcode, self.code, cfg["threads"],
                   cfg["blocks"], int(flat), self._stream())
@@ -223,6 +254,25 @@ class BatchedLattice:
         _lib.call("lbgb_batch_shear_amplitude", self.state.data_ptr(), self.total, self._table(True).data_ptr(),
                   self.n, self.code, out.data_ptr(), self._stream())
         return out
+
+    def velocity_change(self):
+        """Per-instance max |u - u_prev| since the previous call (FP32 device
+        tensor; inf on the first call), and u_prev <- u."""
+        out = torch.empty(self.n, dtype=torch.float32, device=self.device)
+        first = self._u_prev is None
+        if first:
+            self._u_prev = torch.zeros(2 * self.cells, dtype=torch.float32, device=self.device)
+        _lib.call("lbgb_batch_velocity_change", self.state.data_ptr(), self.total, self._table(True).data_ptr(),
+                  self.n, self.code, self._u_prev.data_ptr(), self.cells, out.data_ptr(), self._stream())
+        if first:
+            out.fill_(float("inf"))
+        return out
+
+    def fields(self, b):
+        """(rho, ux, uy) of instance b as float32 (nx, ny) tensors."""
+        from .solver import macroscopic
+        f = self.populations(b, torch.float32)
+        return macroscopic(f)
 
     # ------------------------------------------------------------ tuning
     def candidates(self):
@@ -322,3 +372,50 @@ def shear_study(n=512, steps=5000, every=10, seed=0, amplitude=0.05, storage="f3
             "elapsed_s": elapsed, "cells": bl.cells, "steps": steps,
             "mlups_incl_diagnostics": bl.cells * steps / elapsed / 1e6, "config": bl.config,
             "tuning": tuned[1] if tuned else None}
+
+
+def omega_for(re, u_lid, length):
+    """Relaxation parameter of a cavity of side ``length`` at Reynolds number re."""
+    return 2.0 * re / (6.0 * length * u_lid + re)
+
+
+def steady_cavities(re, u_lid, n=256, tol=1e-7, every=1000, max_steps=1_000_000, storage="f32", device=None,
+                    tune=True, log=None, boundary="cavity-ladd"):
+    """Run lid-driven cavities (n x n) to steady state, all in one batch.
+
+    The default lid is the wall-density-1 one: the reference's lid adds mass
+    every step, so above Re ~ 100 its cavities never settle.
+
+    Steady: max over the cavity of |u^(t+every) - u^t| < tol.  Converged
+    instances leave the task queue.  Returns (fields float32 (N, 3, n, n) of
+    rho, ux, uy; steps to convergence per instance, -1 if max_steps passed;
+    wall seconds).
+    """
+    re = np.asarray(re, dtype=np.float64)
+    u_lid = np.asarray(u_lid, dtype=np.float64)
+    om = omega_for(re, u_lid, n)
+    bl = BatchedLattice([(n, n)] * len(re), om, boundary=boundary, u0=u_lid, storage=storage, device=device)
+    bl.equilibrium(lambda b: (1.0, 0.0, 0.0))
+    if tune:
+        bl.autotune(steps=3, warmup=1)
+    bl.velocity_change()
+    steps = np.full(len(re), -1, dtype=np.int64)
+    t0 = time.perf_counter()
+    done = 0
+    while done < max_steps and (steps < 0).any():
+        bl.step(every)
+        done += every
+        ch = bl.velocity_change().cpu().numpy()
+        newly = (steps < 0) & (ch < tol)
+        steps[newly] = done
+        if newly.any():
+            bl.set_active(steps < 0)
+        if log is not None and done % (every * 50) == 0:
+            log("steady_cavities: %d steps, %d/%d converged" % (done, int((steps >= 0).sum()), len(re)))
+    torch.cuda.synchronize(bl.device)
+    wall = time.perf_counter() - t0
+    out = torch.empty((len(re), 3, n, n), dtype=torch.float32, device=bl.device)
+    for b in range(len(re)):
+        r, x, y = bl.fields(b)
+        out[b, 0], out[b, 1], out[b, 2] = r, x, y
+    return out, steps, wall

@@ -41,7 +41,7 @@ k_batch_step(const typename Codec<DT>::raw *__restrict__ src, typename Codec<DT>
         const BatchInstanceDev in = inst[tk.x];
         const long long need = 9ll * in.nx * in.ny;
         if (in.nx <= 0 || in.ny <= 0 || in.offset < 0 || in.offset + need > total_elems) continue;
-        if (BC == LBGB_CAVITY && (in.nx < 2 || in.ny < 2)) continue;
+        if (BC != LBGB_PERIODIC && (in.nx < 2 || in.ny < 2)) continue;
         if (tk.y < 0 || tk.z < 0 || tk.z >= in.ny) continue;
         const bool wide = in.vec == VW && in.ny % VW == 0 && tk.z % VW == 0 && in.offset % VW == 0;
         for (int r = 0; r < rows_per_task; ++r) {
@@ -80,6 +80,11 @@ __device__ __forceinline__ void pull_cell(const typename C::raw *__restrict__ sr
             v[i] = C::dec(ld1(src + opp(i) * n + (long long)k * ny + l), i);
         }
     }
+    if (BC == LBGB_CAVITY_LADD && l == ny - 1) {
+        const real lid = real(6) * real(1.0 / 36.0) * u0;
+        v[CSE] += lid;  // bounce-back of NW (set above) plus the wall term, every lid node
+        v[CSW] -= lid;
+    }
     if (BC == LBGB_CAVITY && l == ny - 1) {
         const int T = ny - 1;
         const int kw = (k == 0) ? nx - 1 : k - 1;
@@ -110,7 +115,7 @@ k_batch_step_flat(const typename Codec<DT>::raw *__restrict__ src, typename Code
         const BatchInstanceDev in = inst[tk.x];
         const long long n = (long long)in.nx * in.ny;
         if (in.nx <= 0 || in.ny <= 0 || in.offset < 0 || in.offset + 9 * n > total_elems) continue;
-        if (BC == LBGB_CAVITY && (in.nx < 2 || in.ny < 2)) continue;
+        if (BC != LBGB_PERIODIC && (in.nx < 2 || in.ny < 2)) continue;
         const raw *s = src + in.offset;
         raw *d = dst + in.offset;
         for (int r = 0; r < rounds; ++r) {
@@ -165,6 +170,51 @@ k_batch_shear_amplitude(const typename Codec<DT>::raw *__restrict__ f, long long
     if (threadIdx.x == 0) out[b] = ok ? sm[0] * 2.0 / (double)n : 0.0;
 }
 
+// Steady-state monitor: per instance, max over cells of |u - u_prev| (both
+// components), then u_prev <- u.  u_prev holds 2 floats per cell, instances
+// back to back in cell_base order.  One block per instance.
+template <int DT>
+__global__ void __launch_bounds__(256)
+k_batch_velocity_change(const typename Codec<DT>::raw *__restrict__ f, long long total_elems,
+                        const BatchInstanceDev *__restrict__ inst, int n_inst, float *__restrict__ u_prev,
+                        long long total_cells, float *__restrict__ out) {
+    using C = Codec<DT>;
+    const int b = blockIdx.x;
+    if (b >= n_inst) return;
+    const BatchInstanceDev in = inst[b];
+    const long long n = (long long)in.nx * in.ny;
+    const bool ok = in.nx > 0 && in.ny > 0 && in.offset >= 0 && in.offset + 9 * n <= total_elems &&
+                    (long long)in.cell_base + n <= total_cells;
+    float m = 0.f;
+    if (ok) {
+        const typename C::raw *g = f + in.offset;
+        float *up = u_prev + 2ll * in.cell_base;
+        for (long long c = threadIdx.x; c < n; c += blockDim.x) {
+            typename C::real v[9];
+#pragma unroll
+            for (int i = 0; i < 9; ++i) v[i] = C::dec(g[i * n + c], i);
+            typename C::real rho = v[0];
+#pragma unroll
+            for (int i = 1; i < 9; ++i) rho += v[i];
+            const float ux = (float)((v[1] - v[3] + v[5] - v[6] - v[7] + v[8]) / rho);
+            const float uy = (float)((v[2] - v[4] + v[5] + v[6] - v[7] - v[8]) / rho);
+            m = fmaxf(m, fmaxf(fabsf(ux - up[2 * c]), fabsf(uy - up[2 * c + 1])));
+            up[2 * c] = ux;
+            up[2 * c + 1] = uy;
+        }
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_down_sync(0xffffffffu, m, o));
+    __shared__ float sm[8];
+    if ((threadIdx.x & 31) == 0) sm[threadIdx.x >> 5] = m;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        float r = 0.f;
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) r = fmaxf(r, sm[w]);
+        out[b] = ok ? r : -1.f;
+    }
+}
+
 template <int DT, int BC>
 static int launch_batch(const void *src, void *dst, long long total, const void *inst, int n_inst, const void *tasks,
                         long long n_tasks, int rows, int threads, int blocks, int flat, cudaStream_t s) {
@@ -196,7 +246,7 @@ extern "C" int lbgb_batch_step(const void *src, void *dst, long long total_elems
         set_error("lbgb_batch_step: null buffer or empty batch");
         return LBGB_EINVAL;
     }
-    if (boundary != LBGB_PERIODIC && boundary != LBGB_CAVITY) {
+    if (boundary != LBGB_PERIODIC && boundary != LBGB_CAVITY && boundary != LBGB_CAVITY_LADD) {
         set_error("lbgb_batch_step: unknown boundary code %d", boundary);
         return LBGB_EINVAL;
     }
@@ -218,11 +268,14 @@ extern "C" int lbgb_batch_step(const void *src, void *dst, long long total_elems
     cudaStream_t s = (cudaStream_t)stream;
 #define LBGB_BATCH_CASE(DTV)                                                                                   \
     case DTV:                                                                                                  \
-        return boundary == LBGB_CAVITY                                                                         \
-                   ? launch_batch<DTV, LBGB_CAVITY>(src, dst, total_elems, instances, n_instances, tasks,      \
-                                                    n_tasks, rows_per_task, threads, blocks, flat, s)          \
-                   : launch_batch<DTV, LBGB_PERIODIC>(src, dst, total_elems, instances, n_instances, tasks,    \
-                                                      n_tasks, rows_per_task, threads, blocks, flat, s);
+        if (boundary == LBGB_CAVITY)                                                                           \
+            return launch_batch<DTV, LBGB_CAVITY>(src, dst, total_elems, instances, n_instances, tasks, n_tasks, \
+                                                  rows_per_task, threads, blocks, flat, s);                    \
+        if (boundary == LBGB_CAVITY_LADD)                                                                      \
+            return launch_batch<DTV, LBGB_CAVITY_LADD>(src, dst, total_elems, instances, n_instances, tasks,   \
+                                                       n_tasks, rows_per_task, threads, blocks, flat, s);      \
+        return launch_batch<DTV, LBGB_PERIODIC>(src, dst, total_elems, instances, n_instances, tasks, n_tasks,  \
+                                                rows_per_task, threads, blocks, flat, s);
     switch (dtype) {
         LBGB_BATCH_CASE(LBGB_F32)
         LBGB_BATCH_CASE(LBGB_F64)
@@ -266,4 +319,41 @@ extern "C" int lbgb_batch_shear_amplitude(const void *f, long long total_elems, 
     default: set_error("lbgb_batch_shear_amplitude: unsupported storage code %d", dtype); return LBGB_EDTYPE;
     }
     return check_launch("k_batch_shear_amplitude");
+}
+
+extern "C" int lbgb_batch_velocity_change(const void *f, long long total_elems, const void *instances,
+                                          int n_instances, int dtype, float *u_prev, long long total_cells,
+                                          float *out_dev, void *stream) {
+    using namespace lbgb;
+    if (!f || !instances || !u_prev || !out_dev || n_instances <= 0 || total_elems <= 0 || total_cells <= 0) {
+        set_error("lbgb_batch_velocity_change: null buffer or empty batch");
+        return LBGB_EINVAL;
+    }
+    if (!aligned(instances, 8) || !aligned(u_prev, 8)) {
+        set_error("lbgb_batch_velocity_change: instance table and u_prev must be 8-byte aligned");
+        return LBGB_EINVAL;
+    }
+    cudaStream_t s = (cudaStream_t)stream;
+    const auto *in = static_cast<const BatchInstanceDev *>(instances);
+    switch (dtype) {
+    case LBGB_F32:
+        k_batch_velocity_change<LBGB_F32><<<n_instances, 256, 0, s>>>((const float *)f, total_elems, in, n_instances,
+                                                                      u_prev, total_cells, out_dev);
+        break;
+    case LBGB_F64:
+        k_batch_velocity_change<LBGB_F64><<<n_instances, 256, 0, s>>>((const double *)f, total_elems, in,
+                                                                      n_instances, u_prev, total_cells, out_dev);
+        break;
+    case LBGB_F16DEV:
+        k_batch_velocity_change<LBGB_F16DEV><<<n_instances, 256, 0, s>>>((const unsigned short *)f, total_elems, in,
+                                                                         n_instances, u_prev, total_cells, out_dev);
+        break;
+    case LBGB_BF16DEV:
+        k_batch_velocity_change<LBGB_BF16DEV><<<n_instances, 256, 0, s>>>((const unsigned short *)f, total_elems,
+                                                                          in, n_instances, u_prev, total_cells,
+                                                                          out_dev);
+        break;
+    default: set_error("lbgb_batch_velocity_change: unsupported storage code %d", dtype); return LBGB_EDTYPE;
+    }
+    return check_launch("k_batch_velocity_change");
 }

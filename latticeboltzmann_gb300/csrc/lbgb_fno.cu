@@ -1,0 +1,256 @@
+// Element-wise and mode-mixing kernels of the Fourier-neural-operator
+// surrogate (the GEMMs are in lbgb_gemm.cu).  Activations are channel-major,
+// (C, B*H*W): channel c's values for all samples and grid points are
+// contiguous, so a pointwise layer is one GEMM over B*H*W columns.
+#include "lbgb_common.cuh"
+
+namespace lbgb {
+
+constexpr float SQ2PI = 0.7978845608028654f;
+
+__device__ __forceinline__ float gelu_f(float x) {
+    return 0.5f * x * (1.f + tanhf(SQ2PI * (x + 0.044715f * x * x * x)));
+}
+__device__ __forceinline__ float gelu_df(float x) {
+    const float t = tanhf(SQ2PI * (x + 0.044715f * x * x * x));
+    return 0.5f * (1.f + t) + 0.5f * x * (1.f - t * t) * SQ2PI * (1.f + 3.f * 0.044715f * x * x);
+}
+
+__global__ void k_to_bf16(const float *__restrict__ x, __nv_bfloat16 *__restrict__ y, long long n) {
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+        y[i] = __float2bfloat16_rn(x[i]);
+}
+
+// z[c, j] += bias[c] (+ extra[c, j]); act: 0 identity, 1 GELU -> v (fp32 and bf16)
+__global__ void k_bias_act(float *__restrict__ z, const float *__restrict__ bias, const float *__restrict__ extra,
+                           float *__restrict__ v, __nv_bfloat16 *__restrict__ vb, int channels, long long cols,
+                           int act) {
+    const long long n = (long long)channels * cols;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        const int c = (int)(i / cols);
+        float x = z[i] + (bias ? bias[c] : 0.f) + (extra ? extra[i] : 0.f);
+        z[i] = x;
+        const float y = act ? gelu_f(x) : x;
+        if (v) v[i] = y;
+        if (vb) vb[i] = __float2bfloat16_rn(y);
+    }
+}
+
+// dz = dy * gelu'(z), also as bf16
+__global__ void k_gelu_back(const float *__restrict__ dy, const float *__restrict__ z, float *__restrict__ dz,
+                            __nv_bfloat16 *__restrict__ dzb, long long n) {
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        const float g = dy[i] * gelu_df(z[i]);
+        dz[i] = g;
+        if (dzb) dzb[i] = __float2bfloat16_rn(g);
+    }
+}
+
+// db[c] = sum_j dy[c, j]; one block per channel
+__global__ void __launch_bounds__(256) k_row_sum(const float *__restrict__ dy, float *__restrict__ db, long long cols) {
+    const int c = blockIdx.x;
+    float acc = 0.f;
+    for (long long j = threadIdx.x; j < cols; j += blockDim.x) acc += dy[c * cols + j];
+    __shared__ float sm[256];
+    sm[threadIdx.x] = acc;
+    __syncthreads();
+    for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+        if (threadIdx.x < s) sm[threadIdx.x] += sm[threadIdx.x + s];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) db[c] = sm[0];
+}
+
+// Complex mixing per Fourier mode.  x: (C, B, Y, K) re and im; R: (C, O, Y, K);
+// y: (O, B, Y, K).  y[o,b,q] = sum_c x[c,b,q] R[c,o,q] (complex), q = mode.
+__global__ void k_mix_fwd(const float *__restrict__ xr, const float *__restrict__ xi,
+                          const __nv_bfloat16 *__restrict__ Rr, const __nv_bfloat16 *__restrict__ Ri,
+                          float *__restrict__ yr, float *__restrict__ yi, int C, int O, int B, int Q) {
+    const long long n = (long long)O * B * Q;
+    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x) {
+        const int q = (int)(t % Q);
+        const int b = (int)((t / Q) % B);
+        const int o = (int)(t / ((long long)Q * B));
+        float ar = 0.f, ai = 0.f;
+        for (int c = 0; c < C; ++c) {
+            const float xre = xr[((long long)c * B + b) * Q + q], xim = xi[((long long)c * B + b) * Q + q];
+            const float rr = __bfloat162float(Rr[((long long)c * O + o) * Q + q]);
+            const float ri = __bfloat162float(Ri[((long long)c * O + o) * Q + q]);
+            ar += xre * rr - xim * ri;
+            ai += xre * ri + xim * rr;
+        }
+        yr[t] = ar;
+        yi[t] = ai;
+    }
+}
+
+// gradients of the mixing: dx[c,b,q] = sum_o dy[o,b,q] conj-transpose R; dR[c,o,q] = sum_b ...
+__global__ void k_mix_bwd_x(const float *__restrict__ dyr, const float *__restrict__ dyi,
+                            const __nv_bfloat16 *__restrict__ Rr, const __nv_bfloat16 *__restrict__ Ri,
+                            float *__restrict__ dxr, float *__restrict__ dxi, int C, int O, int B, int Q) {
+    const long long n = (long long)C * B * Q;
+    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x) {
+        const int q = (int)(t % Q);
+        const int b = (int)((t / Q) % B);
+        const int c = (int)(t / ((long long)Q * B));
+        float ar = 0.f, ai = 0.f;
+        for (int o = 0; o < O; ++o) {
+            const float gr = dyr[((long long)o * B + b) * Q + q], gi = dyi[((long long)o * B + b) * Q + q];
+            const float rr = __bfloat162float(Rr[((long long)c * O + o) * Q + q]);
+            const float ri = __bfloat162float(Ri[((long long)c * O + o) * Q + q]);
+            ar += gr * rr + gi * ri;
+            ai += -gr * ri + gi * rr;
+        }
+        dxr[t] = ar;
+        dxi[t] = ai;
+    }
+}
+
+__global__ void k_mix_bwd_r(const float *__restrict__ dyr, const float *__restrict__ dyi,
+                            const float *__restrict__ xr, const float *__restrict__ xi, float *__restrict__ dRr,
+                            float *__restrict__ dRi, int C, int O, int B, int Q) {
+    const long long n = (long long)C * O * Q;
+    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x) {
+        const int q = (int)(t % Q);
+        const int o = (int)((t / Q) % O);
+        const int c = (int)(t / ((long long)Q * O));
+        float ar = 0.f, ai = 0.f;
+        for (int b = 0; b < B; ++b) {
+            const float gr = dyr[((long long)o * B + b) * Q + q], gi = dyi[((long long)o * B + b) * Q + q];
+            const float x_r = xr[((long long)c * B + b) * Q + q], x_i = xi[((long long)c * B + b) * Q + q];
+            ar += gr * x_r + gi * x_i;
+            ai += -gr * x_i + gi * x_r;
+        }
+        dRr[t] = ar;
+        dRi[t] = ai;
+    }
+}
+
+// mean squared error: partial sums per block into part[], and d = 2 (y - t) / n
+__global__ void __launch_bounds__(256) k_mse(const float *__restrict__ y, const float *__restrict__ t,
+                                             float *__restrict__ d, double *__restrict__ part, long long n) {
+    double acc = 0.0;
+    const float s = 2.f / (float)n;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        const float e = y[i] - t[i];
+        acc += (double)e * e;
+        d[i] = s * e;
+    }
+    __shared__ double sm[256];
+    sm[threadIdx.x] = acc;
+    __syncthreads();
+    for (int k = blockDim.x / 2; k > 0; k >>= 1) {
+        if (threadIdx.x < k) sm[threadIdx.x] += sm[threadIdx.x + k];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) part[blockIdx.x] = sm[0];
+}
+
+// Adam on FP32 master weights, refreshing their BF16 copies
+__global__ void k_adam(float *__restrict__ w, const float *__restrict__ g, float *__restrict__ m, float *__restrict__ v,
+                       __nv_bfloat16 *__restrict__ wb, long long n, float lr, float b1, float b2, float eps, float c1,
+                       float c2, float wd) {
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        const float gi = g[i] + wd * w[i];
+        const float mi = b1 * m[i] + (1.f - b1) * gi;
+        const float vi = b2 * v[i] + (1.f - b2) * gi * gi;
+        m[i] = mi;
+        v[i] = vi;
+        const float wi = w[i] - lr * (mi / c1) / (sqrtf(vi / c2) + eps);
+        w[i] = wi;
+        if (wb) wb[i] = __float2bfloat16_rn(wi);
+    }
+}
+
+// out[i] = beta * out[i] + sum_s parts[s * n + i]   (split-K partial sums)
+__global__ void k_sum_splits(const float *__restrict__ parts, float *__restrict__ out, int S, long long n, float beta) {
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        float acc = beta == 0.f ? 0.f : beta * out[i];
+        for (int s = 0; s < S; ++s) acc += parts[(long long)s * n + i];
+        out[i] = acc;
+    }
+}
+
+static int blocks_for(long long n) {
+    long long b = (n + 255) / 256;
+    if (b > 8192) b = 8192;
+    return (int)(b < 1 ? 1 : b);
+}
+
+}  // namespace lbgb
+
+using namespace lbgb;
+
+extern "C" int lbgb_fno_to_bf16(const float *x, void *y, long long n, void *stream) {
+    if (n <= 0) return LBGB_OK;
+    k_to_bf16<<<blocks_for(n), 256, 0, (cudaStream_t)stream>>>(x, static_cast<__nv_bfloat16 *>(y), n);
+    return check_launch("k_to_bf16");
+}
+
+extern "C" int lbgb_fno_bias_act(float *z, const float *bias, const float *extra, float *v, void *vb, int channels,
+                                 long long cols, int act, void *stream) {
+    const long long n = (long long)channels * cols;
+    if (n <= 0) return LBGB_OK;
+    k_bias_act<<<blocks_for(n), 256, 0, (cudaStream_t)stream>>>(z, bias, extra, v, static_cast<__nv_bfloat16 *>(vb),
+                                                                channels, cols, act);
+    return check_launch("k_bias_act");
+}
+
+extern "C" int lbgb_fno_gelu_back(const float *dy, const float *z, float *dz, void *dzb, long long n, void *stream) {
+    if (n <= 0) return LBGB_OK;
+    k_gelu_back<<<blocks_for(n), 256, 0, (cudaStream_t)stream>>>(dy, z, dz, static_cast<__nv_bfloat16 *>(dzb), n);
+    return check_launch("k_gelu_back");
+}
+
+extern "C" int lbgb_fno_row_sum(const float *dy, float *db, int channels, long long cols, void *stream) {
+    if (channels <= 0) return LBGB_OK;
+    k_row_sum<<<channels, 256, 0, (cudaStream_t)stream>>>(dy, db, cols);
+    return check_launch("k_row_sum");
+}
+
+extern "C" int lbgb_fno_mix(const float *xr, const float *xi, const void *Rr, const void *Ri, float *yr, float *yi,
+                            int C, int O, int B, int Q, void *stream) {
+    const long long n = (long long)O * B * Q;
+    k_mix_fwd<<<blocks_for(n), 256, 0, (cudaStream_t)stream>>>(xr, xi, static_cast<const __nv_bfloat16 *>(Rr),
+                                                               static_cast<const __nv_bfloat16 *>(Ri), yr, yi, C, O,
+                                                               B, Q);
+    return check_launch("k_mix_fwd");
+}
+
+extern "C" int lbgb_fno_mix_back(const float *dyr, const float *dyi, const float *xr, const float *xi,
+                                 const void *Rr, const void *Ri, float *dxr, float *dxi, float *dRr, float *dRi,
+                                 int C, int O, int B, int Q, void *stream) {
+    cudaStream_t s = (cudaStream_t)stream;
+    k_mix_bwd_x<<<blocks_for((long long)C * B * Q), 256, 0, s>>>(dyr, dyi, static_cast<const __nv_bfloat16 *>(Rr),
+                                                                 static_cast<const __nv_bfloat16 *>(Ri), dxr, dxi, C,
+                                                                 O, B, Q);
+    int rc = check_launch("k_mix_bwd_x");
+    if (rc) return rc;
+    k_mix_bwd_r<<<blocks_for((long long)C * O * Q), 256, 0, s>>>(dyr, dyi, xr, xi, dRr, dRi, C, O, B, Q);
+    return check_launch("k_mix_bwd_r");
+}
+
+extern "C" int lbgb_fno_mse(const float *y, const float *t, float *d, double *partials, int nparts, long long n,
+                            void *stream) {
+    if (nparts <= 0 || nparts > 8192) {
+        set_error("lbgb_fno_mse: 1 <= nparts <= 8192");
+        return LBGB_EINVAL;
+    }
+    k_mse<<<nparts, 256, 0, (cudaStream_t)stream>>>(y, t, d, partials, n);
+    return check_launch("k_mse");
+}
+
+extern "C" int lbgb_fno_adam(float *w, const float *g, float *m, float *v, void *wb, long long n, float lr, float b1,
+                             float b2, float eps, int step, float weight_decay, void *stream) {
+    if (n <= 0) return LBGB_OK;
+    const float c1 = 1.f - powf(b1, (float)step), c2 = 1.f - powf(b2, (float)step);
+    k_adam<<<blocks_for(n), 256, 0, (cudaStream_t)stream>>>(w, g, m, v, static_cast<__nv_bfloat16 *>(wb), n, lr, b1,
+                                                            b2, eps, c1, c2, weight_decay);
+    return check_launch("k_adam");
+}
+
+extern "C" int lbgb_fno_sum_splits(const float *parts, float *out, int S, long long n, float beta, void *stream) {
+    if (n <= 0) return LBGB_OK;
+    k_sum_splits<<<blocks_for(n), 256, 0, (cudaStream_t)stream>>>(parts, out, S, n, beta);
+    return check_launch("k_sum_splits");
+}

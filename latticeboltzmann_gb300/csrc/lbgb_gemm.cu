@@ -1,0 +1,334 @@
+// BF16 GEMM with FP32 accumulation for the Fourier-neural-operator layers:
+//   C = alpha * A * B + beta * C,  A (m x k), B (k x n) in BF16, C FP32,
+// every operand addressed by (row stride, column stride) and a batch stride,
+// so row-major, column-major and transposed views all go through one call.
+//
+// Tensor-core path (k_gemm_tc): one CTA of 128 threads computes a 128 x NT
+// tile of C with tcgen05.mma (kind::f16, BF16 inputs, FP32 accumulator held
+// in tensor memory).  Per 64-wide K block the threads copy A (128 x 64) and B
+// (NT x 64) into shared memory in the canonical K-major layout without
+// swizzle -- 8x8 "core matrices" of 16-byte rows, neighbours along K 128 B
+// apart (leading byte offset), neighbours along M/N 1024 B apart (stride byte
+// offset) -- one elected thread issues four K=16 MMAs and commits them to an
+// mbarrier, and all threads wait (bounded) before reusing the buffers.  The
+// epilogue reads the accumulator rows back with tcgen05.ld (warp w owns TMEM
+// lanes 32w..32w+31) and applies alpha/beta.
+//
+// SIMT path (k_gemm_simt): the same contract with FP32 FMAs; the reference the
+// tensor-core path is tested against.
+#include <stdio.h>
+
+#include "lbgb_common.cuh"
+
+namespace lbgb {
+
+__device__ int g_gemm_status;
+
+__device__ __forceinline__ uint32_t smem_u32(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+// shared-memory matrix descriptor (tcgen05): start address, leading and stride
+// byte offsets (16-byte units), descriptor version bit 46, no swizzle
+__device__ __forceinline__ uint64_t umma_desc(uint32_t saddr, uint32_t lbo, uint32_t sbo) {
+    uint64_t d = 0;
+    d |= (uint64_t)((saddr & 0x3ffffu) >> 4);
+    d |= (uint64_t)((lbo >> 4) & 0x3fffu) << 16;
+    d |= (uint64_t)((sbo >> 4) & 0x3fffu) << 32;
+    d |= (uint64_t)1 << 46;
+    return d;
+}
+
+// instruction descriptor for kind::f16: FP32 accumulator, BF16 A and B, both
+// K-major, N and M encoded as N/8 and M/16
+__host__ __device__ constexpr uint32_t umma_idesc_bf16(int m, int n) {
+    return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(n >> 3) << 17) | ((uint32_t)(m >> 4) << 24);
+}
+
+__device__ __forceinline__ void mbar_init_g(uint64_t *bar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait_g(uint64_t *bar, uint32_t parity) {
+    uint32_t done;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(done)
+        : "r"(smem_u32(bar)), "r"(parity)
+        : "memory");
+    return done != 0;
+}
+__device__ __forceinline__ bool mbar_wait_g(uint64_t *bar, uint32_t parity, long long limit) {
+    for (long long i = 0; i < limit; ++i)
+        if (mbar_try_wait_g(bar, parity)) return true;
+    return false;
+}
+
+constexpr int TC_M = 128;
+constexpr int TC_K = 64;
+constexpr long long TC_WAIT = 1ll << 22;
+
+template <int NT>
+__global__ void __launch_bounds__(128, 1)
+k_gemm_tc(int M, int N, int K, const __nv_bfloat16 *__restrict__ A, long long a_rs, long long a_cs, long long a_bs,
+          const __nv_bfloat16 *__restrict__ B, long long b_rs, long long b_cs, long long b_bs, float *__restrict__ C,
+          long long c_rs, long long c_cs, long long c_bs, float alpha, float beta) {
+    static_assert(NT % 16 == 0 && NT >= 32 && NT <= 256, "tile N");
+    __shared__ __align__(1024) unsigned char sA[TC_M * TC_K * 2];
+    // at least 8 KB: any reading of the descriptor's byte offsets stays inside
+    __shared__ __align__(1024) unsigned char sB[(NT < 64 ? 64 : NT) * TC_K * 2];
+    __shared__ __align__(8) uint64_t bar;
+    __shared__ uint32_t tmem_slot;
+
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int m0 = blockIdx.x * TC_M, n0 = blockIdx.y * NT;
+    const long long z = blockIdx.z;
+    A += z * a_bs;
+    B += z * b_bs;
+    C += z * c_bs;
+
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&tmem_slot)),
+                     "r"((uint32_t)NT)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    if (tid == 0) {
+        mbar_init_g(&bar, 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    const uint32_t tmem = tmem_slot;
+    constexpr uint32_t idesc = umma_idesc_bf16(TC_M, NT);
+
+    uint32_t phase = 0;
+    bool ok = true;
+    const int kblocks = (K + TC_K - 1) / TC_K;
+    for (int kb = 0; kb < kblocks && ok; ++kb) {
+        const int k0 = kb * TC_K;
+        // A tile: 128 rows x 64 k; element (r, kk) at (r/8)*1024 + (kk/8)*128 + (r%8)*16 + (kk%8)*2
+        for (int e = tid; e < TC_M * TC_K / 8; e += 128) {
+            const int r = e >> 3, kc = e & 7;
+            const int gm = m0 + r, gk = k0 + kc * 8;
+            uint32_t w[4] = {0u, 0u, 0u, 0u};
+            if (gm < M) {
+                unsigned short h[8];
+#pragma unroll
+                for (int q = 0; q < 8; ++q) {
+                    const int kk = gk + q;
+                    h[q] = kk < K ? __bfloat16_as_ushort(A[(long long)gm * a_rs + (long long)kk * a_cs]) : 0;
+                }
+                memcpy(w, h, 16);
+            }
+            *reinterpret_cast<uint4 *>(sA + (r >> 3) * 1024 + kc * 128 + (r & 7) * 16) = make_uint4(w[0], w[1], w[2],
+                                                                                                  w[3]);
+        }
+        // B tile: NT rows (n) x 64 k, same layout
+        for (int e = tid; e < NT * TC_K / 8; e += 128) {
+            const int r = e >> 3, kc = e & 7;
+            const int gn = n0 + r, gk = k0 + kc * 8;
+            uint32_t w[4] = {0u, 0u, 0u, 0u};
+            if (gn < N) {
+                unsigned short h[8];
+#pragma unroll
+                for (int q = 0; q < 8; ++q) {
+                    const int kk = gk + q;
+                    h[q] = kk < K ? __bfloat16_as_ushort(B[(long long)kk * b_rs + (long long)gn * b_cs]) : 0;
+                }
+                memcpy(w, h, 16);
+            }
+            *reinterpret_cast<uint4 *>(sB + (r >> 3) * 1024 + kc * 128 + (r & 7) * 16) = make_uint4(w[0], w[1], w[2],
+                                                                                                  w[3]);
+        }
+        // make the generic-proxy writes visible to the tensor core
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        __syncthreads();
+        if (tid == 0) {
+            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+#pragma unroll
+            for (int kk = 0; kk < TC_K / 16; ++kk) {
+                // K = 16 per MMA: two core matrices along K, 256 bytes
+                const uint64_t da = umma_desc(smem_u32(sA) + kk * 256, 128, 1024);
+                const uint64_t db = umma_desc(smem_u32(sB) + kk * 256, 128, 1024);
+                const uint32_t acc = (kb > 0 || kk > 0) ? 1u : 0u;
+                asm volatile(
+                    "{\n\t.reg .pred p;\n\t"
+                    "setp.ne.u32 p, %4, 0;\n\t"
+                    "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(tmem),
+                    "l"(da), "l"(db), "r"(idesc), "r"(acc)
+                    : "memory");
+            }
+            asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                             smem_u32(&bar))
+                         : "memory");
+        }
+        if (!mbar_wait_g(&bar, phase, TC_WAIT)) {
+            atomicCAS(&g_gemm_status, 0, 1);
+            ok = false;
+            // the MMAs may still be running: wait again (bounded) before the
+            // buffers and the tensor memory go away
+            mbar_wait_g(&bar, phase, TC_WAIT);
+        }
+        phase ^= 1u;
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        // every thread leaves the loop together if any wait gave up
+        ok = __syncthreads_and(ok) != 0;
+    }
+
+    if (ok) {
+        // epilogue: warp w reads TMEM lanes 32w..32w+31 = rows m0+32w+lane
+        const int row = m0 + warp * 32 + lane;
+#pragma unroll 1
+        for (int c0 = 0; c0 < NT; c0 += 16) {
+            uint32_t v[16];
+            const uint32_t taddr = tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0;
+            asm volatile(
+                "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, "
+                "%14, %15}, [%16];"
+                : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7]),
+                  "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]),
+                  "=r"(v[15])
+                : "r"(taddr));
+            asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+            if (row < M) {
+#pragma unroll
+                for (int j = 0; j < 16; ++j) {
+                    const int col = n0 + c0 + j;
+                    if (col < N) {
+                        float *cp = C + (long long)row * c_rs + (long long)col * c_cs;
+                        const float acc = __uint_as_float(v[j]);
+                        *cp = beta == 0.f ? alpha * acc : alpha * acc + beta * *cp;
+                    }
+                }
+            }
+        }
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    if (warp == 0)
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"((uint32_t)NT)
+                     : "memory");
+}
+
+// SIMT reference: 16x16 threads, 64x64 tile, FP32 accumulation
+__global__ void __launch_bounds__(256)
+k_gemm_simt(int M, int N, int K, const __nv_bfloat16 *__restrict__ A, long long a_rs, long long a_cs, long long a_bs,
+            const __nv_bfloat16 *__restrict__ B, long long b_rs, long long b_cs, long long b_bs, float *__restrict__ C,
+            long long c_rs, long long c_cs, long long c_bs, float alpha, float beta) {
+    __shared__ float As[16][65];
+    __shared__ float Bs[16][65];
+    const long long z = blockIdx.z;
+    A += z * a_bs;
+    B += z * b_bs;
+    C += z * c_bs;
+    const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
+    const int m0 = blockIdx.x * 64, n0 = blockIdx.y * 64;
+    float acc[4][4] = {};
+    for (int k0 = 0; k0 < K; k0 += 16) {
+        for (int e = threadIdx.x; e < 16 * 64; e += 256) {
+            const int kk = e >> 6, i = e & 63;
+            const int gm = m0 + i, gn = n0 + i, gk = k0 + kk;
+            As[kk][i] = (gm < M && gk < K) ? __bfloat162float(A[(long long)gm * a_rs + (long long)gk * a_cs]) : 0.f;
+            Bs[kk][i] = (gn < N && gk < K) ? __bfloat162float(B[(long long)gk * b_rs + (long long)gn * b_cs]) : 0.f;
+        }
+        __syncthreads();
+#pragma unroll
+        for (int kk = 0; kk < 16; ++kk)
+#pragma unroll
+            for (int a = 0; a < 4; ++a)
+#pragma unroll
+                for (int b = 0; b < 4; ++b) acc[a][b] += As[kk][ty * 4 + a] * Bs[kk][tx * 4 + b];
+        __syncthreads();
+    }
+#pragma unroll
+    for (int a = 0; a < 4; ++a)
+#pragma unroll
+        for (int b = 0; b < 4; ++b) {
+            const int gm = m0 + ty * 4 + a, gn = n0 + tx * 4 + b;
+            if (gm < M && gn < N) {
+                float *cp = C + (long long)gm * c_rs + (long long)gn * c_cs;
+                *cp = beta == 0.f ? alpha * acc[a][b] : alpha * acc[a][b] + beta * *cp;
+            }
+        }
+}
+
+}  // namespace lbgb
+
+using namespace lbgb;
+
+extern "C" int lbgb_gemm_bf16(int m, int n, int k, const void *A, long long a_rs, long long a_cs, long long a_bs,
+                              const void *B, long long b_rs, long long b_cs, long long b_bs, float *C, long long c_rs,
+                              long long c_cs, long long c_bs, int batch, float alpha, float beta, int engine,
+                              void *stream) {
+    if (m < 0 || n < 0 || k < 0 || batch < 1 || batch > 65535) {
+        set_error("lbgb_gemm_bf16: bad sizes m=%d n=%d k=%d batch=%d", m, n, k, batch);
+        return LBGB_EINVAL;
+    }
+    if (m == 0 || n == 0) return LBGB_OK;
+    if (!A || !B || !C) {
+        set_error("lbgb_gemm_bf16: null operand");
+        return LBGB_EINVAL;
+    }
+    cudaStream_t s = (cudaStream_t)stream;
+    const auto *a = static_cast<const __nv_bfloat16 *>(A);
+    const auto *b = static_cast<const __nv_bfloat16 *>(B);
+    if (engine == 1) {
+        dim3 grid((m + 63) / 64, (n + 63) / 64, batch);
+        k_gemm_simt<<<grid, 256, 0, s>>>(m, n, k, a, a_rs, a_cs, a_bs, b, b_rs, b_cs, b_bs, C, c_rs, c_cs, c_bs, alpha,
+                                         beta);
+        return check_launch("k_gemm_simt");
+    }
+    if (engine != 0 && engine != 2) {
+        set_error("lbgb_gemm_bf16: unknown engine %d", engine);
+        return LBGB_EINVAL;
+    }
+    // tensor cores: tile N 32/64/128 by problem width.  The extra dynamic
+    // shared memory (unused) caps residency at 3 CTAs per SM, so their tensor
+    // memory (<= 3 x 128 of 512 columns) never makes an allocation wait.
+    const size_t pad = 40 * 1024;
+    static bool attr_set[3] = {false, false, false};
+    if (!attr_set[0]) {
+        cudaFuncSetAttribute(k_gemm_tc<32>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)pad);
+        cudaFuncSetAttribute(k_gemm_tc<64>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)pad);
+        cudaFuncSetAttribute(k_gemm_tc<128>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)pad);
+        attr_set[0] = attr_set[1] = attr_set[2] = true;
+    }
+    if (n <= 32) {
+        dim3 grid((m + TC_M - 1) / TC_M, (n + 31) / 32, batch);
+        k_gemm_tc<32><<<grid, 128, pad, s>>>(m, n, k, a, a_rs, a_cs, a_bs, b, b_rs, b_cs, b_bs, C, c_rs, c_cs, c_bs,
+                                           alpha, beta);
+    } else if (n <= 64) {
+        dim3 grid((m + TC_M - 1) / TC_M, (n + 63) / 64, batch);
+        k_gemm_tc<64><<<grid, 128, pad, s>>>(m, n, k, a, a_rs, a_cs, a_bs, b, b_rs, b_cs, b_bs, C, c_rs, c_cs, c_bs,
+                                           alpha, beta);
+    } else {
+        dim3 grid((m + TC_M - 1) / TC_M, (n + 127) / 128, batch);
+        k_gemm_tc<128><<<grid, 128, pad, s>>>(m, n, k, a, a_rs, a_cs, a_bs, b, b_rs, b_cs, b_bs, C, c_rs, c_cs, c_bs,
+                                            alpha, beta);
+    }
+    return check_launch("k_gemm_tc");
+}
+
+extern "C" int lbgb_gemm_status(int reset) {
+    cudaError_t e = cudaDeviceSynchronize();
+    if (e != cudaSuccess) {
+        set_error("lbgb_gemm_status: %s", cudaGetErrorString(e));
+        return LBGB_ECUDA;
+    }
+    int v = 0;
+    e = cudaMemcpyFromSymbol(&v, g_gemm_status, sizeof(int));
+    if (e == cudaSuccess && reset) {
+        const int zero = 0;
+        e = cudaMemcpyToSymbol(g_gemm_status, &zero, sizeof(int));
+    }
+    if (e != cudaSuccess) {
+        set_error("lbgb_gemm_status: %s", cudaGetErrorString(e));
+        return LBGB_ECUDA;
+    }
+    if (v) {
+        set_error("a bounded wait in the tensor-core GEMM gave up");
+        return LBGB_ETIMEOUT;
+    }
+    return LBGB_OK;
+}

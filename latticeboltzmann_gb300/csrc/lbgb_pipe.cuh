@@ -181,8 +181,8 @@ k_step_pipe(const typename Codec<DT>::raw *__restrict__ src, typename Codec<DT>:
         const int c = l0 + t * NC;  // first cell of this thread
         const bool act = c < ny;
         const raw *stage = slots + (size_t)s * 9 * SLOT;
-        const bool wl = (BC == LBGB_CAVITY) && k == 0;
-        const bool wr = (BC == LBGB_CAVITY) && k == nx - 1;
+        const bool wl = (BC != LBGB_PERIODIC) && k == 0;
+        const bool wr = (BC != LBGB_PERIODIC) && k == nx - 1;
         real v[9][NC];
         if (act) {
 #pragma unroll
@@ -217,7 +217,7 @@ k_step_pipe(const typename Codec<DT>::raw *__restrict__ src, typename Codec<DT>:
         mbar_arrive(&empty[s]);  // this thread is done with the stage
         if (!act) continue;
 
-        if (BC == LBGB_CAVITY) {
+        if (BC != LBGB_PERIODIC) {
             auto g = [&](int ch, int row, int l) { return C::dec(ld1(src + (size_t)ch * cs + (size_t)row * ny + l), ch); };
             if (c == 0) {
                 v[CN][0] = g(CS, k, 0);
@@ -226,15 +226,22 @@ k_step_pipe(const typename Codec<DT>::raw *__restrict__ src, typename Codec<DT>:
             }
             if (c + NC == ny) {
                 const int T = ny - 1;
-                const int kw = (k == 0) ? nx - 1 : k - 1;
-                const int ke = (k == nx - 1) ? 0 : k + 1;
-                const real gN = g(CN, k, T), gNW = g(CNW, k, T), gNE = g(CNE, k, T);
-                const real rho_lid = gNW + gN + gNE + g(CNW, ke, T - 1) + g(CN, k, T - 1) + g(CNE, kw, T - 1) +
-                                     g(CW, ke, T) + g(C0, k, T) + g(CE, kw, T);
-                const real lid = (real(6) * real(1.0 / 36.0)) * rho_lid * u0;
-                v[CS][NC - 1] = gN;
-                v[CSE][NC - 1] = (k == 0) ? gNW : gNW + lid;
-                v[CSW][NC - 1] = (k == nx - 1) ? gNE : gNE - lid;
+                if (BC == LBGB_CAVITY_LADD) {
+                    const real lid = real(6) * real(1.0 / 36.0) * u0;
+                    v[CS][NC - 1] = g(CN, k, T);
+                    v[CSE][NC - 1] = g(CNW, k, T) + lid;
+                    v[CSW][NC - 1] = g(CNE, k, T) - lid;
+                } else {
+                    const int kw = (k == 0) ? nx - 1 : k - 1;
+                    const int ke = (k == nx - 1) ? 0 : k + 1;
+                    const real gN = g(CN, k, T), gNW = g(CNW, k, T), gNE = g(CNE, k, T);
+                    const real rho_lid = gNW + gN + gNE + g(CNW, ke, T - 1) + g(CN, k, T - 1) + g(CNE, kw, T - 1) +
+                                         g(CW, ke, T) + g(C0, k, T) + g(CE, kw, T);
+                    const real lid = (real(6) * real(1.0 / 36.0)) * rho_lid * u0;
+                    v[CS][NC - 1] = gN;
+                    v[CSE][NC - 1] = (k == 0) ? gNW : gNW + lid;
+                    v[CSW][NC - 1] = (k == nx - 1) ? gNE : gNE - lid;
+                }
             }
         }
 

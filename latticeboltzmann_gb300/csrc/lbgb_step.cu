@@ -141,7 +141,7 @@ __device__ __forceinline__ void step_segment(const typename Codec<DT>::raw *__re
     pull_channel<C, V, BC, CSW>(v[CSW], src, cs, ny, k, kp, wr, l0, lane, act);
     pull_channel<C, V, BC, CSE>(v[CSE], src, cs, ny, k, km, wl, l0, lane, act);
 
-    if (BC == LBGB_CAVITY && act) {
+    if (BC != LBGB_PERIODIC && act) {
         if (l0 == 0) {
             // bottom wall: N, NE, NW bounce back from the same node
             v[CN][0] = load_one<C>(src, cs, ny, CS, k, 0);
@@ -149,23 +149,31 @@ __device__ __forceinline__ void step_segment(const typename Codec<DT>::raw *__re
             v[CNW][0] = load_one<C>(src, cs, ny, CSE, k, 0);
         }
         if (l0 + V == ny) {
-            // lid: S bounces back; SE/SW get the Ladd term 6 w rho_lid u0,
-            // except at the corner where the side wall wins (plain bounce-back)
-            const int T = ny - 1;
-            const int kw = (k == 0) ? nx - 1 : k - 1;  // periodic neighbours, as
-            const int ke = (k == nx - 1) ? 0 : k + 1;  // the reference's roll reads them
-            const real gN = load_one<C>(src, cs, ny, CN, k, T);
-            const real gNW = load_one<C>(src, cs, ny, CNW, k, T);
-            const real gNE = load_one<C>(src, cs, ny, CNE, k, T);
-            const real rho_lid = gNW + gN + gNE + load_one<C>(src, cs, ny, CNW, ke, T - 1) +
-                                 load_one<C>(src, cs, ny, CN, k, T - 1) +
-                                 load_one<C>(src, cs, ny, CNE, kw, T - 1) +
-                                 load_one<C>(src, cs, ny, CW, ke, T) + load_one<C>(src, cs, ny, C0, k, T) +
-                                 load_one<C>(src, cs, ny, CE, kw, T);
-            const real lid = (real(6) * real(1.0 / 36.0)) * rho_lid * u0;
-            v[CS][V - 1] = gN;
-            v[CSE][V - 1] = (k == 0) ? gNW : gNW + lid;
-            v[CSW][V - 1] = (k == nx - 1) ? gNE : gNE - lid;
+            if (BC == LBGB_CAVITY_LADD) {
+                // standard Ladd wall, density 1: -/+ 6 w u0 at every lid node
+                const real lid = real(6) * real(1.0 / 36.0) * u0;
+                v[CS][V - 1] = load_one<C>(src, cs, ny, CN, k, ny - 1);
+                v[CSE][V - 1] = load_one<C>(src, cs, ny, CNW, k, ny - 1) + lid;
+                v[CSW][V - 1] = load_one<C>(src, cs, ny, CNE, k, ny - 1) - lid;
+            } else {
+                // lid: S bounces back; SE/SW get the Ladd term 6 w rho_lid u0,
+                // except at the corner where the side wall wins (plain bounce-back)
+                const int T = ny - 1;
+                const int kw = (k == 0) ? nx - 1 : k - 1;  // periodic neighbours, as
+                const int ke = (k == nx - 1) ? 0 : k + 1;  // the reference's roll reads them
+                const real gN = load_one<C>(src, cs, ny, CN, k, T);
+                const real gNW = load_one<C>(src, cs, ny, CNW, k, T);
+                const real gNE = load_one<C>(src, cs, ny, CNE, k, T);
+                const real rho_lid = gNW + gN + gNE + load_one<C>(src, cs, ny, CNW, ke, T - 1) +
+                                     load_one<C>(src, cs, ny, CN, k, T - 1) +
+                                     load_one<C>(src, cs, ny, CNE, kw, T - 1) +
+                                     load_one<C>(src, cs, ny, CW, ke, T) + load_one<C>(src, cs, ny, C0, k, T) +
+                                     load_one<C>(src, cs, ny, CE, kw, T);
+                const real lid = (real(6) * real(1.0 / 36.0)) * rho_lid * u0;
+                v[CS][V - 1] = gN;
+                v[CSE][V - 1] = (k == 0) ? gNW : gNW + lid;
+                v[CSW][V - 1] = (k == nx - 1) ? gNE : gNE - lid;
+            }
         }
     }
 
@@ -352,11 +360,11 @@ static int check_grid(const void *src, void *dst, int nx, int ny, int dtype, int
         set_error("%s: grid %d x %d must be positive", what, nx, ny);
         return LBGB_EINVAL;
     }
-    if (boundary == LBGB_CAVITY && (nx < 2 || ny < 2)) {
+    if (boundary != LBGB_PERIODIC && (nx < 2 || ny < 2)) {
         set_error("%s: the cavity needs nx >= 2 and ny >= 2 (got %d x %d)", what, nx, ny);
         return LBGB_EINVAL;
     }
-    if (boundary != LBGB_CAVITY && boundary != LBGB_PERIODIC) {
+    if (boundary != LBGB_CAVITY && boundary != LBGB_PERIODIC && boundary != LBGB_CAVITY_LADD) {
         set_error("%s: unknown boundary code %d", what, boundary);
         return LBGB_EINVAL;
     }
@@ -400,6 +408,8 @@ extern "C" int lbgb_step_fused(const void *src, void *dst, int nx, int ny, int b
     if (rc) return rc;
     if (boundary == LBGB_CAVITY)
         return dispatch<LBGB_CAVITY, true>(src, dst, nx, ny, dtype, omega, u0, (cudaStream_t)stream);
+    if (boundary == LBGB_CAVITY_LADD)
+        return dispatch<LBGB_CAVITY_LADD, true>(src, dst, nx, ny, dtype, omega, u0, (cudaStream_t)stream);
     return dispatch<LBGB_PERIODIC, true>(src, dst, nx, ny, dtype, omega, 0.0, (cudaStream_t)stream);
 }
 
@@ -450,9 +460,9 @@ extern "C" int lbgb_run_fused_sr(void *a, void *b, int nx, int ny, int boundary,
     sr.seed = seed;
     void *src = a, *dst = b;
     for (int i = 0; i < nsteps; ++i) {
-        rc = boundary == LBGB_CAVITY
-                 ? dispatch<LBGB_CAVITY, true>(src, dst, nx, ny, dtype, omega, u0, s, sr)
-                 : dispatch<LBGB_PERIODIC, true>(src, dst, nx, ny, dtype, omega, 0.0, s, sr);
+        rc = boundary == LBGB_CAVITY        ? dispatch<LBGB_CAVITY, true>(src, dst, nx, ny, dtype, omega, u0, s, sr)
+             : boundary == LBGB_CAVITY_LADD ? dispatch<LBGB_CAVITY_LADD, true>(src, dst, nx, ny, dtype, omega, u0, s, sr)
+                                            : dispatch<LBGB_PERIODIC, true>(src, dst, nx, ny, dtype, omega, 0.0, s, sr);
         if (rc) return rc;
         k_bump_step<<<1, 1, 0, s>>>(step_counter);
         rc = check_launch("k_bump_step");

@@ -45,8 +45,12 @@ class Lattice:
         Grid size (``ny`` is the fast axis; the cavity lid is at ``l = ny-1``).
     omega : float
         BGK relaxation parameter.
-    boundary : {"cavity", "periodic"}
-        ``cavity``: bounce-back on four walls, lid moving with ``u0`` in +x.
+    boundary : {"cavity", "cavity-ladd", "periodic"}
+        ``cavity``: bounce-back on four walls, lid moving with ``u0`` in +x,
+        with the reference's lid term 6 w rho_lid u0 (cavity_opt1.py:225-239).
+        ``cavity-ladd``: the same walls, lid term 6 w u0 (wall density 1) at
+        every lid node; unlike the reference's lid it conserves mass and has a
+        steady state.
     u0 : float
         Lid velocity (cavity only).
     storage : {"f32", "f64", "f16dev", "bf16dev"}
@@ -64,14 +68,14 @@ class Lattice:
         if storage not in _RAW:
             raise ValueError("storage must be one of %s" % sorted(_RAW))
         if boundary not in _lib.BOUNDARY_CODES:
-            raise ValueError("boundary must be 'cavity' or 'periodic'")
+            raise ValueError("boundary must be one of %s" % sorted(_lib.BOUNDARY_CODES))
         if nx <= 0 or ny <= 0:
             raise ValueError("grid must be positive, got %d x %d" % (nx, ny))
-        if boundary == "cavity" and (nx < 2 or ny < 2):
+        if boundary != "periodic" and (nx < 2 or ny < 2):
             raise ValueError("the cavity needs nx >= 2 and ny >= 2")
         self.nx, self.ny = int(nx), int(ny)
         self.omega = float(omega)
-        self.u0 = float(u0) if boundary == "cavity" else 0.0
+        self.u0 = float(u0) if boundary != "periodic" else 0.0
         self.boundary = boundary
         self.storage = storage
         self.code = _lib.STORAGE_CODES[storage]

@@ -196,6 +196,33 @@ def stream_and_bounce_back(f, u0=0.1):
     f[SW, r, :] = g[NE, r, :]
 
 
+def stream_and_bounce_back_ladd(f, u0=0.1):
+    """Standard Ladd moving wall with wall density 1 (boundary code 2).
+
+    Not in the reference; the kernels offer it for steady-state work because
+    the reference's lid term 6 w rho_lid u0 uses a rho_lid that reads across
+    the periodic seam and skips the corners, which makes the cavity gain mass
+    and leaves it without a steady state.  Here every lid node, both corners
+    included, gets f_S = g_N, f_SE = g_NW + 6 w u0 and f_SW = g_NE - 6 w u0
+    (w = 1/36); the rest is stream_and_bounce_back with a resting lid.
+    """
+    _, nx, ny = f.shape
+    if nx < 2 or ny < 2:
+        raise ValueError("stream_and_bounce_back needs nx >= 2 and ny >= 2")
+    t = ny - 1
+    g_nw, g_ne = f[NW, :, t].copy(), f[NE, :, t].copy()
+    stream_and_bounce_back(f, 0.0)
+    lid = 6 * W_I.astype(f.dtype)[SE] * u0
+    f[SE, :, t] = g_nw + lid
+    f[SW, :, t] = g_ne - lid
+
+
+def cavity_ladd_step(f, omega, u0=0.1):
+    """One cavity step with the wall-density-1 lid (stream_and_bounce_back_ladd)."""
+    stream_and_bounce_back_ladd(f, u0)
+    return collide(f, omega)
+
+
 def cavity_step(f, omega, u0=0.1):
     """One cavity time step in the reference's order (cavity_opt1.py:341-343)."""
     stream_and_bounce_back(f, u0)

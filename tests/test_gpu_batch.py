@@ -33,27 +33,44 @@ def test_batch_matches_oracle_per_instance(cuda):
     del bl
 
 
-def test_batch_cavity_and_storages_against_single_lattice(cuda):
+@pytest.mark.parametrize("boundary", ["cavity", "cavity-ladd"])
+def test_batch_cavity_and_storages_against_single_lattice(cuda, boundary):
     """A batch of cavities equals the same cavities run one by one (same kernel code)."""
     import latticeboltzmann_gb300 as PyLB
     sizes = [(24, 16), (33, 40), (8, 64)]
     for storage in ("f32", "f16dev", "bf16dev"):
-        bl = B.BatchedLattice(sizes, [1.3, 1.6, 0.8], boundary="cavity", u0=0.1, storage=storage, device=cuda)
+        bl = B.BatchedLattice(sizes, [1.3, 1.6, 0.8], boundary=boundary, u0=0.1, storage=storage, device=cuda)
         bl.equilibrium(lambda b: (1.0, 0.0, 0.0))
-        flat = B.BatchedLattice(sizes, [1.3, 1.6, 0.8], boundary="cavity", u0=0.1, storage=storage, device=cuda)
+        flat = B.BatchedLattice(sizes, [1.3, 1.6, 0.8], boundary=boundary, u0=0.1, storage=storage, device=cuda)
         flat.equilibrium(lambda b: (1.0, 0.0, 0.0))
         bl.step(12, {"flat": False, "vector": True, "rows": 2, "threads": 256, "blocks": 40})
         flat.step(12, {"flat": True, "vector": False, "rows": 2, "threads": 128, "blocks": 40})
         _lib.set_tuning(_lib.TUNE_KERNEL, _lib.KERNELS["register"])
         try:
             for b, (nx, ny) in enumerate(sizes):
-                lat = PyLB.Lattice(nx, ny, [1.3, 1.6, 0.8][b], boundary="cavity", u0=0.1, storage=storage,
+                lat = PyLB.Lattice(nx, ny, [1.3, 1.6, 0.8][b], boundary=boundary, u0=0.1, storage=storage,
                                    device=cuda)
                 lat.step(12)
                 assert torch.equal(lat.populations(torch.float64), bl.populations(b)), (storage, b)
                 assert torch.equal(lat.populations(torch.float64), flat.populations(b)), (storage, b)
         finally:
             _lib.set_tuning(_lib.TUNE_KERNEL, _lib.KERNELS["auto"])
+
+
+def test_batch_ladd_cavity_f64_matches_oracle(cuda):
+    """FP64 batch of wall-density-1 cavities against the oracle, both task shapes."""
+    sizes = [(24, 16), (5, 9), (40, 33), (2, 2)]
+    om = [1.3, 1.7, 0.9, 1.1]
+    u0 = [0.1, 0.05, 0.08, 0.02]
+    for flat in (False, True):
+        bl = B.BatchedLattice(sizes, om, boundary="cavity-ladd", u0=u0, storage="f64", device=cuda)
+        bl.equilibrium(lambda b: (1.0, 0.0, 0.0))
+        bl.step(20, {"flat": flat, "vector": False, "rows": 1, "threads": 128, "blocks": 16})
+        for b, (nx, ny) in enumerate(sizes):
+            f = oracle.equilibrium(np.ones((nx, ny)), np.zeros((nx, ny)), np.zeros((nx, ny)))
+            for _ in range(20):
+                oracle.cavity_ladd_step(f, om[b], u0[b])
+            assert np.abs(bl.populations(b).cpu().numpy() - f).max() < 1e-13, (b, flat)
 
 
 def test_batch_graph_replay_and_autotune(cuda):
@@ -109,3 +126,24 @@ def test_shear_amplitude_and_viscosity(cuda):
         if np.isfinite(ref):
             assert abs(nu_fit[b] / ref - 1) < 1e-3, (b, nu_fit[b], ref)
         assert np.abs(res["amplitudes"][:, b] - np.array(amps)).max() < 2e-6
+
+
+def test_steady_cavities_batch(cuda):
+    """Small cavities run to steady state in one batch: each converged
+    instance matches a single-lattice run of the same number of steps, and
+    its velocity change over the last interval is below the tolerance."""
+    import latticeboltzmann_gb300 as PyLB
+    re = np.array([10.0, 40.0, 100.0])
+    u = np.array([0.05, 0.08, 0.1])
+    n = 32
+    fields, steps, wall = B.steady_cavities(re, u, n=n, tol=1e-6, every=200, max_steps=40000, device=cuda,
+                                            tune=False)
+    assert (steps > 0).all(), steps
+    for b in range(3):
+        lat = PyLB.Lattice(n, n, B.omega_for(re[b], u[b], n), boundary="cavity-ladd", u0=u[b], device=cuda)
+        lat.step(int(steps[b]))
+        rho, ux, uy = lat.macroscopic()
+        assert torch.allclose(ux, fields[b, 1], atol=1e-6) and torch.allclose(uy, fields[b, 2], atol=1e-6)
+        lat.step(200)
+        _, ux2, uy2 = lat.macroscopic()
+        assert float(torch.maximum((ux2 - ux).abs(), (uy2 - uy).abs()).max()) < 1e-6

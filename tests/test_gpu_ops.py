@@ -170,7 +170,7 @@ def test_cavity_run_golden_operator_path(cuda, golden, dt):
         assert np.abs(out - ref).max() < 2e-5
 
 
-@pytest.mark.parametrize("boundary", ["cavity", "periodic"])
+@pytest.mark.parametrize("boundary", ["cavity", "cavity-ladd", "periodic"])
 @pytest.mark.parametrize("nx,ny", [(24, 16), (33, 17), (5, 7), (64, 128), (130, 96), (2, 2)])
 def test_fused_equals_operator_sequence_f64(cuda, boundary, nx, ny):
     rng = np.random.default_rng(nx + 100 * ny)
@@ -179,6 +179,8 @@ def test_fused_equals_operator_sequence_f64(cuda, boundary, nx, ny):
     for _ in range(5):
         if boundary == "cavity":
             oracle.cavity_step(ref, 1.3, 0.1)
+        elif boundary == "cavity-ladd":
+            oracle.cavity_ladd_step(ref, 1.3, 0.1)
         else:
             oracle.periodic_step(ref, 1.3)
     lat = PyLB.Lattice(nx, ny, 1.3, boundary=boundary, u0=0.1, storage="f64", device=cuda)

@@ -47,7 +47,7 @@ def run_with(kernel, storage, boundary, f0, steps, cuda):
 
 
 @pytest.mark.parametrize("storage", ["f32", "f64", "f16dev", "bf16dev"])
-@pytest.mark.parametrize("boundary", ["cavity", "periodic"])
+@pytest.mark.parametrize("boundary", ["cavity", "cavity-ladd", "periodic"])
 @pytest.mark.parametrize("nx,ny", SIZES)
 def test_pipelined_equals_register_kernel(tuning, cuda, storage, boundary, nx, ny):
     f0 = random_state(nx, ny, nx * 7 + ny)
@@ -60,6 +60,8 @@ def test_pipelined_equals_register_kernel(tuning, cuda, storage, boundary, nx, n
         for _ in range(3):
             if boundary == "cavity":
                 oracle.cavity_step(ref, 1.45, 0.08)
+            elif boundary == "cavity-ladd":
+                oracle.cavity_ladd_step(ref, 1.45, 0.08)
             else:
                 oracle.periodic_step(ref, 1.45)
         assert np.abs(b.populations().cpu().numpy() - ref).max() < 1e-13
