@@ -204,16 +204,33 @@ LBGB_API int lbgb_batch_velocity_change(const void *f, long long total_elems,
                                         float *u_prev, long long total_cells, float *out_dev,
                                         void *stream);
 
+/* Start populations for a known flow: equilibrium plus the first-order
+ * Chapman-Enskog non-equilibrium part,
+ *   f_i = f_i^eq(rho, u) - (3 w_i rho / omega) (c_ia c_ib - delta_ab / 3) d_a u_b,
+ * with central-difference velocity gradients (for the cavity boundaries a
+ * one-sided quadratic through the wall velocity: 0, or u0 at the lid).
+ * post_collision != 0 writes f^eq + (1 - omega) f^neq instead: the state a
+ * time step (stream, then collide) leaves, which is what the solvers hold
+ * between steps.
+ * rho/ux/uy are (nx, ny) fields, f a (9, nx, ny) array, all of type dtype
+ * (LBGB_F32 or LBGB_F64).  Used to warm-start the cavity from a predicted
+ * flow field; no counterpart in the reference (which starts from rest,
+ * simulators/parallel_lid_drive_cavity/cavity_opt1.py:333-335). */
+LBGB_API int lbgb_chapman_enskog(const void *rho, const void *ux, const void *uy, void *f, int nx, int ny,
+                                 double omega, double u0, int boundary, int post_collision, int dtype,
+                                 void *stream);
+
 /* BF16 GEMM with FP32 accumulation: C = alpha * A * B + beta * C for `batch`
- * independent problems.  A (m x k) and B (k x n) are BF16, C FP32; element
+ * independent problems.  A (m x k) and B (k x n) are BF16; C is FP32, or BF16
+ * when c_bf16 != 0 (rounded once, after the FP32 accumulation).  Element
  * (i, j) of X is X[i * x_rs + j * x_cs] and problem z starts at z * x_bs, so
  * any transposed or strided view works.  engine: 0/2 tensor cores
  * (tcgen05.mma, accumulator in tensor memory), 1 CUDA-core reference.  Used
  * by the Fourier-neural-operator surrogate; no counterpart in the reference. */
 LBGB_API int lbgb_gemm_bf16(int m, int n, int k, const void *A, long long a_rs, long long a_cs,
                             long long a_bs, const void *B, long long b_rs, long long b_cs,
-                            long long b_bs, float *C, long long c_rs, long long c_cs, long long c_bs,
-                            int batch, float alpha, float beta, int engine, void *stream);
+                            long long b_bs, void *C, long long c_rs, long long c_cs, long long c_bs,
+                            int batch, float alpha, float beta, int c_bf16, int engine, void *stream);
 
 /* Synchronizes and reports whether a bounded wait in the tensor-core GEMM gave
  * up since the last reset (LBGB_ETIMEOUT).  No counterpart in the reference. */
@@ -226,8 +243,10 @@ LBGB_API int lbgb_gemm_status(int reset);
  *   bias_act     z += bias[c] (+ extra); v = act(z) (0 identity, 1 GELU), fp32 and/or bf16
  *   gelu_back    dz = dy * GELU'(z) (and its bf16 copy)
  *   row_sum      db[c] = sum_j dy[c, j]
- *   mix          y[o,b,q] = sum_c x[c,b,q] R[c,o,q] (complex, BF16 weights)
- *   mix_back     its gradients with respect to x and R
+ *   mix          per Fourier mode y = sum_c x R (complex, BF16 weights), reading the
+ *                transform products P (C, B, 2mk, 2q) and writing the BF16 operand
+ *                Ym (O, B, 2q, 2mk) of the inverse transform (q kept ky, mk kept kx)
+ *   mix_back     its gradients: dP (BF16) from dYm, and dR (FP32) summed over B
  *   mse          partial sums of (y - t)^2 and d = 2 (y - t) / n
  *   adam         Adam step on FP32 weights, refreshing their BF16 copy
  *   sum_splits   out = beta out + sum of S split-K partial results */
@@ -237,11 +256,10 @@ LBGB_API int lbgb_fno_bias_act(float *z, const float *bias, const float *extra, 
 LBGB_API int lbgb_fno_gelu_back(const float *dy, const float *z, float *dz, void *dzb, long long n,
                                 void *stream);
 LBGB_API int lbgb_fno_row_sum(const float *dy, float *db, int channels, long long cols, void *stream);
-LBGB_API int lbgb_fno_mix(const float *xr, const float *xi, const void *Rr, const void *Ri, float *yr,
-                          float *yi, int C, int O, int B, int Q, void *stream);
-LBGB_API int lbgb_fno_mix_back(const float *dyr, const float *dyi, const float *xr, const float *xi,
-                               const void *Rr, const void *Ri, float *dxr, float *dxi, float *dRr,
-                               float *dRi, int C, int O, int B, int Q, void *stream);
+LBGB_API int lbgb_fno_mix(const float *P, const void *Rr, const void *Ri, void *Ym, int C, int O, int B,
+                          int q, int mk, void *stream);
+LBGB_API int lbgb_fno_mix_back(const float *dYm, const float *P, const void *Rr, const void *Ri, void *dP,
+                               float *dRr, float *dRi, int C, int O, int B, int q, int mk, void *stream);
 LBGB_API int lbgb_fno_mse(const float *y, const float *t, float *d, double *partials, int nparts,
                           long long n, void *stream);
 LBGB_API int lbgb_fno_adam(float *w, const float *g, float *m, float *v, void *wb, long long n, float lr,

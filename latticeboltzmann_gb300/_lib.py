@@ -58,16 +58,17 @@ SIGNATURES = {
     "lbgb_batch_step": (_I, [_P, _P, ctypes.c_longlong, _P, _I, _P, ctypes.c_longlong, _I, _I, _I, _I, _I, _I, _P]),
     "lbgb_batch_shear_amplitude": (_I, [_P, ctypes.c_longlong, _P, _I, _I, _P, _P]),
     "lbgb_batch_velocity_change": (_I, [_P, ctypes.c_longlong, _P, _I, _I, _P, ctypes.c_longlong, _P, _P]),
+    "lbgb_chapman_enskog": (_I, [_P, _P, _P, _P, _I, _I, ctypes.c_double, ctypes.c_double, _I, _I, _I, _P]),
     "lbgb_gemm_bf16": (_I, [_I, _I, _I, _P, ctypes.c_longlong, ctypes.c_longlong, ctypes.c_longlong, _P,
                             ctypes.c_longlong, ctypes.c_longlong, ctypes.c_longlong, _P, ctypes.c_longlong,
-                            ctypes.c_longlong, ctypes.c_longlong, _I, ctypes.c_float, ctypes.c_float, _I, _P]),
+                            ctypes.c_longlong, ctypes.c_longlong, _I, ctypes.c_float, ctypes.c_float, _I, _I, _P]),
     "lbgb_gemm_status": (_I, [_I]),
     "lbgb_fno_to_bf16": (_I, [_P, _P, ctypes.c_longlong, _P]),
     "lbgb_fno_bias_act": (_I, [_P, _P, _P, _P, _P, _I, ctypes.c_longlong, _I, _P]),
     "lbgb_fno_gelu_back": (_I, [_P, _P, _P, _P, ctypes.c_longlong, _P]),
     "lbgb_fno_row_sum": (_I, [_P, _P, _I, ctypes.c_longlong, _P]),
-    "lbgb_fno_mix": (_I, [_P, _P, _P, _P, _P, _P, _I, _I, _I, _I, _P]),
-    "lbgb_fno_mix_back": (_I, [_P, _P, _P, _P, _P, _P, _P, _P, _P, _P, _I, _I, _I, _I, _P]),
+    "lbgb_fno_mix": (_I, [_P, _P, _P, _P, _I, _I, _I, _I, _I, _P]),
+    "lbgb_fno_mix_back": (_I, [_P, _P, _P, _P, _P, _P, _P, _I, _I, _I, _I, _I, _P]),
     "lbgb_fno_mse": (_I, [_P, _P, _P, _P, _I, ctypes.c_longlong, _P]),
     "lbgb_fno_adam": (_I, [_P, _P, _P, _P, _P, ctypes.c_longlong, ctypes.c_float, ctypes.c_float, ctypes.c_float,
                            ctypes.c_float, _I, ctypes.c_float, _P]),

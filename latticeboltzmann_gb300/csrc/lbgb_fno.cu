@@ -61,65 +61,101 @@ __global__ void __launch_bounds__(256) k_row_sum(const float *__restrict__ dy, f
     if (threadIdx.x == 0) db[c] = sm[0];
 }
 
-// Complex mixing per Fourier mode.  x: (C, B, Y, K) re and im; R: (C, O, Y, K);
-// y: (O, B, Y, K).  y[o,b,q] = sum_c x[c,b,q] R[c,o,q] (complex), q = mode.
-__global__ void k_mix_fwd(const float *__restrict__ xr, const float *__restrict__ xi,
-                          const __nv_bfloat16 *__restrict__ Rr, const __nv_bfloat16 *__restrict__ Ri,
-                          float *__restrict__ yr, float *__restrict__ yi, int C, int O, int B, int Q) {
+// Complex mixing per Fourier mode, on the layouts of the factorised DFT GEMMs
+// (q kept ky values, mk kept kx values):
+//   P  (C, B, 2mk, 2q) FP32: P[j][n], j < mk: Re of the W-transform at kx = j,
+//      j >= mk: its Im at kx = j - mk; n < q: times cos(ky_n), n >= q: sin(ky_{n-q})
+//   so x = xr + i xi with xr = P[kx][y] + P[mk+kx][q+y], xi = P[mk+kx][y] - P[kx][q+y];
+//   R  (C, O, q, mk) BF16 (real, imaginary parts);
+//   Ym (O, B, 2q, 2mk) BF16, the right operand of the inverse transform along H:
+//      rows y: [yr | yi], rows q+y: [-yi | yr], with y = sum_c x R (complex).
+__device__ __forceinline__ void mode_x(const float *__restrict__ Pcb, int y, int kx, int q, int mk, float &xr,
+                                       float &xi) {
+    const int q2 = 2 * q;
+    xr = Pcb[kx * q2 + y] + Pcb[(mk + kx) * q2 + q + y];
+    xi = Pcb[(mk + kx) * q2 + y] - Pcb[kx * q2 + q + y];
+}
+__device__ __forceinline__ void mode_dy(const float *__restrict__ D, int y, int kx, int q, int mk, float &dyr,
+                                        float &dyi) {
+    const int m2 = 2 * mk;
+    dyr = D[y * m2 + kx] + D[(q + y) * m2 + mk + kx];
+    dyi = D[y * m2 + mk + kx] - D[(q + y) * m2 + kx];
+}
+
+__global__ void k_mix_fwd(const float *__restrict__ P, const __nv_bfloat16 *__restrict__ Rr,
+                          const __nv_bfloat16 *__restrict__ Ri, __nv_bfloat16 *__restrict__ Ym, int C, int O, int B,
+                          int q, int mk) {
+    const int Q = q * mk;
     const long long n = (long long)O * B * Q;
+    const long long pcb = 4LL * mk * q;  // P elements per (c, b)
     for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x) {
-        const int q = (int)(t % Q);
+        const int mode = (int)(t % Q), y = mode / mk, kx = mode % mk;
         const int b = (int)((t / Q) % B);
         const int o = (int)(t / ((long long)Q * B));
         float ar = 0.f, ai = 0.f;
         for (int c = 0; c < C; ++c) {
-            const float xre = xr[((long long)c * B + b) * Q + q], xim = xi[((long long)c * B + b) * Q + q];
-            const float rr = __bfloat162float(Rr[((long long)c * O + o) * Q + q]);
-            const float ri = __bfloat162float(Ri[((long long)c * O + o) * Q + q]);
-            ar += xre * rr - xim * ri;
-            ai += xre * ri + xim * rr;
+            float xr, xi;
+            mode_x(P + ((long long)c * B + b) * pcb, y, kx, q, mk, xr, xi);
+            const long long r = ((long long)c * O + o) * Q + mode;
+            const float rr = __bfloat162float(Rr[r]), ri = __bfloat162float(Ri[r]);
+            ar += xr * rr - xi * ri;
+            ai += xr * ri + xi * rr;
         }
-        yr[t] = ar;
-        yi[t] = ai;
+        __nv_bfloat16 *Y = Ym + ((long long)o * B + b) * pcb;
+        const int m2 = 2 * mk;
+        Y[y * m2 + kx] = __float2bfloat16_rn(ar);
+        Y[y * m2 + mk + kx] = __float2bfloat16_rn(ai);
+        Y[(q + y) * m2 + kx] = __float2bfloat16_rn(-ai);
+        Y[(q + y) * m2 + mk + kx] = __float2bfloat16_rn(ar);
     }
 }
 
-// gradients of the mixing: dx[c,b,q] = sum_o dy[o,b,q] conj-transpose R; dR[c,o,q] = sum_b ...
-__global__ void k_mix_bwd_x(const float *__restrict__ dyr, const float *__restrict__ dyi,
-                            const __nv_bfloat16 *__restrict__ Rr, const __nv_bfloat16 *__restrict__ Ri,
-                            float *__restrict__ dxr, float *__restrict__ dxi, int C, int O, int B, int Q) {
+// Gradient with respect to the inputs: dYm (O, B, 2q, 2mk) FP32 -> dP (C, B, 2mk, 2q) BF16
+__global__ void k_mix_bwd_x(const float *__restrict__ dYm, const __nv_bfloat16 *__restrict__ Rr,
+                            const __nv_bfloat16 *__restrict__ Ri, __nv_bfloat16 *__restrict__ dP, int C, int O, int B,
+                            int q, int mk) {
+    const int Q = q * mk;
     const long long n = (long long)C * B * Q;
+    const long long pcb = 4LL * mk * q;
     for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x) {
-        const int q = (int)(t % Q);
+        const int mode = (int)(t % Q), y = mode / mk, kx = mode % mk;
         const int b = (int)((t / Q) % B);
         const int c = (int)(t / ((long long)Q * B));
         float ar = 0.f, ai = 0.f;
         for (int o = 0; o < O; ++o) {
-            const float gr = dyr[((long long)o * B + b) * Q + q], gi = dyi[((long long)o * B + b) * Q + q];
-            const float rr = __bfloat162float(Rr[((long long)c * O + o) * Q + q]);
-            const float ri = __bfloat162float(Ri[((long long)c * O + o) * Q + q]);
+            float gr, gi;
+            mode_dy(dYm + ((long long)o * B + b) * pcb, y, kx, q, mk, gr, gi);
+            const long long r = ((long long)c * O + o) * Q + mode;
+            const float rr = __bfloat162float(Rr[r]), ri = __bfloat162float(Ri[r]);
             ar += gr * rr + gi * ri;
             ai += -gr * ri + gi * rr;
         }
-        dxr[t] = ar;
-        dxi[t] = ai;
+        __nv_bfloat16 *D = dP + ((long long)c * B + b) * pcb;
+        const int q2 = 2 * q;
+        D[kx * q2 + y] = __float2bfloat16_rn(ar);
+        D[(mk + kx) * q2 + q + y] = __float2bfloat16_rn(ar);
+        D[(mk + kx) * q2 + y] = __float2bfloat16_rn(ai);
+        D[kx * q2 + q + y] = __float2bfloat16_rn(-ai);
     }
 }
 
-__global__ void k_mix_bwd_r(const float *__restrict__ dyr, const float *__restrict__ dyi,
-                            const float *__restrict__ xr, const float *__restrict__ xi, float *__restrict__ dRr,
-                            float *__restrict__ dRi, int C, int O, int B, int Q) {
+// Gradient with respect to the weights: dR (C, O, q, mk) FP32, summed over the batch
+__global__ void k_mix_bwd_r(const float *__restrict__ dYm, const float *__restrict__ P, float *__restrict__ dRr,
+                            float *__restrict__ dRi, int C, int O, int B, int q, int mk) {
+    const int Q = q * mk;
     const long long n = (long long)C * O * Q;
+    const long long pcb = 4LL * mk * q;
     for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x) {
-        const int q = (int)(t % Q);
+        const int mode = (int)(t % Q), y = mode / mk, kx = mode % mk;
         const int o = (int)((t / Q) % O);
         const int c = (int)(t / ((long long)Q * O));
         float ar = 0.f, ai = 0.f;
         for (int b = 0; b < B; ++b) {
-            const float gr = dyr[((long long)o * B + b) * Q + q], gi = dyi[((long long)o * B + b) * Q + q];
-            const float x_r = xr[((long long)c * B + b) * Q + q], x_i = xi[((long long)c * B + b) * Q + q];
-            ar += gr * x_r + gi * x_i;
-            ai += -gr * x_i + gi * x_r;
+            float gr, gi, xr, xi;
+            mode_dy(dYm + ((long long)o * B + b) * pcb, y, kx, q, mk, gr, gi);
+            mode_x(P + ((long long)c * B + b) * pcb, y, kx, q, mk, xr, xi);
+            ar += gr * xr + gi * xi;
+            ai += -gr * xi + gi * xr;
         }
         dRr[t] = ar;
         dRi[t] = ai;
@@ -208,25 +244,26 @@ extern "C" int lbgb_fno_row_sum(const float *dy, float *db, int channels, long l
     return check_launch("k_row_sum");
 }
 
-extern "C" int lbgb_fno_mix(const float *xr, const float *xi, const void *Rr, const void *Ri, float *yr, float *yi,
-                            int C, int O, int B, int Q, void *stream) {
-    const long long n = (long long)O * B * Q;
-    k_mix_fwd<<<blocks_for(n), 256, 0, (cudaStream_t)stream>>>(xr, xi, static_cast<const __nv_bfloat16 *>(Rr),
-                                                               static_cast<const __nv_bfloat16 *>(Ri), yr, yi, C, O,
-                                                               B, Q);
+extern "C" int lbgb_fno_mix(const float *P, const void *Rr, const void *Ri, void *Ym, int C, int O, int B, int q,
+                            int mk, void *stream) {
+    const long long n = (long long)O * B * q * mk;
+    if (n <= 0 || C <= 0) return LBGB_OK;
+    k_mix_fwd<<<blocks_for(n), 256, 0, (cudaStream_t)stream>>>(P, static_cast<const __nv_bfloat16 *>(Rr),
+                                                               static_cast<const __nv_bfloat16 *>(Ri),
+                                                               static_cast<__nv_bfloat16 *>(Ym), C, O, B, q, mk);
     return check_launch("k_mix_fwd");
 }
 
-extern "C" int lbgb_fno_mix_back(const float *dyr, const float *dyi, const float *xr, const float *xi,
-                                 const void *Rr, const void *Ri, float *dxr, float *dxi, float *dRr, float *dRi,
-                                 int C, int O, int B, int Q, void *stream) {
+extern "C" int lbgb_fno_mix_back(const float *dYm, const float *P, const void *Rr, const void *Ri, void *dP,
+                                 float *dRr, float *dRi, int C, int O, int B, int q, int mk, void *stream) {
+    if (C <= 0 || O <= 0 || B <= 0 || q <= 0 || mk <= 0) return LBGB_OK;
     cudaStream_t s = (cudaStream_t)stream;
-    k_mix_bwd_x<<<blocks_for((long long)C * B * Q), 256, 0, s>>>(dyr, dyi, static_cast<const __nv_bfloat16 *>(Rr),
-                                                                 static_cast<const __nv_bfloat16 *>(Ri), dxr, dxi, C,
-                                                                 O, B, Q);
+    k_mix_bwd_x<<<blocks_for((long long)C * B * q * mk), 256, 0, s>>>(
+        dYm, static_cast<const __nv_bfloat16 *>(Rr), static_cast<const __nv_bfloat16 *>(Ri),
+        static_cast<__nv_bfloat16 *>(dP), C, O, B, q, mk);
     int rc = check_launch("k_mix_bwd_x");
     if (rc) return rc;
-    k_mix_bwd_r<<<blocks_for((long long)C * O * Q), 256, 0, s>>>(dyr, dyi, xr, xi, dRr, dRi, C, O, B, Q);
+    k_mix_bwd_r<<<blocks_for((long long)C * O * q * mk), 256, 0, s>>>(dYm, P, dRr, dRi, C, O, B, q, mk);
     return check_launch("k_mix_bwd_r");
 }
 

@@ -63,14 +63,55 @@ __device__ __forceinline__ bool mbar_wait_g(uint64_t *bar, uint32_t parity, long
     return false;
 }
 
+__device__ __forceinline__ void store_out(float *p, float x) { *p = x; }
+__device__ __forceinline__ void store_out(__nv_bfloat16 *p, float x) { *p = __float2bfloat16_rn(x); }
+__device__ __forceinline__ float load_out(const float *p) { return *p; }
+__device__ __forceinline__ float load_out(const __nv_bfloat16 *p) { return __bfloat162float(*p); }
+
 constexpr int TC_M = 128;
 constexpr int TC_K = 64;
 constexpr long long TC_WAIT = 1ll << 22;
 
-template <int NT>
+// Copies rows [r0, r0+ROWS) x k [k0, k0+64) of X (element (r, k) at
+// X[r * rs + k * ks], zero outside R x K) into the core-matrix K-major layout.
+// Thread-to-element mapping follows the contiguous axis so that a warp's
+// loads coalesce: 16-byte vector loads along K when K is contiguous and
+// aligned, consecutive rows per warp when the rows are contiguous.
+template <int ROWS>
+__device__ __forceinline__ void load_tile(unsigned char *dst, const __nv_bfloat16 *__restrict__ X, long long rs,
+                                          long long ks, int r0, int R, int k0, int K, int tid) {
+    const bool row_contig = rs == 1 && ks != 1;
+    const bool vec = ks == 1 && (rs & 7) == 0 && ((reinterpret_cast<uintptr_t>(X) & 15) == 0);
+    for (int e = tid; e < ROWS * TC_K / 8; e += 128) {
+        int r, kc;
+        if (row_contig) {
+            r = e % ROWS;
+            kc = e / ROWS;
+        } else {
+            r = e >> 3;
+            kc = e & 7;
+        }
+        const int gr = r0 + r, gk = k0 + kc * 8;
+        uint4 w = make_uint4(0u, 0u, 0u, 0u);
+        if (gr < R) {
+            const __nv_bfloat16 *p = X + (long long)gr * rs + (long long)gk * ks;
+            if (vec && gk + 8 <= K) {
+                w = __ldg(reinterpret_cast<const uint4 *>(p));
+            } else {
+                unsigned short h[8];
+#pragma unroll
+                for (int q = 0; q < 8; ++q) h[q] = gk + q < K ? __bfloat16_as_ushort(p[(long long)q * ks]) : 0;
+                memcpy(&w, h, 16);
+            }
+        }
+        *reinterpret_cast<uint4 *>(dst + (r >> 3) * 1024 + kc * 128 + (r & 7) * 16) = w;
+    }
+}
+
+template <int NT, typename OUT>
 __global__ void __launch_bounds__(128, 1)
 k_gemm_tc(int M, int N, int K, const __nv_bfloat16 *__restrict__ A, long long a_rs, long long a_cs, long long a_bs,
-          const __nv_bfloat16 *__restrict__ B, long long b_rs, long long b_cs, long long b_bs, float *__restrict__ C,
+          const __nv_bfloat16 *__restrict__ B, long long b_rs, long long b_cs, long long b_bs, OUT *__restrict__ C,
           long long c_rs, long long c_cs, long long c_bs, float alpha, float beta) {
     static_assert(NT % 16 == 0 && NT >= 32 && NT <= 256, "tile N");
     __shared__ __align__(1024) unsigned char sA[TC_M * TC_K * 2];
@@ -108,39 +149,9 @@ k_gemm_tc(int M, int N, int K, const __nv_bfloat16 *__restrict__ A, long long a_
     for (int kb = 0; kb < kblocks && ok; ++kb) {
         const int k0 = kb * TC_K;
         // A tile: 128 rows x 64 k; element (r, kk) at (r/8)*1024 + (kk/8)*128 + (r%8)*16 + (kk%8)*2
-        for (int e = tid; e < TC_M * TC_K / 8; e += 128) {
-            const int r = e >> 3, kc = e & 7;
-            const int gm = m0 + r, gk = k0 + kc * 8;
-            uint32_t w[4] = {0u, 0u, 0u, 0u};
-            if (gm < M) {
-                unsigned short h[8];
-#pragma unroll
-                for (int q = 0; q < 8; ++q) {
-                    const int kk = gk + q;
-                    h[q] = kk < K ? __bfloat16_as_ushort(A[(long long)gm * a_rs + (long long)kk * a_cs]) : 0;
-                }
-                memcpy(w, h, 16);
-            }
-            *reinterpret_cast<uint4 *>(sA + (r >> 3) * 1024 + kc * 128 + (r & 7) * 16) = make_uint4(w[0], w[1], w[2],
-                                                                                                  w[3]);
-        }
-        // B tile: NT rows (n) x 64 k, same layout
-        for (int e = tid; e < NT * TC_K / 8; e += 128) {
-            const int r = e >> 3, kc = e & 7;
-            const int gn = n0 + r, gk = k0 + kc * 8;
-            uint32_t w[4] = {0u, 0u, 0u, 0u};
-            if (gn < N) {
-                unsigned short h[8];
-#pragma unroll
-                for (int q = 0; q < 8; ++q) {
-                    const int kk = gk + q;
-                    h[q] = kk < K ? __bfloat16_as_ushort(B[(long long)kk * b_rs + (long long)gn * b_cs]) : 0;
-                }
-                memcpy(w, h, 16);
-            }
-            *reinterpret_cast<uint4 *>(sB + (r >> 3) * 1024 + kc * 128 + (r & 7) * 16) = make_uint4(w[0], w[1], w[2],
-                                                                                                  w[3]);
-        }
+        load_tile<TC_M>(sA, A, a_rs, a_cs, m0, M, k0, K, tid);
+        // B tile: NT rows (n) x 64 k, same layout; B(k, n) = B[k * b_rs + n * b_cs]
+        load_tile<NT>(sB, B, b_cs, b_rs, n0, N, k0, K, tid);
         // make the generic-proxy writes visible to the tensor core
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
         __syncthreads();
@@ -196,9 +207,9 @@ k_gemm_tc(int M, int N, int K, const __nv_bfloat16 *__restrict__ A, long long a_
                 for (int j = 0; j < 16; ++j) {
                     const int col = n0 + c0 + j;
                     if (col < N) {
-                        float *cp = C + (long long)row * c_rs + (long long)col * c_cs;
+                        OUT *cp = C + (long long)row * c_rs + (long long)col * c_cs;
                         const float acc = __uint_as_float(v[j]);
-                        *cp = beta == 0.f ? alpha * acc : alpha * acc + beta * *cp;
+                        store_out(cp, beta == 0.f ? alpha * acc : alpha * acc + beta * load_out(cp));
                     }
                 }
             }
@@ -212,9 +223,10 @@ k_gemm_tc(int M, int N, int K, const __nv_bfloat16 *__restrict__ A, long long a_
 }
 
 // SIMT reference: 16x16 threads, 64x64 tile, FP32 accumulation
+template <typename OUT>
 __global__ void __launch_bounds__(256)
 k_gemm_simt(int M, int N, int K, const __nv_bfloat16 *__restrict__ A, long long a_rs, long long a_cs, long long a_bs,
-            const __nv_bfloat16 *__restrict__ B, long long b_rs, long long b_cs, long long b_bs, float *__restrict__ C,
+            const __nv_bfloat16 *__restrict__ B, long long b_rs, long long b_cs, long long b_bs, OUT *__restrict__ C,
             long long c_rs, long long c_cs, long long c_bs, float alpha, float beta) {
     __shared__ float As[16][65];
     __shared__ float Bs[16][65];
@@ -247,10 +259,48 @@ k_gemm_simt(int M, int N, int K, const __nv_bfloat16 *__restrict__ A, long long 
         for (int b = 0; b < 4; ++b) {
             const int gm = m0 + ty * 4 + a, gn = n0 + tx * 4 + b;
             if (gm < M && gn < N) {
-                float *cp = C + (long long)gm * c_rs + (long long)gn * c_cs;
-                *cp = beta == 0.f ? alpha * acc[a][b] : alpha * acc[a][b] + beta * *cp;
+                OUT *cp = C + (long long)gm * c_rs + (long long)gn * c_cs;
+                store_out(cp, beta == 0.f ? alpha * acc[a][b] : alpha * acc[a][b] + beta * load_out(cp));
             }
         }
+}
+
+template <typename OUT>
+static int launch_gemm(int m, int n, int k, const __nv_bfloat16 *a, long long a_rs, long long a_cs, long long a_bs,
+                       const __nv_bfloat16 *b, long long b_rs, long long b_cs, long long b_bs, OUT *C, long long c_rs,
+                       long long c_cs, long long c_bs, int batch, float alpha, float beta, int engine,
+                       cudaStream_t s) {
+    if (engine == 1) {
+        dim3 grid((m + 63) / 64, (n + 63) / 64, batch);
+        k_gemm_simt<OUT><<<grid, 256, 0, s>>>(m, n, k, a, a_rs, a_cs, a_bs, b, b_rs, b_cs, b_bs, C, c_rs, c_cs, c_bs,
+                                              alpha, beta);
+        return check_launch("k_gemm_simt");
+    }
+    // tensor cores: tile N 32/64/128 by problem width.  The extra dynamic
+    // shared memory (unused) caps residency at 3 CTAs per SM, so their tensor
+    // memory (<= 3 x 128 of 512 columns) never makes an allocation wait.
+    const int pad = 40 * 1024;
+    static bool attr_set = false;  // one flag per output type (one instantiation each)
+    if (!attr_set) {
+        cudaFuncSetAttribute(k_gemm_tc<32, OUT>, cudaFuncAttributeMaxDynamicSharedMemorySize, pad);
+        cudaFuncSetAttribute(k_gemm_tc<64, OUT>, cudaFuncAttributeMaxDynamicSharedMemorySize, pad);
+        cudaFuncSetAttribute(k_gemm_tc<128, OUT>, cudaFuncAttributeMaxDynamicSharedMemorySize, pad);
+        attr_set = true;
+    }
+    if (n <= 32) {
+        dim3 grid((m + TC_M - 1) / TC_M, (n + 31) / 32, batch);
+        k_gemm_tc<32, OUT><<<grid, 128, pad, s>>>(m, n, k, a, a_rs, a_cs, a_bs, b, b_rs, b_cs, b_bs, C, c_rs, c_cs,
+                                                  c_bs, alpha, beta);
+    } else if (n <= 64) {
+        dim3 grid((m + TC_M - 1) / TC_M, (n + 63) / 64, batch);
+        k_gemm_tc<64, OUT><<<grid, 128, pad, s>>>(m, n, k, a, a_rs, a_cs, a_bs, b, b_rs, b_cs, b_bs, C, c_rs, c_cs,
+                                                  c_bs, alpha, beta);
+    } else {
+        dim3 grid((m + TC_M - 1) / TC_M, (n + 127) / 128, batch);
+        k_gemm_tc<128, OUT><<<grid, 128, pad, s>>>(m, n, k, a, a_rs, a_cs, a_bs, b, b_rs, b_cs, b_bs, C, c_rs, c_cs,
+                                                   c_bs, alpha, beta);
+    }
+    return check_launch("k_gemm_tc");
 }
 
 }  // namespace lbgb
@@ -258,9 +308,9 @@ k_gemm_simt(int M, int N, int K, const __nv_bfloat16 *__restrict__ A, long long 
 using namespace lbgb;
 
 extern "C" int lbgb_gemm_bf16(int m, int n, int k, const void *A, long long a_rs, long long a_cs, long long a_bs,
-                              const void *B, long long b_rs, long long b_cs, long long b_bs, float *C, long long c_rs,
-                              long long c_cs, long long c_bs, int batch, float alpha, float beta, int engine,
-                              void *stream) {
+                              const void *B, long long b_rs, long long b_cs, long long b_bs, void *C, long long c_rs,
+                              long long c_cs, long long c_bs, int batch, float alpha, float beta, int c_bf16,
+                              int engine, void *stream) {
     if (m < 0 || n < 0 || k < 0 || batch < 1 || batch > 65535) {
         set_error("lbgb_gemm_bf16: bad sizes m=%d n=%d k=%d batch=%d", m, n, k, batch);
         return LBGB_EINVAL;
@@ -270,44 +320,18 @@ extern "C" int lbgb_gemm_bf16(int m, int n, int k, const void *A, long long a_rs
         set_error("lbgb_gemm_bf16: null operand");
         return LBGB_EINVAL;
     }
-    cudaStream_t s = (cudaStream_t)stream;
-    const auto *a = static_cast<const __nv_bfloat16 *>(A);
-    const auto *b = static_cast<const __nv_bfloat16 *>(B);
-    if (engine == 1) {
-        dim3 grid((m + 63) / 64, (n + 63) / 64, batch);
-        k_gemm_simt<<<grid, 256, 0, s>>>(m, n, k, a, a_rs, a_cs, a_bs, b, b_rs, b_cs, b_bs, C, c_rs, c_cs, c_bs, alpha,
-                                         beta);
-        return check_launch("k_gemm_simt");
-    }
-    if (engine != 0 && engine != 2) {
+    if (engine != 0 && engine != 1 && engine != 2) {
         set_error("lbgb_gemm_bf16: unknown engine %d", engine);
         return LBGB_EINVAL;
     }
-    // tensor cores: tile N 32/64/128 by problem width.  The extra dynamic
-    // shared memory (unused) caps residency at 3 CTAs per SM, so their tensor
-    // memory (<= 3 x 128 of 512 columns) never makes an allocation wait.
-    const size_t pad = 40 * 1024;
-    static bool attr_set[3] = {false, false, false};
-    if (!attr_set[0]) {
-        cudaFuncSetAttribute(k_gemm_tc<32>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)pad);
-        cudaFuncSetAttribute(k_gemm_tc<64>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)pad);
-        cudaFuncSetAttribute(k_gemm_tc<128>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)pad);
-        attr_set[0] = attr_set[1] = attr_set[2] = true;
-    }
-    if (n <= 32) {
-        dim3 grid((m + TC_M - 1) / TC_M, (n + 31) / 32, batch);
-        k_gemm_tc<32><<<grid, 128, pad, s>>>(m, n, k, a, a_rs, a_cs, a_bs, b, b_rs, b_cs, b_bs, C, c_rs, c_cs, c_bs,
-                                           alpha, beta);
-    } else if (n <= 64) {
-        dim3 grid((m + TC_M - 1) / TC_M, (n + 63) / 64, batch);
-        k_gemm_tc<64><<<grid, 128, pad, s>>>(m, n, k, a, a_rs, a_cs, a_bs, b, b_rs, b_cs, b_bs, C, c_rs, c_cs, c_bs,
-                                           alpha, beta);
-    } else {
-        dim3 grid((m + TC_M - 1) / TC_M, (n + 127) / 128, batch);
-        k_gemm_tc<128><<<grid, 128, pad, s>>>(m, n, k, a, a_rs, a_cs, a_bs, b, b_rs, b_cs, b_bs, C, c_rs, c_cs, c_bs,
-                                            alpha, beta);
-    }
-    return check_launch("k_gemm_tc");
+    cudaStream_t s = (cudaStream_t)stream;
+    const auto *a = static_cast<const __nv_bfloat16 *>(A);
+    const auto *b = static_cast<const __nv_bfloat16 *>(B);
+    if (c_bf16)
+        return launch_gemm(m, n, k, a, a_rs, a_cs, a_bs, b, b_rs, b_cs, b_bs, static_cast<__nv_bfloat16 *>(C), c_rs,
+                           c_cs, c_bs, batch, alpha, beta, engine, s);
+    return launch_gemm(m, n, k, a, a_rs, a_cs, a_bs, b, b_rs, b_cs, b_bs, static_cast<float *>(C), c_rs, c_cs, c_bs,
+                       batch, alpha, beta, engine, s);
 }
 
 extern "C" int lbgb_gemm_status(int reset) {

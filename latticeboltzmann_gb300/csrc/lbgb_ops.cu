@@ -47,6 +47,51 @@ __global__ void k_equilibrium(const T *__restrict__ rho, const T *__restrict__ u
     }
 }
 
+// ------------------------------------------------------- Chapman-Enskog start
+// f_i = f_i^eq(rho, u) - (3 w_i rho / omega) Q_iab d_a u_b,  Q_iab = c_ia c_ib - delta_ab / 3
+// (first-order non-equilibrium part of the Chapman-Enskog expansion, c_s^2 = 1/3),
+// or the post-collision state f^eq + (1 - omega) f^neq that a time step leaves.
+// Velocity gradients: central differences; for the cavity the boundary nodes
+// take the quadratic through the wall value (half a cell out: 0, or the lid
+// velocity) and the next two nodes:  du/dx(0) = -4/3 u_wall + u(0) + u(1)/3.
+template <class T>
+__device__ __forceinline__ T grad1(const T *__restrict__ u, int64_t at, int64_t stride, int i, int n, bool periodic,
+                                   T wall_lo, T wall_hi) {
+    if (periodic || n < 2) {
+        if (n < 2) return T(0);
+        const int64_t lo = i == 0 ? at + (int64_t)(n - 1) * stride : at - stride;
+        const int64_t hi = i == n - 1 ? at - (int64_t)(n - 1) * stride : at + stride;
+        return T(0.5) * (u[hi] - u[lo]);
+    }
+    if (i == 0) return -T(4.0 / 3.0) * wall_lo + u[at] + u[at + stride] * T(1.0 / 3.0);
+    if (i == n - 1) return T(4.0 / 3.0) * wall_hi - u[at] - u[at - stride] * T(1.0 / 3.0);
+    return T(0.5) * (u[at + stride] - u[at - stride]);
+}
+
+template <class T>
+__global__ void k_chapman_enskog(const T *__restrict__ rho, const T *__restrict__ ux, const T *__restrict__ uy,
+                                 T *__restrict__ f, int nx, int ny, T omega, T u0, int boundary, T neq_scale) {
+    const int64_t n = (int64_t)nx * ny;
+    const bool per = boundary == LBGB_PERIODIC;
+    for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < n; c += (int64_t)gridDim.x * blockDim.x) {
+        const int k = (int)(c / ny), l = (int)(c - (int64_t)k * ny);
+        // lid at l = ny-1 moves with (u0, 0); every other wall rests
+        const T dxux = grad1<T>(ux, c, ny, k, nx, per, T(0), T(0));
+        const T dxuy = grad1<T>(uy, c, ny, k, nx, per, T(0), T(0));
+        const T dyux = grad1<T>(ux, c, 1, l, ny, per, T(0), u0);
+        const T dyuy = grad1<T>(uy, c, 1, l, ny, per, T(0), T(0));
+        T feq[9];
+        equilibrium1<T>(rho[c], ux[c], uy[c], feq);
+        const T pre = neq_scale * T(3) * rho[c] / omega;
+#pragma unroll
+        for (int i = 0; i < 9; ++i) {
+            const T ex = T(cx(i)), ey = T(cy(i));
+            const T q = (ex * ex - T(1.0 / 3.0)) * dxux + ex * ey * (dxuy + dyux) + (ey * ey - T(1.0 / 3.0)) * dyuy;
+            f[i * n + c] = feq[i] - pre * wgt<T>(i) * q;
+        }
+    }
+}
+
 // ---------------------------------------------------------------- collide
 // One thread relaxes V consecutive cells; vector access when the channel
 // stride and the pointer allow it, else element by element.
@@ -282,6 +327,36 @@ extern "C" int lbgb_equilibrium(const void *rho, const void *ux, const void *uy,
         return LBGB_EDTYPE;
     }
     return check_launch("k_equilibrium");
+}
+
+extern "C" int lbgb_chapman_enskog(const void *rho, const void *ux, const void *uy, void *f, int nx, int ny,
+                                   double omega, double u0, int boundary, int post_collision, int dtype,
+                                   void *stream) {
+    if (!rho || !ux || !uy || !f || nx <= 0 || ny <= 0 || !(omega > 0.0)) {
+        set_error("lbgb_chapman_enskog: bad arguments (nx=%d ny=%d omega=%g)", nx, ny, omega);
+        return LBGB_EINVAL;
+    }
+    if (boundary != LBGB_PERIODIC && boundary != LBGB_CAVITY && boundary != LBGB_CAVITY_LADD) {
+        set_error("lbgb_chapman_enskog: unknown boundary code %d", boundary);
+        return LBGB_EINVAL;
+    }
+    const int64_t n = (int64_t)nx * ny;
+    cudaStream_t s = (cudaStream_t)stream;
+    const double lid = boundary == LBGB_PERIODIC ? 0.0 : u0;
+    const double scale = post_collision ? 1.0 - omega : 1.0;
+    if (dtype == LBGB_F32) {
+        k_chapman_enskog<float><<<grid_for(n, 256), 256, 0, s>>>((const float *)rho, (const float *)ux,
+                                                                 (const float *)uy, (float *)f, nx, ny, (float)omega,
+                                                                 (float)lid, boundary, (float)scale);
+    } else if (dtype == LBGB_F64) {
+        k_chapman_enskog<double><<<grid_for(n, 256), 256, 0, s>>>((const double *)rho, (const double *)ux,
+                                                                  (const double *)uy, (double *)f, nx, ny, omega,
+                                                                  lid, boundary, scale);
+    } else {
+        set_error("lbgb_chapman_enskog: storage code %d not supported (F32 or F64)", dtype);
+        return LBGB_EDTYPE;
+    }
+    return check_launch("k_chapman_enskog");
 }
 
 extern "C" int lbgb_collide(void *f, int64_t n, int64_t chan_stride, int dtype, double omega, void *stream) {

@@ -136,8 +136,7 @@ class Lattice:
                       self.cells, self.cells, self._stream())
         return self
 
-    def equilibrium(self, rho=None, ux=None, uy=None):
-        """Set the populations to the equilibrium of (rho, ux, uy) (default: rest)."""
+    def _fields(self, rho, ux, uy):
         real = torch.float64 if self.storage == "f64" else torch.float32
         shape = (self.nx, self.ny)
 
@@ -147,18 +146,36 @@ class Lattice:
             v = torch.as_tensor(v, dtype=real, device=self.device)
             return v.expand(shape).contiguous()
 
-        r, x, y = field(rho, 1.0), field(ux, 0.0), field(uy, 0.0)
+        return field(rho, 1.0), field(ux, 0.0), field(uy, 0.0)
+
+    def _set_from(self, fill):
+        """Run ``fill(out_ptr, code)`` into the state (through FP32 for 16-bit storage)."""
         code = _lib.F64 if self.storage == "f64" else _lib.F32
         if self.storage in ("f32", "f64"):
-            _lib.call("lbgb_equilibrium", r.data_ptr(), x.data_ptr(), y.data_ptr(), self.state.data_ptr(),
-                      self.cells, self.cells, code, self._stream())
+            fill(self.state.data_ptr(), code)
         else:
             tmp = torch.empty((9, self.nx, self.ny), dtype=torch.float32, device=self.device)
-            _lib.call("lbgb_equilibrium", r.data_ptr(), x.data_ptr(), y.data_ptr(), tmp.data_ptr(),
-                      self.cells, self.cells, code, self._stream())
+            fill(tmp.data_ptr(), code)
             _lib.call("lbgb_convert", tmp.data_ptr(), _lib.F32, self.cells, self.state.data_ptr(), self.code,
                       self.cells, self.cells, self._stream())
         return self
+
+    def equilibrium(self, rho=None, ux=None, uy=None):
+        """Set the populations to the equilibrium of (rho, ux, uy) (default: rest)."""
+        r, x, y = self._fields(rho, ux, uy)
+        return self._set_from(lambda out, code: _lib.call(
+            "lbgb_equilibrium", r.data_ptr(), x.data_ptr(), y.data_ptr(), out, self.cells, self.cells, code,
+            self._stream()))
+
+    def chapman_enskog(self, rho=None, ux=None, uy=None):
+        """Set the populations from the flow (rho, ux, uy) with its first-order
+        Chapman-Enskog non-equilibrium part at this lattice's omega, in the
+        post-collision form f^eq + (1 - omega) f^neq that a step leaves: the
+        start that lets a predicted steady field skip the initial transient."""
+        r, x, y = self._fields(rho, ux, uy)
+        return self._set_from(lambda out, code: _lib.call(
+            "lbgb_chapman_enskog", r.data_ptr(), x.data_ptr(), y.data_ptr(), out, self.nx, self.ny, self.omega,
+            self.u0, self.bcode, 1, code, self._stream()))
 
     def populations(self, dtype=None, out=None):
         """The populations f as a float tensor ``(9, nx, ny)`` (decoded for 16-bit storage).

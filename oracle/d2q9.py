@@ -223,6 +223,44 @@ def cavity_ladd_step(f, omega, u0=0.1):
     return collide(f, omega)
 
 
+def _grad(u, axis, periodic, wall_lo=0.0, wall_hi=0.0):
+    """d u / d axis: central differences; at a cavity wall the quadratic through
+    the wall value half a cell out and the next two nodes."""
+    n = u.shape[axis]
+    if n < 2:
+        return np.zeros_like(u)
+    if periodic:
+        return 0.5 * (np.roll(u, -1, axis) - np.roll(u, 1, axis))
+    u = np.moveaxis(u, axis, 0)
+    g = np.empty_like(u)
+    g[1:-1] = 0.5 * (u[2:] - u[:-2])
+    g[0] = -4.0 / 3.0 * wall_lo + u[0] + u[1] / 3.0
+    g[-1] = 4.0 / 3.0 * wall_hi - u[-1] - u[-2] / 3.0
+    return np.moveaxis(g, 0, axis)
+
+
+def chapman_enskog(rho, ux, uy, omega, periodic=False, u0=0.0, post_collision=False):
+    """Equilibrium plus first-order Chapman-Enskog non-equilibrium populations.
+
+    f_i = f_i^eq - (3 w_i rho / omega) (c_ia c_ib - delta_ab/3) d_a u_b (c_s^2 = 1/3);
+    post_collision: f^eq + (1 - omega) f^neq, the state a step leaves.
+    Not in the reference (its cavity starts from rest, cavity_opt1.py:333-335);
+    the warm start of a predicted flow uses it.  For the cavity the lid (l = ny-1)
+    moves with (u0, 0) and the other walls rest.
+    """
+    dxux = _grad(ux, 0, periodic)
+    dxuy = _grad(uy, 0, periodic)
+    dyux = _grad(ux, 1, periodic, 0.0, u0)
+    dyuy = _grad(uy, 1, periodic)
+    f = equilibrium(rho, ux, uy)
+    scale = (1.0 - omega) if post_collision else 1.0
+    for i in range(9):
+        ex, ey = float(CX[i]), float(CY[i])
+        q = (ex * ex - 1.0 / 3.0) * dxux + ex * ey * (dxuy + dyux) + (ey * ey - 1.0 / 3.0) * dyuy
+        f[i] -= scale * 3.0 * W_I[i] * rho / omega * q
+    return f
+
+
 def cavity_step(f, omega, u0=0.1):
     """One cavity time step in the reference's order (cavity_opt1.py:341-343)."""
     stream_and_bounce_back(f, u0)

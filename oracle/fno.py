@@ -35,23 +35,34 @@ def ky_modes(H, m):
     return np.concatenate([np.arange(m), np.arange(H - m, H)])
 
 
-def dft_mats(H, W, m):
-    """Real matrices of the factorised transform.
+def dft_mats(H, W, m, Hp=None, Wp=None):
+    """Real matrices of the factorised transform over a zero-padded period.
 
-    fw  (2m, W):  rows kx: cos(2 pi kx w/W), rows m+kx: -sin(...)        (forward, along W)
-    ch, sh (2m, H): cos / sin(2 pi ky h/H) for the kept ky                (along H, both ways)
-    iw  (W, 2m):  inverse along W: c_kx cos / -c_kx sin, c_0 = 1, c_kx = 2, scaled by 1/(H W)
+    The field (H, W) is read as the corner of a (Hp, Wp) zero-padded field
+    (Hp >= H, Wp >= W; default no padding) and only the H x W corner of the
+    result is kept, so the convolution is not forced to be periodic over the
+    cavity.  Padding costs nothing here: it only changes the frequencies.
+    fw  (2m, W):  rows kx: cos(2 pi kx w/Wp), rows m+kx: -sin(...)       (forward, along W)
+    ch, sh (2m, H): cos / sin(2 pi ky h/Hp) for the kept ky               (along H, both ways)
+    iw  (W, 2m):  inverse along W: c_kx cos / -c_kx sin, c_0 = 1, c_kx = 2, scaled by 1/(Hp Wp)
     """
+    Hp = H if Hp is None else Hp
+    Wp = W if Wp is None else Wp
     w = np.arange(W)
     kx = np.arange(m)
-    ang = 2 * np.pi * np.outer(kx, w) / W
+    ang = 2 * np.pi * np.outer(kx, w) / Wp
     fw = np.concatenate([np.cos(ang), -np.sin(ang)], axis=0)
-    ky = ky_modes(H, m)
-    angh = 2 * np.pi * np.outer(ky, np.arange(H)) / H
+    ky = ky_modes(Hp, m)
+    angh = 2 * np.pi * np.outer(ky, np.arange(H)) / Hp
     ch, sh = np.cos(angh), np.sin(angh)
     c = np.where(kx == 0, 1.0, 2.0)
-    iw = np.concatenate([(c[:, None] * np.cos(ang)).T, (-c[:, None] * np.sin(ang)).T], axis=1) / (H * W)
+    iw = np.concatenate([(c[:, None] * np.cos(ang)).T, (-c[:, None] * np.sin(ang)).T], axis=1) / (Hp * Wp)
     return fw, ch, sh, iw
+
+
+def padded_size(n, pad_frac):
+    """Padded period for a side of n cells: n (1 + pad_frac), rounded up to a multiple of 8."""
+    return int(-(-round(n * (1 + pad_frac)) // 8) * 8) if pad_frac > 0 else n
 
 
 def spectral_forward(v, Rr, Ri, mats):
@@ -156,14 +167,19 @@ def loss_and_grads(p, a, target, mats, layers=4):
     return loss, g, out
 
 
-def fft_spectral_reference(v, Rr, Ri, m):
-    """The same spectral convolution written with numpy.fft (for the check)."""
+def fft_spectral_reference(v, Rr, Ri, m, Hp=None, Wp=None):
+    """The same spectral convolution written with numpy.fft (for the check):
+    zero-pad to (Hp, Wp), transform, mix the kept modes, transform back, crop."""
     B, C, H, W = v.shape
-    vh = np.fft.rfft2(v, axes=(2, 3))
-    ky = ky_modes(H, m)
+    Hp = H if Hp is None else Hp
+    Wp = W if Wp is None else Wp
+    vp = np.zeros((B, C, Hp, Wp))
+    vp[:, :, :H, :W] = v
+    vh = np.fft.rfft2(vp, axes=(2, 3))
+    ky = ky_modes(Hp, m)
     X = vh[:, :, ky, :m]
     R = Rr + 1j * Ri
     Y = np.einsum("bcyk,coyk->boyk", X, R)
-    full = np.zeros((B, R.shape[1], H, W // 2 + 1), dtype=complex)
+    full = np.zeros((B, R.shape[1], Hp, Wp // 2 + 1), dtype=complex)
     full[:, :, ky, :m] = Y
-    return np.fft.irfft2(full, s=(H, W), axes=(2, 3))
+    return np.fft.irfft2(full, s=(Hp, Wp), axes=(2, 3))[:, :, :H, :W]

@@ -3,19 +3,22 @@ the numpy.fft definition, and its hand-derived gradients equal central finite
 differences."""
 
 import numpy as np
+import pytest
 
 from oracle import fno
 
 
-def test_factorised_spectral_conv_equals_fft():
+@pytest.mark.parametrize("pad", [None, (40, 32), (36, 30)])
+def test_factorised_spectral_conv_equals_fft(pad):
     rng = np.random.default_rng(0)
     B, C, O, H, W, m = 2, 3, 4, 32, 24, 5
+    Hp, Wp = pad if pad else (None, None)
     v = rng.standard_normal((B, C, H, W))
     Rr = rng.standard_normal((C, O, 2 * m, m))
     Ri = rng.standard_normal((C, O, 2 * m, m))
-    mats = fno.dft_mats(H, W, m)
+    mats = fno.dft_mats(H, W, m, Hp, Wp)
     out, _ = fno.spectral_forward(v, Rr, Ri, mats)
-    ref = fno.fft_spectral_reference(v, Rr, Ri, m)
+    ref = fno.fft_spectral_reference(v, Rr, Ri, m, Hp, Wp)
     assert np.abs(out - ref).max() < 1e-12
 
 
@@ -26,7 +29,7 @@ def test_gradients_match_finite_differences():
     p = fno.init_params(rng, width=6, modes=m, layers=2, hidden=10)
     a = rng.standard_normal((2, 4, H, W))
     target = rng.standard_normal((2, 3, H, W))
-    mats = fno.dft_mats(H, W, m)
+    mats = fno.dft_mats(H, W, m, 20, 24)
     loss, g, _ = fno.loss_and_grads(p, a, target, mats, layers=2)
     for name in ["P", "pb", "W0", "b1", "Rr0", "Ri1", "Q1", "q2b"]:
         x = p[name]

@@ -1,0 +1,105 @@
+"""The GPU Fourier neural operator (BF16 tensor-core GEMMs, FP32 accumulation)
+against the float64 oracle network with the same weights.
+
+Tolerances: BF16 keeps 8 significant bits (relative rounding 2^-9 per value),
+and every layer rounds its activations once, so the network output is held
+to 3e-2 relative L2 and each parameter gradient to 6e-2 relative L2 with a
+cosine similarity above 0.995 -- an error in a layout, a stride or a sign
+gives O(1) errors on these measures."""
+
+import numpy as np
+import pytest
+import torch
+
+from latticeboltzmann_gb300 import fno as F
+from oracle import fno as ofno
+
+pytestmark = pytest.mark.gpu
+
+
+def rel(a, b):
+    return np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-30)
+
+
+def setup(cuda, B=2, H=32, W=24, engine=0, seed=0, layers=4):
+    net = F.FNO2d(layers=layers, device=cuda, seed=seed, engine=engine)
+    rng = np.random.default_rng(seed + 1)
+    a = rng.standard_normal((B, 4, H, W))
+    t = rng.standard_normal((B, 3, H, W))
+    Hp, Wp = F.padded_size(H, net.pad), F.padded_size(W, net.pad)
+    mats = ofno.dft_mats(H, W, net.modes, Hp, Wp)
+    dev_a = torch.from_numpy(a.transpose(1, 0, 2, 3).copy()).float().to(cuda)
+    dev_t = torch.from_numpy(t.transpose(1, 0, 2, 3).copy()).float().to(cuda)
+    return net, a, t, mats, dev_a, dev_t
+
+
+def test_dft_matrices_equal_oracle():
+    fw, G, iw = F.dft_matrices(20, 28, 5, 32, 40)
+    ofw, ch, sh, oiw = ofno.dft_mats(20, 28, 5, 32, 40)
+    np.testing.assert_allclose(fw, ofw, atol=1e-15)
+    np.testing.assert_allclose(G, np.concatenate([ch, sh]), atol=1e-15)
+    np.testing.assert_allclose(iw, oiw, atol=1e-15)
+
+
+@pytest.mark.parametrize("engine", [0, 1])
+@pytest.mark.parametrize("shape", [(2, 32, 24), (3, 40, 40)])
+def test_forward_matches_oracle(cuda, engine, shape):
+    B, H, W = shape
+    net, a, t, mats, dev_a, _ = setup(cuda, B, H, W, engine)
+    out = net.forward(dev_a).cpu().double().numpy().transpose(1, 0, 2, 3)
+    ref, _ = ofno.forward(net.params(), a, mats)
+    assert rel(out, ref) < 3e-2, rel(out, ref)
+
+
+@pytest.mark.parametrize("engine", [0, 1])
+def test_gradients_match_oracle(cuda, engine):
+    net, a, t, mats, dev_a, dev_t = setup(cuda, 2, 32, 24, engine, seed=3)
+    # scale the spectral weights up so that the Fourier path carries real signal
+    p = net.params()
+    for l in range(net.layers):
+        p["Rr%d" % l] *= 30
+        p["Ri%d" % l] *= 30
+    net.load_params(p)
+    loss = float(net.loss_and_backward(dev_a, dev_t))
+    ref_loss, ref_g, _ = ofno.loss_and_grads(net.params(), a, t, mats)
+    assert abs(loss / ref_loss - 1) < 2e-2
+    g = net.grads()
+    for name, r in ref_g.items():
+        x = g[name]
+        cos = float((x * r).sum() / (np.linalg.norm(x) * np.linalg.norm(r) + 1e-30))
+        assert rel(x, r) < 6e-2 and cos > 0.995, (name, rel(x, r), cos)
+
+
+def test_engines_agree_and_training_reduces_loss(cuda):
+    """Tensor-core and CUDA-core GEMMs give the same network to BF16 rounding;
+    a few Adam steps on a fixed batch reduce its loss."""
+    net0, a, t, mats, dev_a, dev_t = setup(cuda, 2, 32, 32, 0, seed=5)
+    net1 = F.FNO2d(device=cuda, seed=5, engine=1)
+    o0 = net0.forward(dev_a).clone()
+    o1 = net1.forward(dev_a).clone()
+    assert rel(o0.cpu().numpy(), o1.cpu().numpy()) < 1e-2
+    first = float(net0.loss_and_backward(dev_a, dev_t))
+    for _ in range(30):
+        net0.loss_and_backward(dev_a, dev_t)
+        net0.adam(3e-3)
+    last = float(net0.loss_and_backward(dev_a, dev_t))
+    assert last < 0.7 * first, (first, last)
+    torch.cuda.synchronize()
+
+
+def test_cavity_inputs_targets_and_prediction_round_trip(cuda, tmp_path):
+    net = F.FNO2d(device=cuda, seed=1)
+    a = net.inputs([10.0, 1000.0], [0.05, 0.1], 8, 6)
+    assert a.shape == (4, 2, 8, 6)
+    assert torch.allclose(a[2, :, 0, 0].cpu(), torch.tensor([-1.0, 1.0]))
+    assert torch.allclose(a[3, :, 0, 0].cpu(), torch.tensor([-1.0, 1.0]))
+    fields = torch.rand(2, 3, 8, 6, device=cuda) * 0.01 + torch.tensor([1.0, 0, 0], device=cuda)[None, :, None, None]
+    tg = F.FNO2d.targets(fields, [0.05, 0.1])
+    assert torch.allclose(1 + tg[0] * torch.tensor([0.05, 0.1], device=cuda)[:, None, None] ** 2, fields[:, 0])
+    path = tmp_path / "net.npz"
+    net.save(path)
+    net2 = F.FNO2d.load(path, device=cuda)
+    r1 = net.predict([30.0], [0.08], 32, 32)
+    r2 = net2.predict([30.0], [0.08], 32, 32)
+    for x, y in zip(r1, r2):
+        assert torch.equal(x, y)
