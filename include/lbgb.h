@@ -198,7 +198,8 @@ LBGB_API int lbgb_batch_shear_amplitude(const void *f, long long total_elems,
  * instance b of |u - u_prev| (x and y components, FP32), then u_prev <- u.
  * u_prev: 2 floats per cell, instances back to back at 2*cell_base.
  * Called every m steps it gives the criterion max|u^(n+m) - u^n| of the
- * steady-cavity data set.  No counterpart in the reference. */
+ * steady-cavity data set.  A non-finite velocity (a diverged instance) gives
+ * +inf, so it never reads as converged.  No counterpart in the reference. */
 LBGB_API int lbgb_batch_velocity_change(const void *f, long long total_elems,
                                         const void *instances, int n_instances, int dtype,
                                         float *u_prev, long long total_cells, float *out_dev,

@@ -176,6 +176,18 @@ class BatchedLattice:
             return 1.0, (amplitude * torch.sin(2 * math.pi * l / ny))[None, :], 0.0
         return self.equilibrium(fields)
 
+    def load(self, b, f):
+        """Set instance b from a float tensor (9, nx, ny) (FP32 or FP64, any device)."""
+        nx, ny = self.sizes[b]
+        n = nx * ny
+        f = torch.as_tensor(f).to(self.device)
+        if tuple(f.shape) != (9, nx, ny) or f.dtype not in (torch.float32, torch.float64):
+            raise ValueError("expected a float32/float64 tensor of shape %s" % ((9, nx, ny),))
+        f = f.contiguous()
+        src = _lib.F64 if f.dtype == torch.float64 else _lib.F32
+        _lib.call("lbgb_convert", f.data_ptr(), src, n, self._slice(b).data_ptr(), self.code, n, n, self._stream())
+        return self
+
     def populations(self, b, dtype=torch.float64):
         """Instance b as a (9, nx, ny) float tensor."""
         nx, ny = self.sizes[b]
@@ -391,8 +403,33 @@ def omega_for(re, u_lid, length):
     return 2.0 * re / (6.0 * length * u_lid + re)
 
 
+def _run_to_steady(bl, tol, every, max_steps, log=None, what=""):
+    """Step the active instances of bl until max|u^(t+every) - u^t| < tol;
+    converged instances leave the queue.  Returns (steps per instance, -1 if
+    max_steps passed; last velocity change per instance)."""
+    bl.velocity_change()
+    steps = np.full(bl.n, -1, dtype=np.int64)
+    steps[~bl.active] = 0
+    change = np.full(bl.n, np.inf)
+    done = 0
+    while done < max_steps and (steps < 0).any():
+        bl.step(every)
+        done += every
+        ch = bl.velocity_change().cpu().numpy()
+        live = steps < 0
+        change[live] = ch[live]
+        newly = live & (ch < tol)
+        steps[newly] = done
+        if newly.any():
+            bl.set_active(steps < 0)
+        if log is not None and done % (every * 50) == 0:
+            log("steady_cavities%s: %d steps, %d/%d converged" % (what, done, int((steps >= 0).sum()), bl.n))
+    return steps, change
+
+
 def steady_cavities(re, u_lid, n=256, tol=1e-7, every=1000, max_steps=1_000_000, storage="f32", device=None,
-                    tune=True, log=None, boundary="cavity-ladd", start=None):
+                    tune=True, log=None, boundary="cavity-ladd", start=None, refine=None, switch_tol=1e-6,
+                    info=None):
     """Run lid-driven cavities (n x n) to steady state, all in one batch.
 
     The default lid is the wall-density-1 one: the reference's lid adds mass
@@ -401,35 +438,52 @@ def steady_cavities(re, u_lid, n=256, tol=1e-7, every=1000, max_steps=1_000_000,
     start: None (rest) or ``start(b) -> (rho, ux, uy)`` (n x n tensors), a
     predicted flow from which instance b starts in its Chapman-Enskog state.
     Steady: max over the cavity of |u^(t+every) - u^t| < tol.  Converged
-    instances leave the task queue.  Returns (fields float32 (N, 3, n, n) of
-    rho, ux, uy; steps to convergence per instance, -1 if max_steps passed;
-    wall seconds, from the first step to the last check).
+    instances leave the task queue.
+
+    refine: None, or a wider storage ("f64") for a second phase: the batch
+    runs in ``storage`` until the change is below max(tol, switch_tol), then
+    continues in ``refine`` storage down to tol.  FP32 storage has a rounding
+    floor of about 1e-7 per 1000 steps at high Reynolds numbers, so tol = 1e-7
+    needs FP64 there.
+
+    Returns (fields float32 (N, 3, n, n) of rho, ux, uy; steps to convergence
+    per instance, summed over both phases, -1 if a phase hit max_steps; wall
+    seconds from the first step to the last check).  ``info`` (a dict), when
+    given, receives the per-phase steps and last velocity changes.
     """
     re = np.asarray(re, dtype=np.float64)
     u_lid = np.asarray(u_lid, dtype=np.float64)
     om = omega_for(re, u_lid, n)
-    bl = BatchedLattice([(n, n)] * len(re), om, boundary=boundary, u0=u_lid, storage=storage, device=device)
+    sizes = [(n, n)] * len(re)
+    bl = BatchedLattice(sizes, om, boundary=boundary, u0=u_lid, storage=storage, device=device)
     if start is None:
         bl.equilibrium(lambda b: (1.0, 0.0, 0.0))
     if tune:
         bl.autotune(steps=3, warmup=1)
     if start is not None:
         bl.chapman_enskog(start)
-    bl.velocity_change()
-    steps = np.full(len(re), -1, dtype=np.int64)
     torch.cuda.synchronize(bl.device)
     t0 = time.perf_counter()
-    done = 0
-    while done < max_steps and (steps < 0).any():
-        bl.step(every)
-        done += every
-        ch = bl.velocity_change().cpu().numpy()
-        newly = (steps < 0) & (ch < tol)
-        steps[newly] = done
-        if newly.any():
-            bl.set_active(steps < 0)
-        if log is not None and done % (every * 50) == 0:
-            log("steady_cavities: %d steps, %d/%d converged" % (done, int((steps >= 0).sum()), len(re)))
+    tol1 = tol if refine is None else max(tol, switch_tol)
+    steps, change = _run_to_steady(bl, tol1, every, max_steps, log, "")
+    if info is not None:
+        info["phase1_steps"], info["phase1_change"] = steps.copy(), change.copy()
+    if refine is not None and tol1 > tol:
+        bl2 = BatchedLattice(sizes, om, boundary=boundary, u0=u_lid, storage=refine, device=device)
+        ok = steps >= 0
+        for b in range(len(re)):
+            bl2.load(b, bl.populations(b, torch.float64))
+        del bl
+        if tune:
+            bl2.autotune(steps=3, warmup=1)
+        bl2.set_active(ok)
+        s2, change = _run_to_steady(bl2, tol, every, max_steps, log, " (%s)" % refine)
+        if info is not None:
+            info["phase2_steps"], info["phase2_change"] = s2.copy(), change.copy()
+        steps = np.where(ok & (s2 >= 0), steps + s2, -1)
+        bl = bl2
+    if info is not None:
+        info["change"] = change
     torch.cuda.synchronize(bl.device)
     wall = time.perf_counter() - t0
     out = torch.empty((len(re), 3, n, n), dtype=torch.float32, device=bl.device)

@@ -198,7 +198,9 @@ k_batch_velocity_change(const typename Codec<DT>::raw *__restrict__ f, long long
             for (int i = 1; i < 9; ++i) rho += v[i];
             const float ux = (float)((v[1] - v[3] + v[5] - v[6] - v[7] + v[8]) / rho);
             const float uy = (float)((v[2] - v[4] + v[5] + v[6] - v[7] - v[8]) / rho);
-            m = fmaxf(m, fmaxf(fabsf(ux - up[2 * c]), fabsf(uy - up[2 * c + 1])));
+            float d = fmaxf(fabsf(ux - up[2 * c]), fabsf(uy - up[2 * c + 1]));
+            if (!(d <= 3.0e38f)) d = INFINITY;  // a NaN (diverged run) must never read as converged
+            m = fmaxf(m, d);
             up[2 * c] = ux;
             up[2 * c + 1] = uy;
         }

@@ -276,28 +276,29 @@ static int launch_gemm(int m, int n, int k, const __nv_bfloat16 *a, long long a_
                                               alpha, beta);
         return check_launch("k_gemm_simt");
     }
-    // tensor cores: tile N 32/64/128 by problem width.  The extra dynamic
-    // shared memory (unused) caps residency at 3 CTAs per SM, so their tensor
-    // memory (<= 3 x 128 of 512 columns) never makes an allocation wait.
-    const int pad = 40 * 1024;
+    // tensor cores: tile N 32/64/128 by problem width.  Unused dynamic shared
+    // memory caps the CTAs resident on one SM so that their tensor memory
+    // (NT columns each) never exceeds the SM's 512 columns and no allocation
+    // has to wait: 24.6 KB static -> 9 CTAs x 32 columns; + 4 KB -> 7 x 64;
+    // 32.8 KB static + 16 KB -> 4 x 128.
+    const int pad32 = 0, pad64 = 4 * 1024, pad128 = 16 * 1024;
     static bool attr_set = false;  // one flag per output type (one instantiation each)
     if (!attr_set) {
-        cudaFuncSetAttribute(k_gemm_tc<32, OUT>, cudaFuncAttributeMaxDynamicSharedMemorySize, pad);
-        cudaFuncSetAttribute(k_gemm_tc<64, OUT>, cudaFuncAttributeMaxDynamicSharedMemorySize, pad);
-        cudaFuncSetAttribute(k_gemm_tc<128, OUT>, cudaFuncAttributeMaxDynamicSharedMemorySize, pad);
+        cudaFuncSetAttribute(k_gemm_tc<64, OUT>, cudaFuncAttributeMaxDynamicSharedMemorySize, pad64);
+        cudaFuncSetAttribute(k_gemm_tc<128, OUT>, cudaFuncAttributeMaxDynamicSharedMemorySize, pad128);
         attr_set = true;
     }
     if (n <= 32) {
         dim3 grid((m + TC_M - 1) / TC_M, (n + 31) / 32, batch);
-        k_gemm_tc<32, OUT><<<grid, 128, pad, s>>>(m, n, k, a, a_rs, a_cs, a_bs, b, b_rs, b_cs, b_bs, C, c_rs, c_cs,
+        k_gemm_tc<32, OUT><<<grid, 128, pad32, s>>>(m, n, k, a, a_rs, a_cs, a_bs, b, b_rs, b_cs, b_bs, C, c_rs, c_cs,
                                                   c_bs, alpha, beta);
     } else if (n <= 64) {
         dim3 grid((m + TC_M - 1) / TC_M, (n + 63) / 64, batch);
-        k_gemm_tc<64, OUT><<<grid, 128, pad, s>>>(m, n, k, a, a_rs, a_cs, a_bs, b, b_rs, b_cs, b_bs, C, c_rs, c_cs,
+        k_gemm_tc<64, OUT><<<grid, 128, pad64, s>>>(m, n, k, a, a_rs, a_cs, a_bs, b, b_rs, b_cs, b_bs, C, c_rs, c_cs,
                                                   c_bs, alpha, beta);
     } else {
         dim3 grid((m + TC_M - 1) / TC_M, (n + 127) / 128, batch);
-        k_gemm_tc<128, OUT><<<grid, 128, pad, s>>>(m, n, k, a, a_rs, a_cs, a_bs, b, b_rs, b_cs, b_bs, C, c_rs, c_cs,
+        k_gemm_tc<128, OUT><<<grid, 128, pad128, s>>>(m, n, k, a, a_rs, a_cs, a_bs, b, b_rs, b_cs, b_bs, C, c_rs, c_cs,
                                                    c_bs, alpha, beta);
     }
     return check_launch("k_gemm_tc");

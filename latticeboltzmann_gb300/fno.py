@@ -31,6 +31,7 @@ the lid speed, each scaled to [-1, 1] over the training ranges.  Outputs
 (3 channels): (rho - 1) / u0^2, ux / u0, uy / u0.
 """
 
+import json
 import math
 
 import numpy as np
@@ -107,6 +108,7 @@ class FNO2d:
         self.v = torch.zeros(off, **f32)
         self.flat_bf16 = torch.zeros(off, dtype=torch.bfloat16, device=self.device)
         self.adam_steps = 0
+        self.out_scale = np.ones(cout)  # network output c is target channel c / out_scale[c]
         self._mats, self._ws = {}, {}
         self.init_params(np.random.default_rng(seed))
 
@@ -156,15 +158,16 @@ class FNO2d:
                 "params": self.params(), "adam_steps": self.adam_steps}
 
     def save(self, path):
+        """Weights (FP32), configuration and output scales in one .npz file."""
         sd = self.state_dict()
-        np.savez(path, config=np.array([sd["config"]], dtype=object),
-                 **{"p_" + k: v for k, v in sd["params"].items()})
+        np.savez(path, config=json.dumps(sd["config"]), out_scale=np.asarray(self.out_scale, dtype=np.float64),
+                 **{"p_" + k: v.astype(np.float32) for k, v in sd["params"].items()})
 
     @classmethod
     def load(cls, path, device=None, engine=ENGINE_TENSOR_CORES):
-        z = np.load(path, allow_pickle=True)
-        cfg = z["config"][0]
-        net = cls(device=device, engine=engine, **cfg)
+        z = np.load(path)
+        net = cls(device=device, engine=engine, **json.loads(str(z["config"])))
+        net.out_scale = np.asarray(z["out_scale"], dtype=np.float64)
         return net.load_params({k[2:]: z[k] for k in z.files if k.startswith("p_")})
 
     # ------------------------------------------------------------ plumbing
@@ -389,5 +392,6 @@ class FNO2d:
     def predict(self, re, u_lid, nx, ny):
         """Predicted steady (rho, ux, uy), each (B, nx, ny) float32 on the device."""
         out = self.forward(self.inputs(re, u_lid, nx, ny))
+        sc = [float(x) for x in self.out_scale]
         u = torch.as_tensor(np.atleast_1d(u_lid), dtype=torch.float32, device=self.device)[:, None, None]
-        return 1 + out[0] * u * u, out[1] * u, out[2] * u
+        return 1 + out[0] * (sc[0] * u * u), out[1] * (sc[1] * u), out[2] * (sc[2] * u)

@@ -1,0 +1,207 @@
+"""Surrogate warm start of the lid-driven cavity: training data, training, and
+the warm-versus-cold study.
+
+1. Training data: steady cavities from the batched solver (all instances in
+   one batch, converged ones leave the queue), Re log-uniform in [10, 1000]
+   and lid speed uniform in [0.05, 0.1], omega from Re = u L / nu with L the
+   side.  Steady means max over the cavity of |u^(t+1000) - u^t| < 1e-7; FP32
+   storage gets there below Re ~ 200, so the batch runs in FP32 down to 1e-6
+   and finishes in FP64.
+2. Training: the Fourier neural operator of ``fno.py`` on (Re, u) ->
+   normalised (rho, ux, uy), Adam with a cosine learning-rate schedule, all on
+   the package's kernels.
+3. Study: held-out (Re, u) pairs run to the same tolerance from rest (cold)
+   and from the predicted fields in their Chapman-Enskog state (warm); steps,
+   wall time (the warm side includes inference and the start kernel) and the
+   error of the prediction against the converged field.
+
+The reference has no learned part (its cavity always starts from rest,
+simulators/parallel_lid_drive_cavity/cavity_opt1.py:333-335).
+"""
+
+import argparse
+import json
+import math
+import os
+import time
+
+import numpy as np
+import torch
+
+from . import batch as B
+from .fno import FNO2d, RE_RANGE, U_RANGE
+
+
+def sample_parameters(n, seed=0, re_range=RE_RANGE, u_range=U_RANGE):
+    """n pairs (Re log-uniform over re_range, lid speed uniform over u_range)."""
+    rng = np.random.default_rng(seed)
+    re = np.exp(rng.uniform(math.log(re_range[0]), math.log(re_range[1]), n))
+    u = rng.uniform(u_range[0], u_range[1], n)
+    return re, u
+
+
+def steady_run(re, u, n, start=None, device=None, tol=1e-7, log=None, max_steps=600_000, tune=True):
+    """Two-phase steady runs of a batch; returns (fields (N, 3, n, n) FP32, steps, wall s, info)."""
+    info = {}
+    fields, steps, wall = B.steady_cavities(re, u, n=n, tol=tol, every=1000, max_steps=max_steps, storage="f32",
+                                            device=device, tune=tune, log=log, start=start, refine="f64",
+                                            switch_tol=max(tol, 1e-6), info=info)
+    return fields, steps, wall, info
+
+
+def generate(n_samples, n=256, seed=0, device=None, log=None, max_steps=600_000, re_range=RE_RANGE):
+    """Steady cavities for n_samples random (Re, u) pairs; instances that did not
+    settle within max_steps (or diverged: a 48^2 cavity at Re 1000 is beyond
+    the BGK stability limit) carry steps -1."""
+    re, u = sample_parameters(n_samples, seed, re_range)
+    fields, steps, wall, info = steady_run(re, u, n, device=device, log=log, max_steps=max_steps)
+    return {"re": re, "u": u, "fields": fields, "steps": steps, "wall": wall, "info": info}
+
+
+def train(net, data, idx, epochs=100, batch=16, lr=1e-3, lr_min=1e-5, log=None, seed=0, val_idx=None):
+    """Adam on the samples ``idx`` of ``data`` (cosine schedule from lr to lr_min).
+    Returns the history of (epoch, mean train loss, validation loss)."""
+    device = net.device
+    fields = data["fields"]
+    n = fields.shape[-1]
+    targets = FNO2d.targets(fields, data["u"])  # (3, S, n, n)
+    scale = targets[:, idx].reshape(3, -1).std(dim=1).clamp_min(1e-6)
+    net.out_scale = scale.cpu().numpy()
+    t_all = targets / scale[:, None, None, None]
+    a_all = net.inputs(data["re"], data["u"], n, n)
+    rng = np.random.default_rng(seed)
+    steps_per_epoch = max(1, len(idx) // batch)
+    total = epochs * steps_per_epoch
+    hist = []
+    k = 0
+    for ep in range(epochs):
+        perm = rng.permutation(idx)
+        acc = torch.zeros((), dtype=torch.float64, device=device)
+        for s in range(steps_per_epoch):
+            sel = torch.as_tensor(np.sort(perm[s * batch:(s + 1) * batch]), device=device)
+            a = a_all.index_select(1, sel).contiguous()
+            t = t_all.index_select(1, sel).contiguous()
+            acc += net.loss_and_backward(a, t)
+            cur = lr_min + 0.5 * (lr - lr_min) * (1 + math.cos(math.pi * k / total))
+            net.adam(cur)
+            k += 1
+        if log is not None and (ep % 10 == 0 or ep == epochs - 1):
+            vl = evaluate(net, data, val_idx) if val_idx is not None and len(val_idx) else float("nan")
+            tl = float(acc) / steps_per_epoch
+            hist.append((ep, tl, vl))
+            log("epoch %d train %.3e val rel-L2 %.3e lr %.2e" % (ep, tl, vl, cur))
+    return hist
+
+
+def evaluate(net, data, idx, batch=16):
+    """Mean relative L2 error of the predicted velocity over the samples idx."""
+    n = data["fields"].shape[-1]
+    errs = []
+    for s in range(0, len(idx), batch):
+        sel = np.asarray(idx[s:s + batch])
+        rho, ux, uy = net.predict(data["re"][sel], data["u"][sel], n, n)
+        f = data["fields"][torch.as_tensor(sel, device=net.device)]
+        num = ((ux - f[:, 1]) ** 2 + (uy - f[:, 2]) ** 2).sum(dim=(1, 2)).sqrt()
+        den = (f[:, 1] ** 2 + f[:, 2] ** 2).sum(dim=(1, 2)).sqrt()
+        errs.append((num / den).cpu())
+    return float(torch.cat(errs).mean())
+
+
+def study(net, re, u, n, device=None, tol=1e-7, log=None, max_steps=600_000, reference=None):
+    """Warm versus cold start on the pairs (re, u) at n x n, both as one batch.
+
+    Returns a dict with per-instance steps and the wall seconds of each side;
+    the warm wall time includes the network's inference and the start
+    kernel.  ``reference``: converged fields (N, 3, n, n) to compare the
+    prediction with; by default the cold run's own result."""
+    cold_f, cold_steps, cold_wall, _ = steady_run(re, u, n, device=device, tol=tol, log=log, max_steps=max_steps)
+    torch.cuda.synchronize(device)
+    t0 = time.perf_counter()
+    rho, ux, uy = net.predict(re, u, n, n)
+    torch.cuda.synchronize(device)
+    t_inf = time.perf_counter() - t0
+    warm_f, warm_steps, warm_wall, _ = steady_run(re, u, n, device=device, tol=tol, log=log, max_steps=max_steps,
+                                                  start=lambda b: (rho[b], ux[b], uy[b]))
+    ref = cold_f if reference is None else reference
+    du = ((ux - ref[:, 1]) ** 2 + (uy - ref[:, 2]) ** 2).sum(dim=(1, 2)).sqrt()
+    un = (ref[:, 1] ** 2 + ref[:, 2] ** 2).sum(dim=(1, 2)).sqrt()
+    dr = (rho - ref[:, 0]).abs().amax(dim=(1, 2))
+    # the two steady answers agree to the solver's tolerance
+    dfin = ((warm_f[:, 1:] - cold_f[:, 1:]).abs().amax(dim=(1, 2, 3)))
+    return {"n": n, "re": np.asarray(re).tolist(), "u": np.asarray(u).tolist(),
+            "cold_steps": cold_steps.tolist(), "warm_steps": warm_steps.tolist(),
+            "cold_wall_s": cold_wall, "warm_wall_s": warm_wall + t_inf, "inference_s": t_inf,
+            "pred_rel_l2_u": (du / un).cpu().numpy().tolist(), "pred_max_abs_rho": dr.cpu().numpy().tolist(),
+            "steady_max_abs_du_warm_vs_cold": dfin.cpu().numpy().tolist()}
+
+
+def main(argv=None):
+    ap = argparse.ArgumentParser(description="steady-cavity data, surrogate training and warm-start study")
+    ap.add_argument("--samples", type=int, default=2000)
+    ap.add_argument("--n", type=int, default=256)
+    ap.add_argument("--held-out", type=int, default=64)
+    ap.add_argument("--epochs", type=int, default=150)
+    ap.add_argument("--batch", type=int, default=16)
+    ap.add_argument("--lr", type=float, default=1e-3)
+    ap.add_argument("--max-steps", type=int, default=600_000)
+    ap.add_argument("--study-large", type=int, default=1024, help="side of the upsampled study (0: skip)")
+    ap.add_argument("--large-cases", type=int, default=4)
+    ap.add_argument("--seed", type=int, default=0)
+    ap.add_argument("--out", default="surrogate_out")
+    args = ap.parse_args(argv)
+    os.makedirs(args.out, exist_ok=True)
+    dev = torch.device("cuda", torch.cuda.current_device())
+    logf = open(os.path.join(args.out, "log.txt"), "a")
+
+    def log(m):
+        print(m, flush=True)
+        logf.write(m + "\n")
+        logf.flush()
+
+    t0 = time.perf_counter()
+    data = generate(args.samples, args.n, args.seed, dev, log, args.max_steps)
+    ok = np.nonzero(data["steps"] > 0)[0]
+    log("data: %d/%d steady in %.1f s; steps median %d max %d" % (len(ok), args.samples, data["wall"],
+                                                                   int(np.median(data["steps"][ok])),
+                                                                   int(data["steps"][ok].max())))
+    rng = np.random.default_rng(args.seed + 1)
+    perm = rng.permutation(ok)
+    val, tr = perm[:args.held_out], perm[args.held_out:]
+    net = FNO2d(device=dev, seed=args.seed)
+    t1 = time.perf_counter()
+    hist = train(net, data, tr, epochs=args.epochs, batch=args.batch, lr=args.lr, log=log, val_idx=val)
+    torch.cuda.synchronize()
+    t_train = time.perf_counter() - t1
+    net.save(os.path.join(args.out, "fno.npz"))
+    log("training: %.1f s, val rel-L2 %.3e" % (t_train, evaluate(net, data, val)))
+    res = {"samples": args.samples, "n": args.n, "steady": int(len(ok)), "data_wall_s": data["wall"],
+           "data_steps": data["steps"].tolist(), "data_re": data["re"].tolist(), "data_u": data["u"].tolist(),
+           "held_out": val.tolist(), "train_s": t_train, "history": hist}
+
+    def dump():
+        with open(os.path.join(args.out, "results.json"), "w") as f:
+            json.dump(res, f, indent=1)
+
+    dump()
+    res["study"] = study(net, data["re"][val], data["u"][val], args.n, dev, log=log, max_steps=args.max_steps,
+                         reference=data["fields"][torch.as_tensor(val, device=dev)])
+    s = res["study"]
+    log("study %d: cold %.1f s, warm %.1f s (inference %.3f s); steps cold %d warm %d (sums)" % (
+        args.n, s["cold_wall_s"], s["warm_wall_s"], s["inference_s"], sum(s["cold_steps"]), sum(s["warm_steps"])))
+    dump()
+    if args.study_large:
+        # cost grows like side^3 / Re at fixed Re: the upsampled study keeps to Re <= 150
+        low = val[data["re"][val] <= 150]
+        low = low[np.argsort(data["re"][low])]
+        sel = low[np.linspace(0, len(low) - 1, min(args.large_cases, len(low))).astype(int)] if len(low) else low
+        res["study_large"] = study(net, data["re"][sel], data["u"][sel], args.study_large, dev, log=log,
+                                   max_steps=1_500_000)
+        s = res["study_large"]
+        log("study %d: cold %.1f s, warm %.1f s; steps cold %s warm %s" % (
+            args.study_large, s["cold_wall_s"], s["warm_wall_s"], s["cold_steps"], s["warm_steps"]))
+    res["total_s"] = time.perf_counter() - t0
+    dump()
+
+
+if __name__ == "__main__":
+    main()

@@ -147,3 +147,15 @@ def test_steady_cavities_batch(cuda):
         lat.step(200)
         _, ux2, uy2 = lat.macroscopic()
         assert float(torch.maximum((ux2 - ux).abs(), (uy2 - uy).abs()).max()) < 1e-6
+
+
+def test_velocity_change_flags_diverged_instances(cuda):
+    """A NaN population makes the monitor report +inf (never 'converged')."""
+    bl = B.BatchedLattice([(16, 16), (8, 8)], [1.0, 1.0], boundary="cavity-ladd", u0=0.05, device=cuda)
+    bl.equilibrium(lambda b: (1.0, 0.0, 0.0))
+    bl.velocity_change()
+    f = bl.populations(1)
+    f[:, 3, 4] = float("nan")
+    bl.load(1, f)
+    ch = bl.velocity_change().cpu().numpy()
+    assert ch[0] == 0.0 and np.isinf(ch[1])

@@ -103,3 +103,28 @@ def test_cavity_inputs_targets_and_prediction_round_trip(cuda, tmp_path):
     r2 = net2.predict([30.0], [0.08], 32, 32)
     for x, y in zip(r1, r2):
         assert torch.equal(x, y)
+
+
+def test_surrogate_pipeline_small(cuda, tmp_path):
+    """The whole learned path at 48 x 48: steady training data from the batched
+    solver, training on the GPU kernels, and the warm start from the network's
+    prediction reaching the same steady state in fewer steps than from rest
+    (summed over held-out cavities)."""
+    from latticeboltzmann_gb300 import surrogate as S
+    n = 48
+    data = S.generate(40, n=n, seed=2, device=cuda, max_steps=200_000, re_range=(10.0, 100.0))
+    ok = np.nonzero(data["steps"] > 0)[0]
+    assert len(ok) == 40, data["steps"]
+    val, tr = ok[:6], ok[6:]
+    net = F.FNO2d(device=cuda, seed=0)
+    S.train(net, data, tr, epochs=60, batch=8, lr=2e-3)
+    err = S.evaluate(net, data, val)
+    assert err < 0.1, err
+    res = S.study(net, data["re"][val], data["u"][val], n, cuda, max_steps=200_000,
+                  reference=data["fields"][torch.as_tensor(val, device=cuda)])
+    assert all(s > 0 for s in res["cold_steps"] + res["warm_steps"])
+    assert sum(res["warm_steps"]) < sum(res["cold_steps"]), res
+    assert max(res["steady_max_abs_du_warm_vs_cold"]) < 1e-5
+    path = tmp_path / "net.npz"
+    net.save(path)
+    assert np.allclose(F.FNO2d.load(path, device=cuda).out_scale, net.out_scale)
