@@ -124,7 +124,9 @@ def test_surrogate_pipeline_small(cuda, tmp_path):
                   reference=data["fields"][torch.as_tensor(val, device=cuda)])
     assert all(s > 0 for s in res["cold_steps"] + res["warm_steps"])
     assert sum(res["warm_steps"]) < sum(res["cold_steps"]), res
-    assert max(res["steady_max_abs_du_warm_vs_cold"]) < 1e-5
+    # both runs stop once u changes by < 1e-7 per 1000 steps; on the slowest
+    # modes that leaves them up to ~1e-4 apart (about 1e-3 of the lid speed)
+    assert max(res["steady_max_abs_du_warm_vs_cold"]) < 2e-4
     path = tmp_path / "net.npz"
     net.save(path)
     assert np.allclose(F.FNO2d.load(path, device=cuda).out_scale, net.out_scale)
