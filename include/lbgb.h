@@ -205,6 +205,14 @@ LBGB_API int lbgb_batch_velocity_change(const void *f, long long total_elems,
                                         float *u_prev, long long total_cells, float *out_dev,
                                         void *stream);
 
+/* Decay diagnostic of the shear-wave scripts: out_dev[0] = 2/ny * max_k
+ * |DFT_k(ux[row, :])| (FP64; direct transform over the ny cells of one row,
+ * ny <= 4096), ux computed from the populations of the (9, nx, ny) array f.
+ * Replaces: simulators/simple_flows/shear_wave_decay.py:155-158 (numpy fft of
+ * ux[nx/2, :] on the host every step). */
+LBGB_API int lbgb_row_fft_amplitude(const void *f, int nx, int ny, int row, int dtype, double *out_dev,
+                                    void *stream);
+
 /* Start populations for a known flow: equilibrium plus the first-order
  * Chapman-Enskog non-equilibrium part,
  *   f_i = f_i^eq(rho, u) - (3 w_i rho / omega) (c_ia c_ib - delta_ab / 3) d_a u_b,

@@ -11,7 +11,7 @@ liblbgb.so; there is no CPU path.  ``Lattice`` is the device-resident solver
 from . import Collision, IO, Streaming
 from .Collision import collide, equilibrium
 from .Streaming import stream
-from .solver import Lattice, macroscopic, mass_momentum, omega_from_reynolds, viscosity_from_omega
+from .solver import Lattice, fft_amplitude, macroscopic, mass_momentum, omega_from_reynolds, viscosity_from_omega
 
 __all__ = ["collide", "equilibrium", "stream", "Collision", "Streaming", "IO", "Lattice", "macroscopic",
            "mass_momentum", "omega_from_reynolds", "viscosity_from_omega"]

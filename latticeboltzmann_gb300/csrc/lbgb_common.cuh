@@ -167,6 +167,18 @@ struct Packet {
         else
             return x;
     }
+    // packs N FP16 values that are already scaled by 2^14, two per conversion
+    static __device__ __forceinline__ vec enc_scaled(const real (&hs)[N]) {
+        uint32_t wd[WORDS];
+#pragma unroll
+        for (int q = 0; q < WORDS; ++q) {
+            const __half2 p = __floats2half2_rn(hs[2 * q], hs[2 * q + 1]);
+            wd[q] = *reinterpret_cast<const uint32_t *>(&p);
+        }
+        vec x;
+        memcpy(&x, wd, BYTES);
+        return x;
+    }
     // packs N deviations of a 16-bit codec, two per conversion
     static __device__ __forceinline__ vec enc_h(const real (&h)[N]) {
         uint32_t wd[WORDS];
@@ -250,17 +262,14 @@ __device__ __forceinline__ typename Packet<DT, N>::vec enc_h_sr(const float (&h)
 __device__ __forceinline__ float recip(float x) { return __frcp_rn(x); }
 __device__ __forceinline__ double recip(double x) { return __drcp_rn(x); }
 
+// BGK relaxation of one node with its density already summed.
 template <class R>
-__device__ __forceinline__ void bgk_collide(R (&f)[9], R omega, R &rho_out, R &ux_out, R &uy_out) {
-    R rho = f[0];
-#pragma unroll
-    for (int i = 1; i < 9; ++i) rho += f[i];
+__device__ __forceinline__ void bgk_relax(R (&f)[9], R omega, R rho, R &ux_out, R &uy_out) {
     const R inv = recip(rho);
     R ux = (f[1] - f[3] + f[5] - f[6] - f[7] + f[8]) * inv;
     R uy = (f[2] - f[4] + f[5] + f[6] - f[7] - f[8]) * inv;
     ux_out = ux;
     uy_out = uy;
-    rho_out = rho;
     const R w0 = rho * R(4.0 / 9.0), w1 = rho * R(1.0 / 9.0), w5 = rho * R(1.0 / 36.0);
     ux *= R(3);
     uy *= R(3);
@@ -284,9 +293,32 @@ __device__ __forceinline__ void bgk_collide(R (&f)[9], R omega, R &rho_out, R &u
 }
 
 template <class R>
+__device__ __forceinline__ void bgk_collide(R (&f)[9], R omega, R &rho_out, R &ux_out, R &uy_out) {
+    R rho = f[0];
+#pragma unroll
+    for (int i = 1; i < 9; ++i) rho += f[i];
+    rho_out = rho;
+    bgk_relax(f, omega, rho, ux_out, uy_out);
+}
+
+template <class R>
 __device__ __forceinline__ void bgk_collide(R (&f)[9], R omega) {
     R a, b, c;
     bgk_collide(f, omega, a, b, c);
+}
+
+// FP16 deviation storage, round to nearest: collide one node and return its
+// scaled mass deviation D S, D = sum_i (f_i - w_i) summed over the small
+// deviations (accurate to FP32 rounding of numbers ~1e-2, unbiased); the
+// density for the collision is 1 + D.  The mass fix stores the rest
+// population as D S minus what the other eight stored values carry.
+__device__ __forceinline__ float collide_f16_mass(float (&f)[9], float omega) {
+    float d = f[0] - wgt<float>(0);
+#pragma unroll
+    for (int i = 1; i < 9; ++i) d += f[i] - wgt<float>(i);
+    float ux, uy;
+    bgk_relax(f, omega, 1.f + d, ux, uy);
+    return d * F16_SCALE;
 }
 
 // Equilibrium of one node (same formulation as above).
@@ -344,16 +376,18 @@ __device__ __forceinline__ void collide_encode(typename Codec<DT>::real (&f)[9],
 #pragma unroll
         for (int i = 0; i < 9; ++i) out[i] = f[i];
     } else if constexpr (DT == LBGB_F16DEV) {
-        real dm = f[0] - wgt<real>(0);
-#pragma unroll
-        for (int i = 1; i < 9; ++i) dm += f[i] - wgt<real>(i);
-        bgk_collide(f, omega);
+        // Scaled deviations h S = f S - w S (one FMA each); the rest population
+        // takes the node's mass deviation minus what the other eight stored
+        // values carry, so the node keeps its mass up to the rounding of h_0
+        // alone.  The pipelined kernel does the same operations.
+        real dms = collide_f16_mass(f, omega);
 #pragma unroll
         for (int i = 1; i < 9; ++i) {
-            out[i] = C::enc(f[i], i);
-            dm -= C::dec_h(out[i]);
+            const __half q = __float2half_rn(fmaf(f[i], F16_SCALE, -wgt<float>(i) * F16_SCALE));
+            out[i] = __half_as_ushort(q);
+            dms -= __half2float(q);
         }
-        out[0] = C::enc_h(dm);
+        out[0] = __half_as_ushort(__float2half_rn(dms));
     } else {
         bgk_collide(f, omega);
 #pragma unroll

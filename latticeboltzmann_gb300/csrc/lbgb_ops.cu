@@ -178,6 +178,52 @@ __global__ void k_macroscopic(const typename Codec<DT>::raw *__restrict__ f, typ
     }
 }
 
+// ------------------------------------------------------ row spectrum amplitude
+// The decay diagnostic of simulators/simple_flows/shear_wave_decay.py:155-158:
+// 2/ny * max_k |DFT_k(ux[row, :])|, in FP64 (direct transform, one block).
+constexpr int SPEC_MAX_NY = 4096;
+
+template <int DT>
+__global__ void __launch_bounds__(256) k_row_fft_amplitude(const typename Codec<DT>::raw *__restrict__ f, int nx,
+                                                           int ny, int row, double *__restrict__ out) {
+    using C = Codec<DT>;
+    __shared__ double u[SPEC_MAX_NY];
+    __shared__ double red[256];
+    const int64_t cs = (int64_t)nx * ny;
+    for (int l = threadIdx.x; l < ny; l += blockDim.x) {
+        const int64_t c = (int64_t)row * ny + l;
+        double v[9];
+#pragma unroll
+        for (int i = 0; i < 9; ++i) v[i] = (double)C::dec(f[i * cs + c], i);
+        double r = v[0];
+#pragma unroll
+        for (int i = 1; i < 9; ++i) r += v[i];
+        u[l] = (v[1] - v[3] + v[5] - v[6] - v[7] + v[8]) / r;
+    }
+    __syncthreads();
+    double best = 0.0;
+    for (int k = threadIdx.x; k < ny; k += blockDim.x) {
+        double re = 0.0, im = 0.0;
+        int64_t ph = 0;  // k * l mod ny, kept exact
+        for (int l = 0; l < ny; ++l) {
+            double sv, cv;
+            sincospi(2.0 * (double)ph / (double)ny, &sv, &cv);
+            re += u[l] * cv;
+            im -= u[l] * sv;
+            ph += k;
+            if (ph >= ny) ph -= ny;
+        }
+        best = fmax(best, sqrt(re * re + im * im));
+    }
+    red[threadIdx.x] = best;
+    __syncthreads();
+    for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+        if (threadIdx.x < w) red[threadIdx.x] = fmax(red[threadIdx.x], red[threadIdx.x + w]);
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) out[0] = 2.0 / ny * red[0];
+}
+
 // ---------------------------------------------------------------- convert
 template <int SD, int DD>
 __global__ void k_convert(const typename Codec<SD>::raw *__restrict__ src, int64_t ss,
@@ -357,6 +403,27 @@ extern "C" int lbgb_chapman_enskog(const void *rho, const void *ux, const void *
         return LBGB_EDTYPE;
     }
     return check_launch("k_chapman_enskog");
+}
+
+extern "C" int lbgb_row_fft_amplitude(const void *f, int nx, int ny, int row, int dtype, double *out_dev,
+                                      void *stream) {
+    if (!f || !out_dev || nx <= 0 || ny <= 0 || ny > SPEC_MAX_NY || row < 0 || row >= nx) {
+        set_error("lbgb_row_fft_amplitude: bad arguments (nx=%d ny=%d row=%d; ny <= %d)", nx, ny, row, SPEC_MAX_NY);
+        return LBGB_EINVAL;
+    }
+    cudaStream_t s = (cudaStream_t)stream;
+    switch (dtype) {
+    case LBGB_F32: k_row_fft_amplitude<LBGB_F32><<<1, 256, 0, s>>>((const float *)f, nx, ny, row, out_dev); break;
+    case LBGB_F64: k_row_fft_amplitude<LBGB_F64><<<1, 256, 0, s>>>((const double *)f, nx, ny, row, out_dev); break;
+    case LBGB_F16DEV:
+        k_row_fft_amplitude<LBGB_F16DEV><<<1, 256, 0, s>>>((const unsigned short *)f, nx, ny, row, out_dev);
+        break;
+    case LBGB_BF16DEV:
+        k_row_fft_amplitude<LBGB_BF16DEV><<<1, 256, 0, s>>>((const unsigned short *)f, nx, ny, row, out_dev);
+        break;
+    default: set_error("lbgb_row_fft_amplitude: unsupported storage code %d", dtype); return LBGB_EDTYPE;
+    }
+    return check_launch("k_row_fft_amplitude");
 }
 
 extern "C" int lbgb_collide(void *f, int64_t n, int64_t chan_stride, int dtype, double omega, void *stream) {

@@ -254,6 +254,39 @@ k_step_pipe(const typename Codec<DT>::raw *__restrict__ src, typename Codec<DT>:
             // round every value stochastically and keep the mass the same way
             // (see collide_encode_sr).
             constexpr bool sr = SRND;
+            if constexpr (DT == LBGB_F16DEV && !SRND) {
+                // FP16, round to nearest: the operations of collide_encode<F16DEV>
+                // (mass deviation summed once, scaled deviations by one FMA), two
+                // values per conversion
+                real hs[9][NC];
+#pragma unroll
+                for (int j = 0; j < NC; ++j) {
+                    real f[9];
+#pragma unroll
+                    for (int i = 0; i < 9; ++i) f[i] = v[i][j];
+                    hs[0][j] = collide_f16_mass(f, omega);
+#pragma unroll
+                    for (int i = 1; i < 9; ++i) hs[i][j] = fmaf(f[i], F16_SCALE, -wgt<float>(i) * F16_SCALE);
+                }
+                typename P::vec pk[9];
+#pragma unroll
+                for (int i = 1; i < 9; ++i) {
+                    pk[i] = P::enc_scaled(hs[i]);
+                    uint32_t wd[NC / 2];
+                    memcpy(wd, &pk[i], sizeof(wd));
+#pragma unroll
+                    for (int q = 0; q < NC / 2; ++q) {
+                        const float2 y = __half22float2(*reinterpret_cast<const __half2 *>(&wd[q]));
+                        hs[0][2 * q] -= y.x;
+                        hs[0][2 * q + 1] -= y.y;
+                    }
+                }
+                pk[0] = P::enc_scaled(hs[0]);
+#pragma unroll
+                for (int i = 0; i < 9; ++i)
+                    st_cs(reinterpret_cast<typename P::vec *>(out_row + (size_t)i * cs), pk[i]);
+                continue;
+            }
             constexpr bool keep_mass = SRND || DT == LBGB_F16DEV;
             real hpost[9][NC];
             real dm[NC];

@@ -304,3 +304,21 @@ def macroscopic(f):
         _lib.call("lbgb_macroscopic", f.data_ptr(), rho.data_ptr(), ux.data_ptr(), uy.data_ptr(), n, cs, code,
                   stream_handle(f))
     return rho, ux, uy
+
+
+def fft_amplitude(f, row=None):
+    """2/ny * max_k |FFT(ux[row, :])| of a float32/float64 ``(9, nx, ny)`` CUDA
+    tensor (row defaults to nx // 2): the decay amplitude of the shear-wave
+    scripts (simulators/simple_flows/shear_wave_decay.py:155-158), computed on
+    the device.  Returns a float64 device scalar."""
+    from ._tensor import storage_code, stream_handle
+    if not isinstance(f, torch.Tensor) or f.device.type != "cuda":
+        raise TypeError("fft_amplitude: expected a CUDA tensor (there is no CPU path)")
+    if f.dim() != 3 or f.shape[0] != 9 or not f.is_contiguous():
+        raise ValueError("fft_amplitude: expected a contiguous (9, nx, ny) tensor")
+    code = storage_code(f, "fft_amplitude")
+    nx, ny = int(f.shape[1]), int(f.shape[2])
+    out = torch.empty((), dtype=torch.float64, device=f.device)
+    _lib.call("lbgb_row_fft_amplitude", f.data_ptr(), nx, ny, nx // 2 if row is None else int(row), code,
+              out.data_ptr(), stream_handle(f))
+    return out

@@ -233,3 +233,19 @@ def test_chapman_enskog_matches_oracle(cuda, boundary, nx, ny, post):
     ref1 = oracle.chapman_enskog(rho, ux, uy, 1.37, periodic=boundary == "periodic",
                                  u0=0.08 if boundary != "periodic" else 0.0, post_collision=True)
     assert np.abs(lat.populations(torch.float64).cpu().numpy() - ref1).max() < 1e-6
+
+
+@pytest.mark.parametrize("dt", ["f64", "f32"])
+@pytest.mark.parametrize("nx,ny", [(64, 64), (7, 50), (3, 1)])
+def test_fft_amplitude_matches_numpy(cuda, dt, nx, ny):
+    """The reference's decay diagnostic 2/ny max|fft(ux[nx/2, :])|
+    (shear_wave_decay.py:155-158) on the device, against numpy.fft."""
+    rng = np.random.default_rng(nx * ny)
+    l = np.arange(ny)
+    ux = 0.05 * np.sin(2 * np.pi * 3 * l / ny)[None, :] + 0.01 * rng.standard_normal((nx, ny))
+    f = oracle.equilibrium(1 + 0.01 * rng.standard_normal((nx, ny)), ux, 0.01 * rng.standard_normal((nx, ny)))
+    f = f.astype(np.float64 if dt == "f64" else np.float32)
+    _, u, _ = oracle.macroscopic(f.astype(np.float64))
+    ref = np.max(2 / ny * np.abs(np.fft.fft(u[nx // 2, :])))
+    got = float(PyLB.fft_amplitude(T(f, cuda)))
+    assert abs(got - ref) <= (1e-12 if dt == "f64" else 1e-6) * max(ref, 1e-3), (got, ref)
