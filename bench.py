@@ -47,7 +47,7 @@ def parse(argv=None):
     p.add_argument("--impl", choices=["ours", "reference"], default="ours")
     p.add_argument("--nx", type=int, default=8192)
     p.add_argument("--ny", type=int, default=8192)
-    p.add_argument("--storage", choices=["f32", "f16dev", "bf16dev", "f64"], default="f32")
+    p.add_argument("--storage", choices=["f32", "f16dev", "bf16dev", "f64", "f32dev"], default="f32")
     p.add_argument("--boundary", choices=["cavity", "periodic"], default="cavity")
     p.add_argument("--omega", type=float, default=1.7)
     p.add_argument("--u0", type=float, default=0.1)

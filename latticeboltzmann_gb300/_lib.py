@@ -12,13 +12,13 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "liblbgb.so")
 
 # storage codes
-F32, F64, F16DEV, BF16DEV = 0, 1, 2, 3
+F32, F64, F16DEV, BF16DEV, F32DEV = 0, 1, 2, 3, 4
 # boundary codes
 PERIODIC, CAVITY, CAVITY_LADD = 0, 1, 2
 # return codes
 OK, EINVAL, EDTYPE, ECUDA, EWORKSPACE, ETIMEOUT = 0, -1, -2, -3, -4, -5
 
-STORAGE_CODES = {"f32": F32, "f64": F64, "f16dev": F16DEV, "bf16dev": BF16DEV}
+STORAGE_CODES = {"f32": F32, "f64": F64, "f16dev": F16DEV, "bf16dev": BF16DEV, "f32dev": F32DEV}
 BOUNDARY_CODES = {"periodic": PERIODIC, "cavity": CAVITY, "cavity-ladd": CAVITY_LADD}
 
 

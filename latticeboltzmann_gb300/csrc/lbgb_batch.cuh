@@ -92,7 +92,7 @@ __device__ __forceinline__ void pull_cell(const typename C::raw *__restrict__ sr
         auto g = [&](int ch, int row, int col) { return C::dec(ld1(src + ch * n + (long long)row * ny + col), ch); };
         const real gN = g(CN, k, T), gNW = g(CNW, k, T), gNE = g(CNE, k, T);
         const real rho_lid = gNW + gN + gNE + g(CNW, ke, T - 1) + g(CN, k, T - 1) + g(CNE, kw, T - 1) + g(CW, ke, T) +
-                             g(C0, k, T) + g(CE, kw, T);
+                             g(C0, k, T) + g(CE, kw, T) + (C::DEV ? real(1) : real(0));
         const real lid = (real(6) * real(1.0 / 36.0)) * rho_lid * u0;
         if (k != 0) v[CSE] = gNW + lid;
         if (k != nx - 1) v[CSW] = gNE - lid;
@@ -152,9 +152,7 @@ k_batch_shear_amplitude(const typename Codec<DT>::raw *__restrict__ f, long long
             typename C::real v[9];
 #pragma unroll
             for (int i = 0; i < 9; ++i) v[i] = C::dec(g[i * n + c], i);
-            typename C::real rho = v[0];
-#pragma unroll
-            for (int i = 1; i < 9; ++i) rho += v[i];
+            const typename C::real rho = node_density<DT>(v);
             const double ux = (double)((v[1] - v[3] + v[5] - v[6] - v[7] + v[8]) / rho);
             const int l = (int)(c % in.ny);
             acc += ux * (double)sinpif(two_over_ny * (float)l);
@@ -193,9 +191,7 @@ k_batch_velocity_change(const typename Codec<DT>::raw *__restrict__ f, long long
             typename C::real v[9];
 #pragma unroll
             for (int i = 0; i < 9; ++i) v[i] = C::dec(g[i * n + c], i);
-            typename C::real rho = v[0];
-#pragma unroll
-            for (int i = 1; i < 9; ++i) rho += v[i];
+            const typename C::real rho = node_density<DT>(v);
             const float ux = (float)((v[1] - v[3] + v[5] - v[6] - v[7] + v[8]) / rho);
             const float uy = (float)((v[2] - v[4] + v[5] + v[6] - v[7] - v[8]) / rho);
             float d = fmaxf(fabsf(ux - up[2 * c]), fabsf(uy - up[2 * c + 1]));
@@ -283,6 +279,7 @@ extern "C" int lbgb_batch_step(const void *src, void *dst, long long total_elems
         LBGB_BATCH_CASE(LBGB_F64)
         LBGB_BATCH_CASE(LBGB_F16DEV)
         LBGB_BATCH_CASE(LBGB_BF16DEV)
+        LBGB_BATCH_CASE(LBGB_F32DEV)
     }
 #undef LBGB_BATCH_CASE
     return LBGB_EDTYPE;
@@ -317,6 +314,10 @@ extern "C" int lbgb_batch_shear_amplitude(const void *f, long long total_elems, 
     case LBGB_BF16DEV:
         k_batch_shear_amplitude<LBGB_BF16DEV><<<n_instances, 256, 0, s>>>((const unsigned short *)f, total_elems,
                                                                           in, n_instances, out_dev);
+        break;
+    case LBGB_F32DEV:
+        k_batch_shear_amplitude<LBGB_F32DEV><<<n_instances, 256, 0, s>>>((const float *)f, total_elems, in,
+                                                                         n_instances, out_dev);
         break;
     default: set_error("lbgb_batch_shear_amplitude: unsupported storage code %d", dtype); return LBGB_EDTYPE;
     }
@@ -354,6 +355,10 @@ extern "C" int lbgb_batch_velocity_change(const void *f, long long total_elems, 
         k_batch_velocity_change<LBGB_BF16DEV><<<n_instances, 256, 0, s>>>((const unsigned short *)f, total_elems,
                                                                           in, n_instances, u_prev, total_cells,
                                                                           out_dev);
+        break;
+    case LBGB_F32DEV:
+        k_batch_velocity_change<LBGB_F32DEV><<<n_instances, 256, 0, s>>>((const float *)f, total_elems, in,
+                                                                         n_instances, u_prev, total_cells, out_dev);
         break;
     default: set_error("lbgb_batch_velocity_change: unsupported storage code %d", dtype); return LBGB_EDTYPE;
     }

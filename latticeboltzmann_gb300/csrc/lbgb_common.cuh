@@ -37,17 +37,34 @@ __host__ __device__ constexpr R wgt(int i) {
 // store h_i = f_i - w_i as 16-bit bits (IEEE half or bfloat16).
 template <int DT> struct Codec;
 
+// DEV: the kernels' values are deviations h_i = f_i - w_i (LBGB_F32DEV) rather
+// than populations; decd/encd convert to and from the population in FP64.
 template <> struct Codec<LBGB_F32> {
     using raw = float;
     using real = float;
+    static constexpr bool DEV = false;
     static __device__ __forceinline__ real dec(raw x, int) { return x; }
     static __device__ __forceinline__ raw enc(real x, int) { return x; }
+    static __device__ __forceinline__ double decd(raw x, int) { return x; }
+    static __device__ __forceinline__ raw encd(double f, int) { return (raw)f; }
 };
 template <> struct Codec<LBGB_F64> {
     using raw = double;
     using real = double;
+    static constexpr bool DEV = false;
     static __device__ __forceinline__ real dec(raw x, int) { return x; }
     static __device__ __forceinline__ raw enc(real x, int) { return x; }
+    static __device__ __forceinline__ double decd(raw x, int) { return x; }
+    static __device__ __forceinline__ raw encd(double f, int) { return f; }
+};
+template <> struct Codec<LBGB_F32DEV> {
+    using raw = float;
+    using real = float;
+    static constexpr bool DEV = true;
+    static __device__ __forceinline__ real dec(raw x, int) { return x; }
+    static __device__ __forceinline__ raw enc(real x, int) { return x; }
+    static __device__ __forceinline__ double decd(raw x, int i) { return (double)x + wgt<double>(i); }
+    static __device__ __forceinline__ raw encd(double f, int i) { return (raw)(f - wgt<double>(i)); }
 };
 // Half deviations are stored scaled by 2^14: deviations down to ~4e-9 stay
 // in half's normal range (full 11-bit precision instead of the coarse
@@ -59,21 +76,38 @@ constexpr float F16_UNSCALE = 1.0f / 16384.0f;
 template <> struct Codec<LBGB_F16DEV> {
     using raw = unsigned short;
     using real = float;
+    static constexpr bool DEV = false;
     static __device__ __forceinline__ real dec_h(raw x) { return __half2float(__ushort_as_half(x)) * F16_UNSCALE; }
     static __device__ __forceinline__ raw enc_h(real h) { return __half_as_ushort(__float2half_rn(h * F16_SCALE)); }
     static __device__ __forceinline__ real dec(raw x, int i) {
         return fmaf(__half2float(__ushort_as_half(x)), F16_UNSCALE, wgt<float>(i));
     }
     static __device__ __forceinline__ raw enc(real x, int i) { return enc_h(x - wgt<float>(i)); }
+    static __device__ __forceinline__ double decd(raw x, int i) { return (double)dec(x, i); }
+    static __device__ __forceinline__ raw encd(double f, int i) { return enc((real)f, i); }
 };
 template <> struct Codec<LBGB_BF16DEV> {
     using raw = unsigned short;
     using real = float;
+    static constexpr bool DEV = false;
     static __device__ __forceinline__ real dec_h(raw x) { return __bfloat162float(__ushort_as_bfloat16(x)); }
     static __device__ __forceinline__ raw enc_h(real h) { return __bfloat16_as_ushort(__float2bfloat16_rn(h)); }
     static __device__ __forceinline__ real dec(raw x, int i) { return dec_h(x) + wgt<float>(i); }
     static __device__ __forceinline__ raw enc(real x, int i) { return enc_h(x - wgt<float>(i)); }
+    static __device__ __forceinline__ double decd(raw x, int i) { return (double)dec(x, i); }
+    static __device__ __forceinline__ raw encd(double f, int i) { return enc((real)f, i); }
 };
+
+// Density of a node from its nine kernel values (populations, or deviations
+// for DEV codecs: 1 + sum h, the small numbers summed first).
+template <int DT>
+__device__ __forceinline__ typename Codec<DT>::real node_density(const typename Codec<DT>::real (&v)[9]) {
+    typename Codec<DT>::real r = v[0];
+#pragma unroll
+    for (int i = 1; i < 9; ++i) r += v[i];
+    if constexpr (Codec<DT>::DEV) r += typename Codec<DT>::real(1);
+    return r;
+}
 
 // ---------------------------------------------------------------- memory
 // A vector of V raw elements moved as one 2/4/8/16-byte access.
@@ -138,7 +172,7 @@ struct Packet {
     static __device__ __forceinline__ void dec(const vec &x, real w, real (&o)[N]) {
         uint32_t wd[WORDS];
         memcpy(wd, &x, BYTES);
-        if constexpr (DT == LBGB_F32) {
+        if constexpr (DT == LBGB_F32 || DT == LBGB_F32DEV) {
 #pragma unroll
             for (int q = 0; q < N; ++q) o[q] = __uint_as_float(wd[q]);
         } else if constexpr (DT == LBGB_F64) {
@@ -321,6 +355,46 @@ __device__ __forceinline__ float collide_f16_mass(float (&f)[9], float omega) {
     return d * F16_SCALE;
 }
 
+// BGK in deviation form, h_i = f_i - w_i (LBGB_F32DEV): every intermediate is
+// a small number, so FP32 rounds at ~1e-9 instead of ~3e-8.  With D = sum h,
+// rho = 1 + D, j = sum c_i h_i (the weights carry no momentum), u = j / rho:
+//   h_i^eq = w_i (D + rho (cu + cu^2/2 - uu))   (same polynomial as feq)
+//   h_i' = h_i + omega (h_i^eq - h_i),  and h_0' = D - sum_{i>0} h_i' so the
+// node keeps its mass exactly in exact arithmetic of the stored values.
+__device__ __forceinline__ void collide_dev(float (&h)[9], float omega) {
+    float d = h[0];
+#pragma unroll
+    for (int i = 1; i < 9; ++i) d += h[i];
+    const float rho = 1.f + d;
+    const float inv = recip(rho);
+    float ux = (h[1] - h[3] + h[5] - h[6] - h[7] + h[8]) * inv;
+    float uy = (h[2] - h[4] + h[5] + h[6] - h[7] - h[8]) * inv;
+    ux *= 3.f;
+    uy *= 3.f;
+    const float uu = (ux * ux + uy * uy) * (1.f / 6.f);
+    const float cu5 = ux + uy, cu6 = uy - ux;
+    const float hx = 0.5f * ux * ux, hy = 0.5f * uy * uy;
+    const float h5 = 0.5f * cu5 * cu5, h6 = 0.5f * cu6 * cu6;
+    float q[9];
+    q[0] = -uu;
+    q[1] = ux + hx - uu;
+    q[2] = uy + hy - uu;
+    q[3] = -ux + hx - uu;
+    q[4] = -uy + hy - uu;
+    q[5] = cu5 + h5 - uu;
+    q[6] = cu6 + h6 - uu;
+    q[7] = -cu5 + h5 - uu;
+    q[8] = -cu6 + h6 - uu;
+    float rest = d;
+#pragma unroll
+    for (int i = 1; i < 9; ++i) {
+        const float heq = wgt<float>(i) * fmaf(rho, q[i], d);
+        h[i] += omega * (heq - h[i]);
+        rest -= h[i];
+    }
+    h[0] = rest;
+}
+
 // Equilibrium of one node (same formulation as above).
 template <class R>
 __device__ __forceinline__ void equilibrium1(R rho, R ux, R uy, R (&feq)[9]) {
@@ -375,6 +449,10 @@ __device__ __forceinline__ void collide_encode(typename Codec<DT>::real (&f)[9],
         f[0] = pre[0] + d;
 #pragma unroll
         for (int i = 0; i < 9; ++i) out[i] = f[i];
+    } else if constexpr (DT == LBGB_F32DEV) {
+        collide_dev(f, omega);
+#pragma unroll
+        for (int i = 0; i < 9; ++i) out[i] = f[i];
     } else if constexpr (DT == LBGB_F16DEV) {
         // Scaled deviations h S = f S - w S (one FMA each); the rest population
         // takes the node's mass deviation minus what the other eight stored
@@ -423,7 +501,8 @@ inline bool aligned(const void *p, size_t a) { return (reinterpret_cast<uintptr_
 
 inline size_t raw_size(int dt) {
     switch (dt) {
-    case LBGB_F32: return 4;
+    case LBGB_F32:
+    case LBGB_F32DEV: return 4;
     case LBGB_F64: return 8;
     case LBGB_F16DEV:
     case LBGB_BF16DEV: return 2;

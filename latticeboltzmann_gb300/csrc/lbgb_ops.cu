@@ -166,9 +166,7 @@ __global__ void k_macroscopic(const typename Codec<DT>::raw *__restrict__ f, typ
         real v[9];
 #pragma unroll
         for (int i = 0; i < 9; ++i) v[i] = C::dec(f[i * cs + c], i);
-        real r = v[0];
-#pragma unroll
-        for (int i = 1; i < 9; ++i) r += v[i];
+        const real r = node_density<DT>(v);
         // same expressions as the reference's diagnostics (cavity_opt1.py:154-156)
         const real jx = v[1] - v[3] + v[5] - v[6] - v[7] + v[8];
         const real jy = v[2] - v[4] + v[5] + v[6] - v[7] - v[8];
@@ -194,7 +192,7 @@ __global__ void __launch_bounds__(256) k_row_fft_amplitude(const typename Codec<
         const int64_t c = (int64_t)row * ny + l;
         double v[9];
 #pragma unroll
-        for (int i = 0; i < 9; ++i) v[i] = (double)C::dec(f[i * cs + c], i);
+        for (int i = 0; i < 9; ++i) v[i] = C::decd(f[i * cs + c], i);
         double r = v[0];
 #pragma unroll
         for (int i = 1; i < 9; ++i) r += v[i];
@@ -231,8 +229,7 @@ __global__ void k_convert(const typename Codec<SD>::raw *__restrict__ src, int64
     for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < n; c += (int64_t)gridDim.x * blockDim.x) {
 #pragma unroll
         for (int i = 0; i < 9; ++i) {
-            const double x = (double)Codec<SD>::dec(src[i * ss + c], i);
-            dst[i * ds + c] = Codec<DD>::enc((typename Codec<DD>::real)x, i);
+            dst[i * ds + c] = Codec<DD>::encd(Codec<SD>::decd(src[i * ss + c], i), i);
         }
     }
 }
@@ -250,6 +247,7 @@ static int launch_convert_to(const void *src, int64_t ss, void *dst, int dd, int
     case LBGB_BF16DEV:
         k_convert<SD, LBGB_BF16DEV><<<g, 256, 0, s>>>(a, ss, static_cast<unsigned short *>(dst), ds, n);
         break;
+    case LBGB_F32DEV: k_convert<SD, LBGB_F32DEV><<<g, 256, 0, s>>>(a, ss, static_cast<float *>(dst), ds, n); break;
     default: set_error("lbgb_convert: unsupported destination storage code %d", dd); return LBGB_EDTYPE;
     }
     return check_launch("k_convert");
@@ -270,7 +268,7 @@ k_mass_momentum_partial(const typename Codec<DT>::raw *__restrict__ f, int64_t n
     for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < n; c += (int64_t)gridDim.x * blockDim.x) {
         double v[9];
 #pragma unroll
-        for (int i = 0; i < 9; ++i) v[i] = (double)C::dec(f[i * cs + c], i);
+        for (int i = 0; i < 9; ++i) v[i] = C::decd(f[i * cs + c], i);
         double r = v[0];
 #pragma unroll
         for (int i = 1; i < 9; ++i) r += v[i];
@@ -421,6 +419,7 @@ extern "C" int lbgb_row_fft_amplitude(const void *f, int nx, int ny, int row, in
     case LBGB_BF16DEV:
         k_row_fft_amplitude<LBGB_BF16DEV><<<1, 256, 0, s>>>((const unsigned short *)f, nx, ny, row, out_dev);
         break;
+    case LBGB_F32DEV: k_row_fft_amplitude<LBGB_F32DEV><<<1, 256, 0, s>>>((const float *)f, nx, ny, row, out_dev); break;
     default: set_error("lbgb_row_fft_amplitude: unsupported storage code %d", dtype); return LBGB_EDTYPE;
     }
     return check_launch("k_row_fft_amplitude");
@@ -436,6 +435,7 @@ extern "C" int lbgb_collide(void *f, int64_t n, int64_t chan_stride, int dtype, 
     case LBGB_F64: return launch_collide<LBGB_F64>(f, n, chan_stride, omega, s);
     case LBGB_F16DEV: return launch_collide<LBGB_F16DEV>(f, n, chan_stride, omega, s);
     case LBGB_BF16DEV: return launch_collide<LBGB_BF16DEV>(f, n, chan_stride, omega, s);
+    case LBGB_F32DEV: return launch_collide<LBGB_F32DEV>(f, n, chan_stride, omega, s);
     }
     return LBGB_EDTYPE;
 }
@@ -463,6 +463,10 @@ extern "C" int lbgb_macroscopic(const void *f, void *rho, void *ux, void *uy, in
     case LBGB_BF16DEV:
         k_macroscopic<LBGB_BF16DEV><<<g, 256, 0, s>>>((const unsigned short *)f, (float *)rho, (float *)ux,
                                                       (float *)uy, n, chan_stride);
+        break;
+    case LBGB_F32DEV:
+        k_macroscopic<LBGB_F32DEV><<<g, 256, 0, s>>>((const float *)f, (float *)rho, (float *)ux, (float *)uy, n,
+                                                     chan_stride);
         break;
     }
     return check_launch("k_macroscopic");
@@ -501,6 +505,10 @@ extern "C" int lbgb_mass_momentum(const void *f, int64_t n, int64_t chan_stride,
         k_mass_momentum_partial<LBGB_BF16DEV><<<RED_BLOCKS, RED_THREADS, 0, s>>>((const unsigned short *)f, n,
                                                                                  chan_stride, partial);
         break;
+    case LBGB_F32DEV:
+        k_mass_momentum_partial<LBGB_F32DEV><<<RED_BLOCKS, RED_THREADS, 0, s>>>((const float *)f, n, chan_stride,
+                                                                                partial);
+        break;
     }
     rc = check_launch("k_mass_momentum_partial");
     if (rc) return rc;
@@ -521,6 +529,7 @@ extern "C" int lbgb_convert(const void *src, int src_dtype, int64_t src_stride, 
     case LBGB_F64: return launch_convert_to<LBGB_F64>(src, src_stride, dst, dst_dtype, dst_stride, n, s);
     case LBGB_F16DEV: return launch_convert_to<LBGB_F16DEV>(src, src_stride, dst, dst_dtype, dst_stride, n, s);
     case LBGB_BF16DEV: return launch_convert_to<LBGB_BF16DEV>(src, src_stride, dst, dst_dtype, dst_stride, n, s);
+    case LBGB_F32DEV: return launch_convert_to<LBGB_F32DEV>(src, src_stride, dst, dst_dtype, dst_stride, n, s);
     }
     return LBGB_EDTYPE;
 }
@@ -611,6 +620,11 @@ extern "C" int lbgb_mass_momentum_noalloc(const void *f, int64_t n, int64_t chan
         k_mass_momentum_partial<LBGB_BF16DEV><<<nblocks, RED_THREADS, 0, s>>>((const unsigned short *)f, n,
                                                                               chan_stride, partial);
         break;
+    case LBGB_F32DEV:
+        k_mass_momentum_partial<LBGB_F32DEV><<<nblocks, RED_THREADS, 0, s>>>((const float *)f, n, chan_stride,
+                                                                             partial);
+        break;
+    default: set_error("lbgb_mass_momentum_noalloc: unsupported storage code %d", dtype); return LBGB_EDTYPE;
     }
     rc = check_launch("k_mass_momentum_partial (no-alloc)");
     if (rc) return rc;

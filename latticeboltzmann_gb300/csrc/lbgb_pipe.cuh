@@ -236,7 +236,7 @@ k_step_pipe(const typename Codec<DT>::raw *__restrict__ src, typename Codec<DT>:
                     const int ke = (k == nx - 1) ? 0 : k + 1;
                     const real gN = g(CN, k, T), gNW = g(CNW, k, T), gNE = g(CNE, k, T);
                     const real rho_lid = gNW + gN + gNE + g(CNW, ke, T - 1) + g(CN, k, T - 1) + g(CNE, kw, T - 1) +
-                                         g(CW, ke, T) + g(C0, k, T) + g(CE, kw, T);
+                                         g(CW, ke, T) + g(C0, k, T) + g(CE, kw, T) + (C::DEV ? real(1) : real(0));
                     const real lid = (real(6) * real(1.0 / 36.0)) * rho_lid * u0;
                     v[CS][NC - 1] = gN;
                     v[CSE][NC - 1] = (k == 0) ? gNW : gNW + lid;

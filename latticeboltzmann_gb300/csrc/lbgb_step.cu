@@ -168,7 +168,7 @@ __device__ __forceinline__ void step_segment(const typename Codec<DT>::raw *__re
                                      load_one<C>(src, cs, ny, CN, k, T - 1) +
                                      load_one<C>(src, cs, ny, CNE, kw, T - 1) +
                                      load_one<C>(src, cs, ny, CW, ke, T) + load_one<C>(src, cs, ny, C0, k, T) +
-                                     load_one<C>(src, cs, ny, CE, kw, T);
+                                     load_one<C>(src, cs, ny, CE, kw, T) + (C::DEV ? real(1) : real(0));
                 const real lid = (real(6) * real(1.0 / 36.0)) * rho_lid * u0;
                 v[CS][V - 1] = gN;
                 v[CSE][V - 1] = (k == 0) ? gNW : gNW + lid;
@@ -347,6 +347,7 @@ static int dispatch(const void *src, void *dst, int nx, int ny, int dtype, doubl
     case LBGB_F64: return launch<LBGB_F64, BC, COLLIDE>(src, dst, nx, ny, omega, u0, s);
     case LBGB_F16DEV: return launch<LBGB_F16DEV, BC, COLLIDE>(src, dst, nx, ny, omega, u0, s, sr);
     case LBGB_BF16DEV: return launch<LBGB_BF16DEV, BC, COLLIDE>(src, dst, nx, ny, omega, u0, s, sr);
+    case LBGB_F32DEV: return launch<LBGB_F32DEV, BC, COLLIDE>(src, dst, nx, ny, omega, u0, s);
     default: set_error("unsupported storage code %d", dtype); return LBGB_EDTYPE;
     }
 }

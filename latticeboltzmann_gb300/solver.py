@@ -18,8 +18,10 @@ import torch
 from . import _lib
 from ._tensor import require_cuda
 
-_RAW = {"f32": torch.float32, "f64": torch.float64, "f16dev": torch.int16, "bf16dev": torch.int16}
-_REAL = {"f32": torch.float32, "f64": torch.float64, "f16dev": torch.float32, "bf16dev": torch.float32}
+_RAW = {"f32": torch.float32, "f64": torch.float64, "f16dev": torch.int16, "bf16dev": torch.int16,
+        "f32dev": torch.float32}
+_REAL = {"f32": torch.float32, "f64": torch.float64, "f16dev": torch.float32, "bf16dev": torch.float32,
+         "f32dev": torch.float32}
 
 
 def omega_from_reynolds(re, lid_velocity, length):
@@ -53,7 +55,7 @@ class Lattice:
         steady state.
     u0 : float
         Lid velocity (cavity only).
-    storage : {"f32", "f64", "f16dev", "bf16dev"}
+    storage : {"f32", "f64", "f16dev", "bf16dev", "f32dev"}
     device : torch device (CUDA).
     rounding : {"nearest", "stochastic"}
         How 16-bit storage rounds (FP32/FP64 ignore it).  Stochastic rounding

@@ -38,7 +38,7 @@ def test_batch_cavity_and_storages_against_single_lattice(cuda, boundary):
     """A batch of cavities equals the same cavities run one by one (same kernel code)."""
     import latticeboltzmann_gb300 as PyLB
     sizes = [(24, 16), (33, 40), (8, 64)]
-    for storage in ("f32", "f16dev", "bf16dev"):
+    for storage in ("f32", "f16dev", "bf16dev", "f32dev"):
         bl = B.BatchedLattice(sizes, [1.3, 1.6, 0.8], boundary=boundary, u0=0.1, storage=storage, device=cuda)
         bl.equilibrium(lambda b: (1.0, 0.0, 0.0))
         flat = B.BatchedLattice(sizes, [1.3, 1.6, 0.8], boundary=boundary, u0=0.1, storage=storage, device=cuda)

@@ -46,7 +46,7 @@ def run_with(kernel, storage, boundary, f0, steps, cuda):
     return lat
 
 
-@pytest.mark.parametrize("storage", ["f32", "f64", "f16dev", "bf16dev"])
+@pytest.mark.parametrize("storage", ["f32", "f64", "f16dev", "bf16dev", "f32dev"])
 @pytest.mark.parametrize("boundary", ["cavity", "cavity-ladd", "periodic"])
 @pytest.mark.parametrize("nx,ny", SIZES)
 def test_pipelined_equals_register_kernel(tuning, cuda, storage, boundary, nx, ny):
