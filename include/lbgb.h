@@ -217,6 +217,25 @@ LBGB_API int lbgb_batch_velocity_change(const void *f, long long total_elems,
 LBGB_API int lbgb_row_fft_amplitude(const void *f, int nx, int ny, int row, int dtype, double *out_dev,
                                     void *stream);
 
+/* Channel flows with dry wall rows (the simple-flow scripts' convention): the
+ * rows y = 0 and y = ny-1 of the (9, nx, ny) array f are walls.  After a push
+ * stream, the populations that entered a wall row are reflected into the
+ * adjacent fluid row, in place; the top wall moves with uw (SW and SE get
+ * -uw/6 and +uw/6).  interior != 0 treats columns 1 .. nx-2 only (the ghost
+ * columns of a pressure-periodic channel), clear != 0 zeroes the reflected
+ * wall entries afterwards.  dtype LBGB_F32 or LBGB_F64.
+ * Replaces: simulators/simple_flows/PoiseuilleFlow.py:59-75 (interior) and
+ *           simulators/simple_flows/CouetteFlow.py:106-119 (every column, clear). */
+LBGB_API int lbgb_wall_bounce_back(void *f, int nx, int ny, double uw, int interior, int clear, int dtype,
+                                   void *stream);
+
+/* Pressure-periodic inlet/outlet ghost columns, in place: column 0 becomes
+ * f^eq(rho_in, u of column nx-2) + (f - f^eq) of column nx-2, column nx-1
+ * becomes f^eq(rho_out, u of column 1) + (f - f^eq) of column 1.
+ * Replaces: simulators/simple_flows/PoiseuilleFlow.py:76-88. */
+LBGB_API int lbgb_pressure_periodic(void *f, int nx, int ny, double rho_in, double rho_out, int dtype,
+                                    void *stream);
+
 /* Start populations for a known flow: equilibrium plus the first-order
  * Chapman-Enskog non-equilibrium part,
  *   f_i = f_i^eq(rho, u) - (3 w_i rho / omega) (c_ia c_ib - delta_ab / 3) d_a u_b,

@@ -149,14 +149,15 @@ class BatchedLattice:
         return self._init(fields, True)
 
     def _init(self, fields, ce):
-        real = torch.float64 if self.storage == "f64" else torch.float32
-        code = _lib.F64 if self.storage == "f64" else _lib.F32
+        # FP64 fields for f64 and for FP32 deviations (see Lattice._fill_real)
+        real = torch.float64 if self.storage in ("f64", "f32dev") else torch.float32
+        code = _lib.F64 if real == torch.float64 else _lib.F32
         for b, (nx, ny) in enumerate(self.sizes):
             rho, ux, uy = (torch.as_tensor(x, dtype=real, device=self.device).expand(nx, ny).contiguous()
                            for x in fields(b))
             n = nx * ny
             direct = self.storage in ("f32", "f64")
-            out = self._slice(b) if direct else torch.empty(9 * n, dtype=torch.float32, device=self.device)
+            out = self._slice(b) if direct else torch.empty(9 * n, dtype=real, device=self.device)
             if ce:
                 _lib.call("lbgb_chapman_enskog", rho.data_ptr(), ux.data_ptr(), uy.data_ptr(), out.data_ptr(), nx, ny,
                           float(self.omegas[b]), float(self.u0s[b]), self.bcode, 1, code, self._stream())
@@ -164,7 +165,7 @@ class BatchedLattice:
                 _lib.call("lbgb_equilibrium", rho.data_ptr(), ux.data_ptr(), uy.data_ptr(), out.data_ptr(), n, n,
                           code, self._stream())
             if not direct:
-                _lib.call("lbgb_convert", out.data_ptr(), _lib.F32, n, self._slice(b).data_ptr(), self.code, n, n,
+                _lib.call("lbgb_convert", out.data_ptr(), code, n, self._slice(b).data_ptr(), self.code, n, n,
                           self._stream())
         return self
 

@@ -222,6 +222,64 @@ __global__ void __launch_bounds__(256) k_row_fft_amplitude(const typename Codec<
     if (threadIdx.x == 0) out[0] = 2.0 / ny * red[0];
 }
 
+// ---------------------------------------------------------------- channel walls
+// Dry wall rows y = 0 and y = ny-1 of the simple-flow scripts (convention B):
+// after a push stream, what entered a wall row is reflected into the adjacent
+// fluid row; the top wall moves with uw (SW, SE gain -uw/6, +uw/6).  One
+// thread per column, in the scripts' statement order (bottom, then top), so
+// ny = 2 and 3 give the same result as the sequential numpy code.
+template <class T>
+__global__ void k_wall_bounce_back(T *__restrict__ f, int nx, int ny, T uw6, int k0, int k1, int clear) {
+    const int64_t cs = (int64_t)nx * ny;
+    const int t = ny - 1;
+    for (int k = k0 + blockIdx.x * blockDim.x + threadIdx.x; k < k1; k += gridDim.x * blockDim.x) {
+        T *col = f + (int64_t)k * ny;
+        col[2 * cs + 1] = col[4 * cs];
+        col[5 * cs + 1] = col[7 * cs];
+        col[6 * cs + 1] = col[8 * cs];
+        if (clear) col[4 * cs] = col[7 * cs] = col[8 * cs] = T(0);
+        col[4 * cs + t - 1] = col[2 * cs + t];
+        col[7 * cs + t - 1] = col[5 * cs + t] - uw6;
+        col[8 * cs + t - 1] = col[6 * cs + t] + uw6;
+        if (clear) col[2 * cs + t] = col[5 * cs + t] = col[6 * cs + t] = T(0);
+    }
+}
+
+// Pressure-periodic ghost columns: x = 0 takes the equilibrium at rho_in with
+// the velocity of column nx-2 plus that column's non-equilibrium part; x =
+// nx-1 the same with rho_out and column 1.  One thread per row; every input
+// is read before either ghost is written.
+template <class T>
+__global__ void k_pressure_periodic(T *__restrict__ f, int nx, int ny, T rho_in, T rho_out) {
+    const int64_t cs = (int64_t)nx * ny;
+    for (int l = blockIdx.x * blockDim.x + threadIdx.x; l < ny; l += gridDim.x * blockDim.x) {
+        T a[9], b[9];
+#pragma unroll
+        for (int i = 0; i < 9; ++i) {
+            a[i] = f[i * cs + (int64_t)(nx - 2) * ny + l];
+            b[i] = f[i * cs + (int64_t)1 * ny + l];
+        }
+        T ra = a[0], rb = b[0];
+#pragma unroll
+        for (int i = 1; i < 9; ++i) {
+            ra += a[i];
+            rb += b[i];
+        }
+        const T uxa = (a[1] - a[3] + a[5] - a[6] - a[7] + a[8]) / ra, uya = (a[2] - a[4] + a[5] + a[6] - a[7] - a[8]) / ra;
+        const T uxb = (b[1] - b[3] + b[5] - b[6] - b[7] + b[8]) / rb, uyb = (b[2] - b[4] + b[5] + b[6] - b[7] - b[8]) / rb;
+        T ea[9], eb[9], ein[9], eout[9];
+        equilibrium1<T>(ra, uxa, uya, ea);
+        equilibrium1<T>(rb, uxb, uyb, eb);
+        equilibrium1<T>(rho_in, uxa, uya, ein);
+        equilibrium1<T>(rho_out, uxb, uyb, eout);
+#pragma unroll
+        for (int i = 0; i < 9; ++i) {
+            f[i * cs + l] = ein[i] + (a[i] - ea[i]);
+            f[i * cs + (int64_t)(nx - 1) * ny + l] = eout[i] + (b[i] - eb[i]);
+        }
+    }
+}
+
 // ---------------------------------------------------------------- convert
 template <int SD, int DD>
 __global__ void k_convert(const typename Codec<SD>::raw *__restrict__ src, int64_t ss,
@@ -423,6 +481,46 @@ extern "C" int lbgb_row_fft_amplitude(const void *f, int nx, int ny, int row, in
     default: set_error("lbgb_row_fft_amplitude: unsupported storage code %d", dtype); return LBGB_EDTYPE;
     }
     return check_launch("k_row_fft_amplitude");
+}
+
+extern "C" int lbgb_wall_bounce_back(void *f, int nx, int ny, double uw, int interior, int clear, int dtype,
+                                     void *stream) {
+    if (!f || nx <= 0 || ny < 2 || (interior && nx < 3)) {
+        set_error("lbgb_wall_bounce_back: need ny >= 2 (and nx >= 3 for interior columns), got %d x %d", nx, ny);
+        return LBGB_EINVAL;
+    }
+    const int k0 = interior ? 1 : 0, k1 = interior ? nx - 1 : nx;
+    const int g = (k1 - k0 + 255) / 256;
+    cudaStream_t s = (cudaStream_t)stream;
+    const double uw6 = 1.0 / 6.0 * uw;
+    if (dtype == LBGB_F32)
+        k_wall_bounce_back<float><<<g, 256, 0, s>>>((float *)f, nx, ny, (float)uw6, k0, k1, clear);
+    else if (dtype == LBGB_F64)
+        k_wall_bounce_back<double><<<g, 256, 0, s>>>((double *)f, nx, ny, uw6, k0, k1, clear);
+    else {
+        set_error("lbgb_wall_bounce_back: storage code %d not supported (F32 or F64)", dtype);
+        return LBGB_EDTYPE;
+    }
+    return check_launch("k_wall_bounce_back");
+}
+
+extern "C" int lbgb_pressure_periodic(void *f, int nx, int ny, double rho_in, double rho_out, int dtype,
+                                      void *stream) {
+    if (!f || nx < 2 || ny <= 0) {
+        set_error("lbgb_pressure_periodic: need nx >= 2 and ny >= 1, got %d x %d", nx, ny);
+        return LBGB_EINVAL;
+    }
+    const int g = (ny + 255) / 256;
+    cudaStream_t s = (cudaStream_t)stream;
+    if (dtype == LBGB_F32)
+        k_pressure_periodic<float><<<g, 256, 0, s>>>((float *)f, nx, ny, (float)rho_in, (float)rho_out);
+    else if (dtype == LBGB_F64)
+        k_pressure_periodic<double><<<g, 256, 0, s>>>((double *)f, nx, ny, rho_in, rho_out);
+    else {
+        set_error("lbgb_pressure_periodic: storage code %d not supported (F32 or F64)", dtype);
+        return LBGB_EDTYPE;
+    }
+    return check_launch("k_pressure_periodic");
 }
 
 extern "C" int lbgb_collide(void *f, int64_t n, int64_t chan_stride, int dtype, double omega, void *stream) {

@@ -130,16 +130,25 @@ class Lattice:
         if self.storage in ("f32", "f64") and f.dtype == self.state.dtype and f.is_contiguous():
             self.state.copy_(f, non_blocking=f.device.type == "cpu" and f.is_pinned())
             return self
-        src = f.to(device=self.device, dtype=_REAL[self.storage]).contiguous()
+        # FP32 deviations take a float64 input as it is (f - w in FP64, then rounded)
+        real = torch.float64 if self.storage == "f32dev" and f.dtype == torch.float64 else _REAL[self.storage]
+        src = f.to(device=self.device, dtype=real).contiguous()
         if self.storage in ("f32", "f64"):
             self.state.copy_(src)
         else:
-            _lib.call("lbgb_convert", src.data_ptr(), _lib.F32, self.cells, self.state.data_ptr(), self.code,
+            code = _lib.F64 if real == torch.float64 else _lib.F32
+            _lib.call("lbgb_convert", src.data_ptr(), code, self.cells, self.state.data_ptr(), self.code,
                       self.cells, self.cells, self._stream())
         return self
 
+    def _fill_real(self):
+        """Arithmetic type of the fields and start populations: FP64 for f64 and
+        for FP32 deviations (whose h = f - w must not inherit the rounding of
+        an FP32 population, e.g. w_i in FP32 at rest), FP32 otherwise."""
+        return torch.float64 if self.storage in ("f64", "f32dev") else torch.float32
+
     def _fields(self, rho, ux, uy):
-        real = torch.float64 if self.storage == "f64" else torch.float32
+        real = self._fill_real()
         shape = (self.nx, self.ny)
 
         def field(v, default):
@@ -151,14 +160,16 @@ class Lattice:
         return field(rho, 1.0), field(ux, 0.0), field(uy, 0.0)
 
     def _set_from(self, fill):
-        """Run ``fill(out_ptr, code)`` into the state (through FP32 for 16-bit storage)."""
-        code = _lib.F64 if self.storage == "f64" else _lib.F32
+        """Run ``fill(out_ptr, code)`` into the state (through an FP32 or FP64
+        temporary for the deviation storages)."""
+        real = self._fill_real()
+        code = _lib.F64 if real == torch.float64 else _lib.F32
         if self.storage in ("f32", "f64"):
             fill(self.state.data_ptr(), code)
         else:
-            tmp = torch.empty((9, self.nx, self.ny), dtype=torch.float32, device=self.device)
+            tmp = torch.empty((9, self.nx, self.ny), dtype=real, device=self.device)
             fill(tmp.data_ptr(), code)
-            _lib.call("lbgb_convert", tmp.data_ptr(), _lib.F32, self.cells, self.state.data_ptr(), self.code,
+            _lib.call("lbgb_convert", tmp.data_ptr(), code, self.cells, self.state.data_ptr(), self.code,
                       self.cells, self.cells, self._stream())
         return self
 
