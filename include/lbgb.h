@@ -196,7 +196,12 @@ LBGB_API int lbgb_batch_step(const void *src, void *dst, long long total_elems,
  * The decay diagnostic of shear_wave_opt1.py:174 / shear_wave_decay.py:155-158. */
 LBGB_API int lbgb_batch_shear_amplitude(const void *f, long long total_elems,
                                         const void *instances, int n_instances, int dtype,
-                                        double *out_dev, void *stream);
+                                        double *out_dev, double *partials, void *stream);
+
+/* Scratch of the per-instance diagnostics: partials holds n_instances *
+ * LBGB_DIAG_CHUNKS doubles (each instance's cells are reduced in this many
+ * chunks in parallel, then combined in chunk order: deterministic). */
+#define LBGB_DIAG_CHUNKS 64
 
 /* Steady-state monitor of a batch: out_dev[b] = max over the cells of
  * instance b of |u - u_prev| (x and y components, FP32), then u_prev <- u.
@@ -207,7 +212,7 @@ LBGB_API int lbgb_batch_shear_amplitude(const void *f, long long total_elems,
 LBGB_API int lbgb_batch_velocity_change(const void *f, long long total_elems,
                                         const void *instances, int n_instances, int dtype,
                                         float *u_prev, long long total_cells, float *out_dev,
-                                        void *stream);
+                                        double *partials, void *stream);
 
 /* Decay diagnostic of the shear-wave scripts: out_dev[0] = 2/ny * max_k
  * |DFT_k(ux[row, :])| (FP64; direct transform over the ny cells of one row,
@@ -274,7 +279,7 @@ LBGB_API int lbgb_gemm_status(int reset);
  *   to_bf16      y = bf16(x)
  *   bias_act     z += bias[c] (+ extra); v = act(z) (0 identity, 1 GELU), fp32 and/or bf16
  *   gelu_back    dz = dy * GELU'(z) (and its bf16 copy)
- *   row_sum      db[c] = sum_j dy[c, j]
+ *   row_sum      db[c] = sum_j dy[c, j] (partials: channels * 64 floats of scratch)
  *   mix          per Fourier mode y = sum_c x R (complex, BF16 weights), reading the
  *                transform products P (C, B, 2mk, 2q) and writing the BF16 operand
  *                Ym (O, B, 2q, 2mk) of the inverse transform (q kept ky, mk kept kx)
@@ -287,7 +292,8 @@ LBGB_API int lbgb_fno_bias_act(float *z, const float *bias, const float *extra, 
                                int channels, long long cols, int act, void *stream);
 LBGB_API int lbgb_fno_gelu_back(const float *dy, const float *z, float *dz, void *dzb, long long n,
                                 void *stream);
-LBGB_API int lbgb_fno_row_sum(const float *dy, float *db, int channels, long long cols, void *stream);
+LBGB_API int lbgb_fno_row_sum(const float *dy, float *db, float *partials, int channels, long long cols,
+                              void *stream);
 LBGB_API int lbgb_fno_mix(const float *P, const void *Rr, const void *Ri, void *Ym, int C, int O, int B,
                           int q, int mk, void *stream);
 LBGB_API int lbgb_fno_mix_back(const float *dYm, const float *P, const void *Rr, const void *Ri, void *dP,

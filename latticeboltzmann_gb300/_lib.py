@@ -56,8 +56,8 @@ SIGNATURES = {
     "lbgb_mass_momentum_noalloc": (_I, [_P, _I64, _I64, _I, _P, _P]),
     "lbgb_convert": (_I, [_P, _I, _I64, _P, _I, _I64, _I64, _P]),
     "lbgb_batch_step": (_I, [_P, _P, ctypes.c_longlong, _P, _I, _P, ctypes.c_longlong, _I, _I, _I, _I, _I, _I, _P]),
-    "lbgb_batch_shear_amplitude": (_I, [_P, ctypes.c_longlong, _P, _I, _I, _P, _P]),
-    "lbgb_batch_velocity_change": (_I, [_P, ctypes.c_longlong, _P, _I, _I, _P, ctypes.c_longlong, _P, _P]),
+    "lbgb_batch_shear_amplitude": (_I, [_P, ctypes.c_longlong, _P, _I, _I, _P, _P, _P]),
+    "lbgb_batch_velocity_change": (_I, [_P, ctypes.c_longlong, _P, _I, _I, _P, ctypes.c_longlong, _P, _P, _P]),
     "lbgb_row_fft_amplitude": (_I, [_P, _I, _I, _I, _I, _P, _P]),
     "lbgb_wall_bounce_back": (_I, [_P, _I, _I, ctypes.c_double, _I, _I, _I, _P]),
     "lbgb_pressure_periodic": (_I, [_P, _I, _I, ctypes.c_double, ctypes.c_double, _I, _P]),
@@ -69,7 +69,7 @@ SIGNATURES = {
     "lbgb_fno_to_bf16": (_I, [_P, _P, ctypes.c_longlong, _P]),
     "lbgb_fno_bias_act": (_I, [_P, _P, _P, _P, _P, _I, ctypes.c_longlong, _I, _P]),
     "lbgb_fno_gelu_back": (_I, [_P, _P, _P, _P, ctypes.c_longlong, _P]),
-    "lbgb_fno_row_sum": (_I, [_P, _P, _I, ctypes.c_longlong, _P]),
+    "lbgb_fno_row_sum": (_I, [_P, _P, _P, _I, ctypes.c_longlong, _P]),
     "lbgb_fno_mix": (_I, [_P, _P, _P, _P, _I, _I, _I, _I, _I, _P]),
     "lbgb_fno_mix_back": (_I, [_P, _P, _P, _P, _P, _P, _P, _I, _I, _I, _I, _I, _P]),
     "lbgb_fno_mse": (_I, [_P, _P, _P, _P, _I, ctypes.c_longlong, _P]),
@@ -84,6 +84,7 @@ SIGNATURES = {
 TUNE_KERNEL, TUNE_STAGES, TUNE_WAIT_LIMIT, TUNE_PIPE_MIN_CELLS, TUNE_TEST_STALL_PRODUCER = 0, 1, 2, 3, 4
 KERNELS = {"auto": 0, "register": 1, "pipelined": 2}
 NOALLOC_MAX_CELLS = 268435456
+DIAG_CHUNKS = 64  # LBGB_DIAG_CHUNKS: partials per instance of the batch diagnostics
 
 
 def load(path=LIB_PATH):

@@ -80,6 +80,7 @@ class BatchedLattice:
         self.config = {"flat": True, "vector": False, "rows": 2, "threads": 256, "blocks": n_sm * 8}
         self._tasks = {}
         self._amp = torch.empty(self.n, dtype=torch.float64, device=self.device)
+        self._partials = torch.empty(self.n * _lib.DIAG_CHUNKS, dtype=torch.float64, device=self.device)
         self.active = np.ones(self.n, dtype=bool)  # instances that still advance
         self._u_prev = None
 
@@ -277,7 +278,7 @@ class BatchedLattice:
         """Per-instance amplitude of the u_x ~ sin(2 pi l / ny) mode (float64 device tensor)."""
         out = self._amp if out is None else out
         _lib.call("lbgb_batch_shear_amplitude", self.state.data_ptr(), self.total, self._table(True).data_ptr(),
-                  self.n, self.code, out.data_ptr(), self._stream())
+                  self.n, self.code, out.data_ptr(), self._partials.data_ptr(), self._stream())
         return out
 
     def velocity_change(self):
@@ -288,7 +289,8 @@ class BatchedLattice:
         if first:
             self._u_prev = torch.zeros(2 * self.cells, dtype=torch.float32, device=self.device)
         _lib.call("lbgb_batch_velocity_change", self.state.data_ptr(), self.total, self._table(True).data_ptr(),
-                  self.n, self.code, self._u_prev.data_ptr(), self.cells, out.data_ptr(), self._stream())
+                  self.n, self.code, self._u_prev.data_ptr(), self.cells, out.data_ptr(), self._partials.data_ptr(),
+                  self._stream())
         if first:
             out.fill_(float("inf"))
         return out

@@ -132,14 +132,25 @@ k_batch_step_flat(const typename Codec<DT>::raw *__restrict__ src, typename Code
     }
 }
 
-// Per-instance amplitude of a sine mode of u_x along y:
-// a_b = 2/(nx*ny) * sum_{k,l} u_x(k,l) sin(2 pi l / ny)   (one block per instance).
+// Per-instance diagnostics run on a (LBGB_DIAG_CHUNKS, n_inst) grid: block
+// (c, b) covers chunk c of instance b's cells and writes one partial; a second
+// kernel combines the partials of each instance in chunk order, so results
+// do not depend on scheduling.  (One block per instance left the largest
+// lattice on a single SM.)
+__device__ __forceinline__ void chunk_range(long long n, int c, long long &c0, long long &c1) {
+    const long long len = (n + LBGB_DIAG_CHUNKS - 1) / LBGB_DIAG_CHUNKS;
+    c0 = (long long)c * len;
+    c1 = c0 + len < n ? c0 + len : n;
+}
+
+// Amplitude of a sine mode of u_x along y:
+// a_b = 2/(nx*ny) * sum_{k,l} u_x(k,l) sin(2 pi l / ny).
 template <int DT>
 __global__ void __launch_bounds__(256)
 k_batch_shear_amplitude(const typename Codec<DT>::raw *__restrict__ f, long long total_elems,
-                        const BatchInstanceDev *__restrict__ inst, int n_inst, double *__restrict__ out) {
+                        const BatchInstanceDev *__restrict__ inst, int n_inst, double *__restrict__ part) {
     using C = Codec<DT>;
-    const int b = blockIdx.x;
+    const int b = blockIdx.y, chunk = blockIdx.x;
     if (b >= n_inst) return;
     const BatchInstanceDev in = inst[b];
     const long long n = (long long)in.nx * in.ny;
@@ -148,7 +159,9 @@ k_batch_shear_amplitude(const typename Codec<DT>::raw *__restrict__ f, long long
     if (ok) {
         const typename C::raw *g = f + in.offset;
         const float two_over_ny = 2.0f / (float)in.ny;
-        for (long long c = threadIdx.x; c < n; c += blockDim.x) {
+        long long c0, c1;
+        chunk_range(n, chunk, c0, c1);
+        for (long long c = c0 + threadIdx.x; c < c1; c += blockDim.x) {
             typename C::real v[9];
 #pragma unroll
             for (int i = 0; i < 9; ++i) v[i] = C::dec(g[i * n + c], i);
@@ -165,19 +178,32 @@ k_batch_shear_amplitude(const typename Codec<DT>::raw *__restrict__ f, long long
         if (threadIdx.x < s) sm[threadIdx.x] += sm[threadIdx.x + s];
         __syncthreads();
     }
-    if (threadIdx.x == 0) out[b] = ok ? sm[0] * 2.0 / (double)n : 0.0;
+    if (threadIdx.x == 0) part[(long long)b * LBGB_DIAG_CHUNKS + chunk] = sm[0];
+}
+
+__global__ void k_batch_amplitude_finish(const BatchInstanceDev *__restrict__ inst, int n_inst,
+                                         const double *__restrict__ part, long long total_elems,
+                                         double *__restrict__ out) {
+    const int b = blockIdx.x * blockDim.x + threadIdx.x;
+    if (b >= n_inst) return;
+    const BatchInstanceDev in = inst[b];
+    const long long n = (long long)in.nx * in.ny;
+    const bool ok = in.nx > 0 && in.ny > 0 && in.offset >= 0 && in.offset + 9 * n <= total_elems;
+    double s = 0.0;
+    for (int c = 0; c < LBGB_DIAG_CHUNKS; ++c) s += part[(long long)b * LBGB_DIAG_CHUNKS + c];
+    out[b] = ok ? s * 2.0 / (double)n : 0.0;
 }
 
 // Steady-state monitor: per instance, max over cells of |u - u_prev| (both
 // components), then u_prev <- u.  u_prev holds 2 floats per cell, instances
-// back to back in cell_base order.  One block per instance.
+// back to back in cell_base order.
 template <int DT>
 __global__ void __launch_bounds__(256)
 k_batch_velocity_change(const typename Codec<DT>::raw *__restrict__ f, long long total_elems,
                         const BatchInstanceDev *__restrict__ inst, int n_inst, float *__restrict__ u_prev,
-                        long long total_cells, float *__restrict__ out) {
+                        long long total_cells, double *__restrict__ part) {
     using C = Codec<DT>;
-    const int b = blockIdx.x;
+    const int b = blockIdx.y, chunk = blockIdx.x;
     if (b >= n_inst) return;
     const BatchInstanceDev in = inst[b];
     const long long n = (long long)in.nx * in.ny;
@@ -187,7 +213,9 @@ k_batch_velocity_change(const typename Codec<DT>::raw *__restrict__ f, long long
     if (ok) {
         const typename C::raw *g = f + in.offset;
         float *up = u_prev + 2ll * in.cell_base;
-        for (long long c = threadIdx.x; c < n; c += blockDim.x) {
+        long long c0, c1;
+        chunk_range(n, chunk, c0, c1);
+        for (long long c = c0 + threadIdx.x; c < c1; c += blockDim.x) {
             typename C::real v[9];
 #pragma unroll
             for (int i = 0; i < 9; ++i) v[i] = C::dec(g[i * n + c], i);
@@ -209,8 +237,16 @@ k_batch_velocity_change(const typename Codec<DT>::raw *__restrict__ f, long long
     if (threadIdx.x == 0) {
         float r = 0.f;
         for (int w = 0; w < (int)(blockDim.x >> 5); ++w) r = fmaxf(r, sm[w]);
-        out[b] = ok ? r : -1.f;
+        part[(long long)b * LBGB_DIAG_CHUNKS + chunk] = ok ? r : -1.0;
     }
+}
+
+__global__ void k_batch_change_finish(int n_inst, const double *__restrict__ part, float *__restrict__ out) {
+    const int b = blockIdx.x * blockDim.x + threadIdx.x;
+    if (b >= n_inst) return;
+    double m = part[(long long)b * LBGB_DIAG_CHUNKS];
+    for (int c = 1; c < LBGB_DIAG_CHUNKS; ++c) m = fmax(m, part[(long long)b * LBGB_DIAG_CHUNKS + c]);
+    out[b] = (float)m;
 }
 
 template <int DT, int BC>
@@ -286,81 +322,91 @@ extern "C" int lbgb_batch_step(const void *src, void *dst, long long total_elems
 }
 
 extern "C" int lbgb_batch_shear_amplitude(const void *f, long long total_elems, const void *instances,
-                                          int n_instances, int dtype, double *out_dev, void *stream) {
+                                          int n_instances, int dtype, double *out_dev, double *partials,
+                                          void *stream) {
     using namespace lbgb;
-    if (!f || !instances || !out_dev || n_instances <= 0 || total_elems <= 0) {
-        set_error("lbgb_batch_shear_amplitude: null buffer or empty batch");
+    if (!f || !instances || !out_dev || !partials || n_instances <= 0 || n_instances > 65535 || total_elems <= 0) {
+        set_error("lbgb_batch_shear_amplitude: null buffer, empty batch or more than 65535 instances");
         return LBGB_EINVAL;
     }
-    if (!aligned(instances, 8)) {
-        set_error("lbgb_batch_shear_amplitude: instance table must be 8-byte aligned");
+    if (!aligned(instances, 8) || !aligned(partials, 8)) {
+        set_error("lbgb_batch_shear_amplitude: instance table and partials must be 8-byte aligned");
         return LBGB_EINVAL;
     }
     cudaStream_t s = (cudaStream_t)stream;
     const auto *in = static_cast<const BatchInstanceDev *>(instances);
+    const dim3 grid(LBGB_DIAG_CHUNKS, n_instances);
     switch (dtype) {
     case LBGB_F32:
-        k_batch_shear_amplitude<LBGB_F32><<<n_instances, 256, 0, s>>>((const float *)f, total_elems, in, n_instances,
-                                                                      out_dev);
+        k_batch_shear_amplitude<LBGB_F32><<<grid, 256, 0, s>>>((const float *)f, total_elems, in, n_instances,
+                                                               partials);
         break;
     case LBGB_F64:
-        k_batch_shear_amplitude<LBGB_F64><<<n_instances, 256, 0, s>>>((const double *)f, total_elems, in,
-                                                                      n_instances, out_dev);
+        k_batch_shear_amplitude<LBGB_F64><<<grid, 256, 0, s>>>((const double *)f, total_elems, in, n_instances,
+                                                               partials);
         break;
     case LBGB_F16DEV:
-        k_batch_shear_amplitude<LBGB_F16DEV><<<n_instances, 256, 0, s>>>((const unsigned short *)f, total_elems, in,
-                                                                         n_instances, out_dev);
+        k_batch_shear_amplitude<LBGB_F16DEV><<<grid, 256, 0, s>>>((const unsigned short *)f, total_elems, in,
+                                                                  n_instances, partials);
         break;
     case LBGB_BF16DEV:
-        k_batch_shear_amplitude<LBGB_BF16DEV><<<n_instances, 256, 0, s>>>((const unsigned short *)f, total_elems,
-                                                                          in, n_instances, out_dev);
+        k_batch_shear_amplitude<LBGB_BF16DEV><<<grid, 256, 0, s>>>((const unsigned short *)f, total_elems, in,
+                                                                   n_instances, partials);
         break;
     case LBGB_F32DEV:
-        k_batch_shear_amplitude<LBGB_F32DEV><<<n_instances, 256, 0, s>>>((const float *)f, total_elems, in,
-                                                                         n_instances, out_dev);
+        k_batch_shear_amplitude<LBGB_F32DEV><<<grid, 256, 0, s>>>((const float *)f, total_elems, in, n_instances,
+                                                                  partials);
         break;
     default: set_error("lbgb_batch_shear_amplitude: unsupported storage code %d", dtype); return LBGB_EDTYPE;
     }
-    return check_launch("k_batch_shear_amplitude");
+    int rc = check_launch("k_batch_shear_amplitude");
+    if (rc) return rc;
+    k_batch_amplitude_finish<<<(n_instances + 127) / 128, 128, 0, s>>>(in, n_instances, partials, total_elems,
+                                                                       out_dev);
+    return check_launch("k_batch_amplitude_finish");
 }
 
 extern "C" int lbgb_batch_velocity_change(const void *f, long long total_elems, const void *instances,
                                           int n_instances, int dtype, float *u_prev, long long total_cells,
-                                          float *out_dev, void *stream) {
+                                          float *out_dev, double *partials, void *stream) {
     using namespace lbgb;
-    if (!f || !instances || !u_prev || !out_dev || n_instances <= 0 || total_elems <= 0 || total_cells <= 0) {
-        set_error("lbgb_batch_velocity_change: null buffer or empty batch");
+    if (!f || !instances || !u_prev || !out_dev || !partials || n_instances <= 0 || n_instances > 65535 ||
+        total_elems <= 0 || total_cells <= 0) {
+        set_error("lbgb_batch_velocity_change: null buffer, empty batch or more than 65535 instances");
         return LBGB_EINVAL;
     }
-    if (!aligned(instances, 8) || !aligned(u_prev, 8)) {
-        set_error("lbgb_batch_velocity_change: instance table and u_prev must be 8-byte aligned");
+    if (!aligned(instances, 8) || !aligned(u_prev, 8) || !aligned(partials, 8)) {
+        set_error("lbgb_batch_velocity_change: instance table, u_prev and partials must be 8-byte aligned");
         return LBGB_EINVAL;
     }
     cudaStream_t s = (cudaStream_t)stream;
     const auto *in = static_cast<const BatchInstanceDev *>(instances);
+    const dim3 grid(LBGB_DIAG_CHUNKS, n_instances);
     switch (dtype) {
     case LBGB_F32:
-        k_batch_velocity_change<LBGB_F32><<<n_instances, 256, 0, s>>>((const float *)f, total_elems, in, n_instances,
-                                                                      u_prev, total_cells, out_dev);
+        k_batch_velocity_change<LBGB_F32><<<grid, 256, 0, s>>>((const float *)f, total_elems, in, n_instances, u_prev,
+                                                               total_cells, partials);
         break;
     case LBGB_F64:
-        k_batch_velocity_change<LBGB_F64><<<n_instances, 256, 0, s>>>((const double *)f, total_elems, in,
-                                                                      n_instances, u_prev, total_cells, out_dev);
+        k_batch_velocity_change<LBGB_F64><<<grid, 256, 0, s>>>((const double *)f, total_elems, in, n_instances,
+                                                               u_prev, total_cells, partials);
         break;
     case LBGB_F16DEV:
-        k_batch_velocity_change<LBGB_F16DEV><<<n_instances, 256, 0, s>>>((const unsigned short *)f, total_elems, in,
-                                                                         n_instances, u_prev, total_cells, out_dev);
+        k_batch_velocity_change<LBGB_F16DEV><<<grid, 256, 0, s>>>((const unsigned short *)f, total_elems, in,
+                                                                  n_instances, u_prev, total_cells, partials);
         break;
     case LBGB_BF16DEV:
-        k_batch_velocity_change<LBGB_BF16DEV><<<n_instances, 256, 0, s>>>((const unsigned short *)f, total_elems,
-                                                                          in, n_instances, u_prev, total_cells,
-                                                                          out_dev);
+        k_batch_velocity_change<LBGB_BF16DEV><<<grid, 256, 0, s>>>((const unsigned short *)f, total_elems, in,
+                                                                   n_instances, u_prev, total_cells, partials);
         break;
     case LBGB_F32DEV:
-        k_batch_velocity_change<LBGB_F32DEV><<<n_instances, 256, 0, s>>>((const float *)f, total_elems, in,
-                                                                         n_instances, u_prev, total_cells, out_dev);
+        k_batch_velocity_change<LBGB_F32DEV><<<grid, 256, 0, s>>>((const float *)f, total_elems, in, n_instances,
+                                                                  u_prev, total_cells, partials);
         break;
     default: set_error("lbgb_batch_velocity_change: unsupported storage code %d", dtype); return LBGB_EDTYPE;
     }
-    return check_launch("k_batch_velocity_change");
+    int rc = check_launch("k_batch_velocity_change");
+    if (rc) return rc;
+    k_batch_change_finish<<<(n_instances + 127) / 128, 128, 0, s>>>(n_instances, partials, out_dev);
+    return check_launch("k_batch_change_finish");
 }

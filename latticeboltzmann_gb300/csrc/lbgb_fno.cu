@@ -21,14 +21,16 @@ __global__ void k_to_bf16(const float *__restrict__ x, __nv_bfloat16 *__restrict
         y[i] = __float2bfloat16_rn(x[i]);
 }
 
-// z[c, j] += bias[c] (+ extra[c, j]); act: 0 identity, 1 GELU -> v (fp32 and bf16)
+// z[c, j] += bias[c] (+ extra[c, j]); act: 0 identity, 1 GELU -> v (fp32 and bf16).
+// Grid (column blocks, channel): no per-element index division.
 __global__ void k_bias_act(float *__restrict__ z, const float *__restrict__ bias, const float *__restrict__ extra,
-                           float *__restrict__ v, __nv_bfloat16 *__restrict__ vb, int channels, long long cols,
-                           int act) {
-    const long long n = (long long)channels * cols;
-    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
-        const int c = (int)(i / cols);
-        float x = z[i] + (bias ? bias[c] : 0.f) + (extra ? extra[i] : 0.f);
+                           float *__restrict__ v, __nv_bfloat16 *__restrict__ vb, long long cols, int act) {
+    const int c = blockIdx.y;
+    const float b = bias ? bias[c] : 0.f;
+    const long long base = (long long)c * cols;
+    for (long long j = blockIdx.x * (long long)blockDim.x + threadIdx.x; j < cols; j += (long long)gridDim.x * blockDim.x) {
+        const long long i = base + j;
+        float x = z[i] + b + (extra ? extra[i] : 0.f);
         z[i] = x;
         const float y = act ? gelu_f(x) : x;
         if (v) v[i] = y;
@@ -46,11 +48,17 @@ __global__ void k_gelu_back(const float *__restrict__ dy, const float *__restric
     }
 }
 
-// db[c] = sum_j dy[c, j]; one block per channel
-__global__ void __launch_bounds__(256) k_row_sum(const float *__restrict__ dy, float *__restrict__ db, long long cols) {
-    const int c = blockIdx.x;
+// db[c] = sum_j dy[c, j]: block (chunk, c) sums one of ROWSUM_CHUNKS slices
+// of row c into part[c][chunk]; k_row_sum_finish adds the slices in order
+// (deterministic, and every SM busy however few channels there are).
+constexpr int ROWSUM_CHUNKS = 64;
+
+__global__ void __launch_bounds__(256) k_row_sum(const float *__restrict__ dy, float *__restrict__ part, long long cols) {
+    const int c = blockIdx.y, chunk = blockIdx.x;
+    const long long len = (cols + ROWSUM_CHUNKS - 1) / ROWSUM_CHUNKS;
+    const long long j0 = chunk * len, j1 = j0 + len < cols ? j0 + len : cols;
     float acc = 0.f;
-    for (long long j = threadIdx.x; j < cols; j += blockDim.x) acc += dy[c * cols + j];
+    for (long long j = j0 + threadIdx.x; j < j1; j += blockDim.x) acc += dy[c * cols + j];
     __shared__ float sm[256];
     sm[threadIdx.x] = acc;
     __syncthreads();
@@ -58,7 +66,15 @@ __global__ void __launch_bounds__(256) k_row_sum(const float *__restrict__ dy, f
         if (threadIdx.x < s) sm[threadIdx.x] += sm[threadIdx.x + s];
         __syncthreads();
     }
-    if (threadIdx.x == 0) db[c] = sm[0];
+    if (threadIdx.x == 0) part[c * ROWSUM_CHUNKS + chunk] = sm[0];
+}
+
+__global__ void k_row_sum_finish(const float *__restrict__ part, float *__restrict__ db, int channels) {
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= channels) return;
+    float s = 0.f;
+    for (int k = 0; k < ROWSUM_CHUNKS; ++k) s += part[c * ROWSUM_CHUNKS + k];
+    db[c] = s;
 }
 
 // Complex mixing per Fourier mode, on the layouts of the factorised DFT GEMMs
@@ -227,8 +243,15 @@ extern "C" int lbgb_fno_bias_act(float *z, const float *bias, const float *extra
                                  long long cols, int act, void *stream) {
     const long long n = (long long)channels * cols;
     if (n <= 0) return LBGB_OK;
-    k_bias_act<<<blocks_for(n), 256, 0, (cudaStream_t)stream>>>(z, bias, extra, v, static_cast<__nv_bfloat16 *>(vb),
-                                                                channels, cols, act);
+    if (channels > 65535) {
+        set_error("lbgb_fno_bias_act: at most 65535 channels");
+        return LBGB_EINVAL;
+    }
+    long long per = (cols + 255) / 256;
+    const long long cap = (8192 + channels - 1) / channels;  // ~8192 blocks in all
+    const int gx = (int)(per < cap ? (per < 1 ? 1 : per) : cap);
+    k_bias_act<<<dim3(gx, channels), 256, 0, (cudaStream_t)stream>>>(z, bias, extra, v, static_cast<__nv_bfloat16 *>(vb),
+                                                                     cols, act);
     return check_launch("k_bias_act");
 }
 
@@ -238,10 +261,18 @@ extern "C" int lbgb_fno_gelu_back(const float *dy, const float *z, float *dz, vo
     return check_launch("k_gelu_back");
 }
 
-extern "C" int lbgb_fno_row_sum(const float *dy, float *db, int channels, long long cols, void *stream) {
-    if (channels <= 0) return LBGB_OK;
-    k_row_sum<<<channels, 256, 0, (cudaStream_t)stream>>>(dy, db, cols);
-    return check_launch("k_row_sum");
+extern "C" int lbgb_fno_row_sum(const float *dy, float *db, float *partials, int channels, long long cols,
+                                void *stream) {
+    if (channels <= 0 || channels > 65535) {
+        set_error("lbgb_fno_row_sum: 1 <= channels <= 65535");
+        return LBGB_EINVAL;
+    }
+    cudaStream_t s = (cudaStream_t)stream;
+    k_row_sum<<<dim3(ROWSUM_CHUNKS, channels), 256, 0, s>>>(dy, partials, cols);
+    int rc = check_launch("k_row_sum");
+    if (rc) return rc;
+    k_row_sum_finish<<<(channels + 127) / 128, 128, 0, s>>>(partials, db, channels);
+    return check_launch("k_row_sum_finish");
 }
 
 extern "C" int lbgb_fno_mix(const float *P, const void *Rr, const void *Ri, void *Ym, int C, int O, int B, int q,

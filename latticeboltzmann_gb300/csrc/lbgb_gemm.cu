@@ -79,8 +79,34 @@ constexpr long long TC_WAIT = 1ll << 22;
 // aligned, consecutive rows per warp when the rows are contiguous.
 template <int ROWS>
 __device__ __forceinline__ void load_tile(unsigned char *dst, const __nv_bfloat16 *__restrict__ X, long long rs,
-                                          long long ks, int r0, int R, int k0, int K, int tid) {
+                                          long long ks, int r0, int R, int k0, int K, int tid,
+                                          unsigned short *stage) {
     const bool row_contig = rs == 1 && ks != 1;
+    if (row_contig && (ks & 7) == 0 && r0 + ROWS <= R && (reinterpret_cast<uintptr_t>(X) & 15) == 0) {
+        // rows contiguous (an M- or N-major operand): 16-byte loads of 8 rows
+        // at one k into a [k][row] staging tile, then each thread gathers the
+        // 8 k values of one row into a 16-byte core-matrix row
+        constexpr int G = ROWS / 8;
+        for (int e = tid; e < TC_K * G; e += 128) {
+            const int kk = e / G, g = e - kk * G;
+            const int gk = k0 + kk;
+            uint4 w = make_uint4(0u, 0u, 0u, 0u);
+            if (gk < K) w = __ldg(reinterpret_cast<const uint4 *>(X + (long long)(r0 + 8 * g) + (long long)gk * ks));
+            *reinterpret_cast<uint4 *>(stage + kk * ROWS + 8 * g) = w;
+        }
+        __syncthreads();
+        for (int e = tid; e < ROWS * (TC_K / 8); e += 128) {
+            const int r = e % ROWS, kc = e / ROWS;
+            unsigned short h[8];
+#pragma unroll
+            for (int q = 0; q < 8; ++q) h[q] = stage[(kc * 8 + q) * ROWS + r];
+            uint4 w;
+            memcpy(&w, h, 16);
+            *reinterpret_cast<uint4 *>(dst + (r >> 3) * 1024 + kc * 128 + (r & 7) * 16) = w;
+        }
+        __syncthreads();  // the staging tile is reused by the next operand
+        return;
+    }
     const bool vec = ks == 1 && (rs & 7) == 0 && ((reinterpret_cast<uintptr_t>(X) & 15) == 0);
     for (int e = tid; e < ROWS * TC_K / 8; e += 128) {
         int r, kc;
@@ -119,6 +145,8 @@ k_gemm_tc(int M, int N, int K, const __nv_bfloat16 *__restrict__ A, long long a_
     __shared__ __align__(1024) unsigned char sB[(NT < 64 ? 64 : NT) * TC_K * 2];
     __shared__ __align__(8) uint64_t bar;
     __shared__ uint32_t tmem_slot;
+    // dynamic shared memory: the [k][row] staging tile of row-contiguous operands
+    extern __shared__ __align__(16) unsigned short stage[];
 
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const int m0 = blockIdx.x * TC_M, n0 = blockIdx.y * NT;
@@ -149,9 +177,9 @@ k_gemm_tc(int M, int N, int K, const __nv_bfloat16 *__restrict__ A, long long a_
     for (int kb = 0; kb < kblocks && ok; ++kb) {
         const int k0 = kb * TC_K;
         // A tile: 128 rows x 64 k; element (r, kk) at (r/8)*1024 + (kk/8)*128 + (r%8)*16 + (kk%8)*2
-        load_tile<TC_M>(sA, A, a_rs, a_cs, m0, M, k0, K, tid);
+        load_tile<TC_M>(sA, A, a_rs, a_cs, m0, M, k0, K, tid, stage);
         // B tile: NT rows (n) x 64 k, same layout; B(k, n) = B[k * b_rs + n * b_cs]
-        load_tile<NT>(sB, B, b_cs, b_rs, n0, N, k0, K, tid);
+        load_tile<NT>(sB, B, b_cs, b_rs, n0, N, k0, K, tid, stage);
         // make the generic-proxy writes visible to the tensor core
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
         __syncthreads();
@@ -187,7 +215,40 @@ k_gemm_tc(int M, int N, int K, const __nv_bfloat16 *__restrict__ A, long long a_
         ok = __syncthreads_and(ok) != 0;
     }
 
-    if (ok) {
+    if (ok && c_cs == 1 && c_rs != 1) {
+        // row-major C: each warp stages its 32 x 16 block in shared memory (the
+        // A tile is free now; a 17-float pitch keeps the banks distinct) and
+        // writes it two rows per instruction, 16 consecutive columns each, so
+        // the stores coalesce instead of 32 lanes hitting 32 rows
+        float *stage = reinterpret_cast<float *>(sA) + warp * (32 * 17);
+#pragma unroll 1
+        for (int c0 = 0; c0 < NT; c0 += 16) {
+            uint32_t v[16];
+            const uint32_t taddr = tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0;
+            asm volatile(
+                "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, "
+                "%14, %15}, [%16];"
+                : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7]),
+                  "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]),
+                  "=r"(v[15])
+                : "r"(taddr));
+            asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+            for (int j = 0; j < 16; ++j) stage[lane * 17 + j] = __uint_as_float(v[j]);
+            __syncwarp();
+#pragma unroll 4
+            for (int i = 0; i < 16; ++i) {
+                const int r = 2 * i + (lane >> 4), j = lane & 15;
+                const int row = m0 + warp * 32 + r, col = n0 + c0 + j;
+                if (row < M && col < N) {
+                    OUT *cp = C + (long long)row * c_rs + col;
+                    const float acc = stage[r * 17 + j];
+                    store_out(cp, beta == 0.f ? alpha * acc : alpha * acc + beta * load_out(cp));
+                }
+            }
+            __syncwarp();
+        }
+    } else if (ok) {
         // epilogue: warp w reads TMEM lanes 32w..32w+31 = rows m0+32w+lane
         const int row = m0 + warp * 32 + lane;
 #pragma unroll 1
@@ -276,14 +337,16 @@ static int launch_gemm(int m, int n, int k, const __nv_bfloat16 *a, long long a_
                                               alpha, beta);
         return check_launch("k_gemm_simt");
     }
-    // tensor cores: tile N 32/64/128 by problem width.  Unused dynamic shared
-    // memory caps the CTAs resident on one SM so that their tensor memory
-    // (NT columns each) never exceeds the SM's 512 columns and no allocation
-    // has to wait: 24.6 KB static -> 9 CTAs x 32 columns; + 4 KB -> 7 x 64;
-    // 32.8 KB static + 16 KB -> 4 x 128.
-    const int pad32 = 0, pad64 = 4 * 1024, pad128 = 16 * 1024;
+    // tensor cores: tile N 32/64/128 by problem width.  The dynamic shared
+    // memory (16 KB: the staging tile of row-contiguous operands) also caps
+    // the CTAs resident on one SM so that their tensor memory (NT columns
+    // each) never exceeds the SM's 512 columns and no allocation waits:
+    // 24.6 KB static + 16 KB -> 5 CTAs x 32 or 64 columns; 32.8 KB + 16 KB ->
+    // 4 x 128.
+    const int pad32 = TC_K * TC_M * 2, pad64 = pad32, pad128 = pad32;
     static bool attr_set = false;  // one flag per output type (one instantiation each)
     if (!attr_set) {
+        cudaFuncSetAttribute(k_gemm_tc<32, OUT>, cudaFuncAttributeMaxDynamicSharedMemorySize, pad32);
         cudaFuncSetAttribute(k_gemm_tc<64, OUT>, cudaFuncAttributeMaxDynamicSharedMemorySize, pad64);
         cudaFuncSetAttribute(k_gemm_tc<128, OUT>, cudaFuncAttributeMaxDynamicSharedMemorySize, pad128);
         attr_set = true;

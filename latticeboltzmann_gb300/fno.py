@@ -231,7 +231,8 @@ class FNO2d:
                        "dP": torch.empty(C * B * m2 * q2, **bf),
                        "parts": torch.empty(256 * max(self.hidden * C, C * C, C * self.cin, self.cout * self.hidden),
                                             **f32),
-                       "mse": torch.empty(1024, dtype=torch.float64, device=self.device)})
+                       "mse": torch.empty(1024, dtype=torch.float64, device=self.device),
+                       "rowsum": torch.empty(64 * max(self.hidden, C, self.cout), **f32)})
         self._ws[key] = ws
         return ws
 
@@ -321,13 +322,13 @@ class FNO2d:
         _lib.call("lbgb_fno_to_bf16", _ptr(d), _ptr(ws["db"]), self.cout * N, s)
         # out = Q2 g + q2
         self._wgrad(hid, self.cout, N, _ptr(ws["gb"]), _ptr(ws["db"]), _ptr(g, o["Q2"]), 1, hid, ws)
-        _lib.call("lbgb_fno_row_sum", _ptr(d), _ptr(g, o["q2b"]), self.cout, N, s)
+        _lib.call("lbgb_fno_row_sum", _ptr(d), _ptr(g, o["q2b"]), _ptr(ws["rowsum"]), self.cout, N, s)
         dh = ws["dh"]
         self._gemm(N, hid, self.cout, _ptr(ws["db"]), (1, N, 0), _ptr(pb, o["Q2"]), (hid, 1, 0), _ptr(dh), (1, N, 0))
         _lib.call("lbgb_fno_gelu_back", _ptr(dh), _ptr(ws["h"]), _ptr(dh), _ptr(ws["dhb"]), hid * N, s)
         # h = Q1 v_L + q1
         self._wgrad(hid, C, N, _ptr(ws["dhb"]), _ptr(ws["vb"][self.layers]), _ptr(g, o["Q1"]), C, 1, ws)
-        _lib.call("lbgb_fno_row_sum", _ptr(dh), _ptr(g, o["q1b"]), hid, N, s)
+        _lib.call("lbgb_fno_row_sum", _ptr(dh), _ptr(g, o["q1b"]), _ptr(ws["rowsum"]), hid, N, s)
         dv = ws["dv"]
         self._gemm(N, C, hid, _ptr(ws["dhb"]), (1, N, 0), _ptr(pb, o["Q1"]), (C, 1, 0), _ptr(dv), (1, N, 0))
         dzb = ws["dzb"]
@@ -338,7 +339,7 @@ class FNO2d:
                 _lib.call("lbgb_fno_gelu_back", _ptr(dv), _ptr(ws["z"][l]), _ptr(dv), _ptr(dzb), C * N, s)
             v = ws["vb"][l]
             self._wgrad(C, C, N, _ptr(dzb), _ptr(v), _ptr(g, o["W%d" % l]), C, 1, ws)
-            _lib.call("lbgb_fno_row_sum", _ptr(dv), _ptr(g, o["b%d" % l]), C, N, s)
+            _lib.call("lbgb_fno_row_sum", _ptr(dv), _ptr(g, o["b%d" % l]), _ptr(ws["rowsum"]), C, N, s)
             # spectral branch, transposed step by step
             self._gemm(C * B * H, m2, W, _ptr(dzb), (W, 1, 0), _ptr(iw), (m2, 1, 0), _ptr(ws["Z"]), (m2, 1, 0),
                        bf16_out=True)
@@ -356,7 +357,7 @@ class FNO2d:
         # lifting
         _lib.call("lbgb_fno_to_bf16", _ptr(dv), _ptr(dzb), C * N, s)
         self._wgrad(C, self.cin, N, _ptr(dzb), _ptr(ws["ab"]), _ptr(g, o["P"]), self.cin, 1, ws)
-        _lib.call("lbgb_fno_row_sum", _ptr(dv), _ptr(g, o["pb"]), C, N, s)
+        _lib.call("lbgb_fno_row_sum", _ptr(dv), _ptr(g, o["pb"]), _ptr(ws["rowsum"]), C, N, s)
 
     def adam(self, lr, b1=0.9, b2=0.999, eps=1e-8, weight_decay=0.0):
         """One Adam step on the FP32 master weights; refreshes the BF16 copy."""
