@@ -406,33 +406,55 @@ def omega_for(re, u_lid, length):
     return 2.0 * re / (6.0 * length * u_lid + re)
 
 
-def _run_to_steady(bl, tol, every, max_steps, log=None, what=""):
+def _run_to_steady(bl, tol, every, max_steps, log=None, what="", patience=0):
     """Step the active instances of bl until max|u^(t+every) - u^t| < tol;
-    converged instances leave the queue.  Returns (steps per instance, -1 if
-    max_steps passed; last velocity change per instance)."""
+    converged instances leave the queue.
+
+    patience > 0: an instance whose change has not dropped below 0.9 x its
+    best for ``patience`` checks in a row stops as stalled (its storage's
+    rounding floor lies above tol).  Returns (steps per instance: the step
+    count at convergence, -1 if max_steps passed, -2 if stalled; the last
+    velocity change; the step count at which each instance stalled)."""
     bl.velocity_change()
-    steps = np.full(bl.n, -1, dtype=np.int64)
-    steps[~bl.active] = 0
-    change = np.full(bl.n, np.inf)
+    n = bl.n
+    state = np.where(bl.active, 0, 3)  # 0 running, 1 converged, 2 stalled, 3 not run
+    steps = np.where(state == 3, 0, -1).astype(np.int64)
+    change = np.full(n, np.inf)
+    best = np.full(n, np.inf)
+    since = np.zeros(n, dtype=np.int64)
+    stalled_at = np.zeros(n, dtype=np.int64)
     done = 0
-    while done < max_steps and (steps < 0).any():
+    while done < max_steps and (state == 0).any():
         bl.step(every)
         done += every
         ch = bl.velocity_change().cpu().numpy()
-        live = steps < 0
+        live = state == 0
         change[live] = ch[live]
-        newly = live & (ch < tol)
-        steps[newly] = done
-        if newly.any():
-            bl.set_active(steps < 0)
+        conv = live & (ch < tol)
+        steps[conv] = done
+        state[conv] = 1
+        stall = np.zeros(n, dtype=bool)
+        if patience:
+            going = live & ~conv
+            better = going & (ch < 0.9 * best)
+            best[better] = ch[better]
+            since[better] = 0
+            since[going & ~better] += 1
+            stall = going & (since >= patience)
+            state[stall] = 2
+            steps[stall] = -2
+            stalled_at[stall] = done
+        if conv.any() or stall.any():
+            bl.set_active(state == 0)
         if log is not None and done % (every * 50) == 0:
-            log("steady_cavities%s: %d steps, %d/%d converged" % (what, done, int((steps >= 0).sum()), bl.n))
-    return steps, change
+            log("steady_cavities%s: %d steps, %d/%d converged, %d stalled" % (
+                what, done, int((state == 1).sum()), n, int((state == 2).sum())))
+    return steps, change, stalled_at
 
 
 def steady_cavities(re, u_lid, n=256, tol=1e-7, every=1000, max_steps=1_000_000, storage="f32", device=None,
-                    tune=True, log=None, boundary="cavity-ladd", start=None, refine=None, switch_tol=1e-6,
-                    info=None):
+                    tune=True, log=None, boundary="cavity-ladd", start=None, refine=None, switch_tol=None,
+                    patience=30, info=None):
     """Run lid-driven cavities (n x n) to steady state, all in one batch.
 
     The default lid is the wall-density-1 one: the reference's lid adds mass
@@ -443,11 +465,13 @@ def steady_cavities(re, u_lid, n=256, tol=1e-7, every=1000, max_steps=1_000_000,
     Steady: max over the cavity of |u^(t+every) - u^t| < tol.  Converged
     instances leave the task queue.
 
-    refine: None, or a wider storage ("f64") for a second phase: the batch
-    runs in ``storage`` until the change is below max(tol, switch_tol), then
-    continues in ``refine`` storage down to tol.  FP32 storage has a rounding
-    floor of about 1e-7 per 1000 steps at high Reynolds numbers, so tol = 1e-7
-    needs FP64 there.
+    refine: None, or a wider storage ("f64") for the instances the first
+    storage cannot bring to tol: with switch_tol = None (adaptive) an
+    instance moves to ``refine`` once its change has stalled for
+    ``patience`` checks (FP32 storage stalls near 1e-6 per 1000 steps above
+    Re ~ 200 at 256^2, FP32 deviations near 1e-7); with a switch_tol every
+    instance runs in ``storage`` down to max(tol, switch_tol) and finishes in
+    ``refine``.
 
     Returns (fields float32 (N, 3, n, n) of rho, ux, uy; steps to convergence
     per instance, summed over both phases, -1 if a phase hit max_steps; wall
@@ -467,23 +491,26 @@ def steady_cavities(re, u_lid, n=256, tol=1e-7, every=1000, max_steps=1_000_000,
         bl.chapman_enskog(start)
     torch.cuda.synchronize(bl.device)
     t0 = time.perf_counter()
-    tol1 = tol if refine is None else max(tol, switch_tol)
-    steps, change = _run_to_steady(bl, tol1, every, max_steps, log, "")
+    adaptive = refine is not None and switch_tol is None
+    tol1 = tol if refine is None or adaptive else max(tol, switch_tol)
+    steps, change, stalled_at = _run_to_steady(bl, tol1, every, max_steps, log, "", patience if adaptive else 0)
     if info is not None:
         info["phase1_steps"], info["phase1_change"] = steps.copy(), change.copy()
-    if refine is not None and tol1 > tol:
+    need = (steps == -2) if adaptive else (steps >= 0 if (refine is not None and tol1 > tol) else None)
+    if need is not None and need.any():
         bl2 = BatchedLattice(sizes, om, boundary=boundary, u0=u_lid, storage=refine, device=device)
-        ok = steps >= 0
         for b in range(len(re)):
             bl2.load(b, bl.populations(b, torch.float64))
         del bl
         if tune:
             bl2.autotune(steps=3, warmup=1)
-        bl2.set_active(ok)
-        s2, change = _run_to_steady(bl2, tol, every, max_steps, log, " (%s)" % refine)
+        bl2.set_active(need)
+        s2, change2, _ = _run_to_steady(bl2, tol, every, max_steps, log, " (%s)" % refine)
+        change = np.where(need, change2, change)
         if info is not None:
-            info["phase2_steps"], info["phase2_change"] = s2.copy(), change.copy()
-        steps = np.where(ok & (s2 >= 0), steps + s2, -1)
+            info["phase2_steps"], info["phase2_change"] = np.where(need, s2, 0), change2.copy()
+        base = stalled_at if adaptive else steps
+        steps = np.where(need, np.where(s2 >= 0, base + s2, -1), steps)
         bl = bl2
     if info is not None:
         info["change"] = change

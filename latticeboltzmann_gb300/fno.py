@@ -396,3 +396,44 @@ class FNO2d:
         sc = [float(x) for x in self.out_scale]
         u = torch.as_tensor(np.atleast_1d(u_lid), dtype=torch.float32, device=self.device)[:, None, None]
         return 1 + out[0] * (sc[0] * u * u), out[1] * (sc[1] * u), out[2] * (sc[2] * u)
+
+
+def main(argv=None):
+    """Time training steps (forward, backward, Adam) and inference of the
+    network on synthetic inputs: ``python -m latticeboltzmann_gb300.fno``."""
+    import argparse
+    import time
+    ap = argparse.ArgumentParser(description=main.__doc__)
+    ap.add_argument("--batch", type=int, default=16)
+    ap.add_argument("--n", type=int, default=256)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--engine", choices=["tensor", "cuda"], default="tensor")
+    args = ap.parse_args(argv)
+    dev = torch.device("cuda", torch.cuda.current_device())
+    net = FNO2d(device=dev, engine=ENGINE_TENSOR_CORES if args.engine == "tensor" else ENGINE_CUDA_CORES)
+    rng = np.random.default_rng(0)
+    re = np.exp(rng.uniform(math.log(RE_RANGE[0]), math.log(RE_RANGE[1]), args.batch))
+    a = net.inputs(re, rng.uniform(*U_RANGE, args.batch), args.n, args.n)
+    t = torch.randn(net.cout, args.batch, args.n, args.n, device=dev)
+    for _ in range(args.warmup):
+        net.loss_and_backward(a, t)
+        net.adam(1e-3)
+    torch.cuda.synchronize(dev)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        net.loss_and_backward(a, t)
+        net.adam(1e-3)
+    torch.cuda.synchronize(dev)
+    train = (time.perf_counter() - t0) / max(args.steps, 1)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        net.forward(a)
+    torch.cuda.synchronize(dev)
+    fwd = (time.perf_counter() - t0) / max(args.steps, 1)
+    print(json.dumps({"batch": args.batch, "n": args.n, "engine": args.engine, "train_step_ms": round(train * 1e3, 3),
+                      "forward_ms": round(fwd * 1e3, 3), "params": int(sum(np.prod(s) for s in net.shapes.values()))}))
+
+
+if __name__ == "__main__":
+    main()

@@ -40,12 +40,24 @@ def sample_parameters(n, seed=0, re_range=RE_RANGE, u_range=U_RANGE):
     return re, u
 
 
+# How the steady runs go: FP32-deviation storage (same speed as FP32, a 10x
+# lower rounding floor) straight to the tolerance; an instance whose velocity
+# change stalls above it (its floor) finishes in FP64.  set_precision() changes
+# it (the first data set was made with FP32 down to 1e-6, then FP64).
+PRECISION = {"storage": "f32dev", "switch_tol": None}
+
+
+def set_precision(storage="f32dev", switch_tol=None):
+    PRECISION.update(storage=storage, switch_tol=switch_tol)
+
+
 def steady_run(re, u, n, start=None, device=None, tol=1e-7, log=None, max_steps=600_000, tune=True):
-    """Two-phase steady runs of a batch; returns (fields (N, 3, n, n) FP32, steps, wall s, info)."""
+    """Steady runs of a batch (see PRECISION); returns (fields (N, 3, n, n) FP32, steps, wall s, info)."""
     info = {}
-    fields, steps, wall = B.steady_cavities(re, u, n=n, tol=tol, every=1000, max_steps=max_steps, storage="f32",
-                                            device=device, tune=tune, log=log, start=start, refine="f64",
-                                            switch_tol=max(tol, 1e-6), info=info)
+    fields, steps, wall = B.steady_cavities(re, u, n=n, tol=tol, every=1000, max_steps=max_steps,
+                                            storage=PRECISION["storage"], device=device, tune=tune, log=log,
+                                            start=start, refine="f64", switch_tol=PRECISION["switch_tol"],
+                                            info=info)
     return fields, steps, wall, info
 
 
@@ -135,6 +147,67 @@ def study(net, re, u, n, device=None, tol=1e-7, log=None, max_steps=600_000, ref
             "steady_max_abs_du_warm_vs_cold": dfin.cpu().numpy().tolist()}
 
 
+def single_case_timing(net, re, u, n, device=None, tol=1e-7, max_steps=600_000):
+    """Wall time of each cavity (re[i], u[i]) run on its own, from rest and from
+    the network's prediction (the warm time includes inference and the start
+    kernel): what a user solving one cavity sees."""
+    rows = []
+    for r, v in zip(np.atleast_1d(re), np.atleast_1d(u)):
+        _, cs, cw, _ = steady_run([r], [v], n, device=device, tol=tol, max_steps=max_steps, tune=False)
+        torch.cuda.synchronize(device)
+        t0 = time.perf_counter()
+        rho, ux, uy = net.predict([r], [v], n, n)
+        _, ws, ww, _ = steady_run([r], [v], n, device=device, tol=tol, max_steps=max_steps, tune=False,
+                                  start=lambda b: (rho[b], ux[b], uy[b]))
+        torch.cuda.synchronize(device)
+        warm = time.perf_counter() - t0
+        rows.append({"re": float(r), "u": float(v), "cold_steps": int(cs[0]), "warm_steps": int(ws[0]),
+                     "cold_s": cw, "warm_s": warm})
+    return rows
+
+
+def study_only(args):
+    """Warm-versus-cold study of a trained network on the held-out pairs of
+    an earlier run (no data generation, no training)."""
+    os.makedirs(args.out, exist_ok=True)
+    dev = torch.device("cuda", torch.cuda.current_device())
+    logf = open(os.path.join(args.out, "log.txt"), "a")
+
+    def log(m):
+        print(m, flush=True)
+        logf.write(m + "\n")
+        logf.flush()
+
+    net = FNO2d.load(args.weights, device=dev)
+    prev = json.load(open(args.held_out_from))
+    val = np.asarray(prev["held_out"])
+    re_all, u_all = np.asarray(prev["data_re"]), np.asarray(prev["data_u"])
+    res = {"weights": os.path.basename(args.weights), "storage": args.storage, "switch_tol": args.switch_tol}
+    res["study"] = study(net, re_all[val], u_all[val], args.n, dev, max_steps=args.max_steps)
+    s = res["study"]
+    log("study %d: cold %.1f s, warm %.1f s (inference %.3f s); steps cold %d warm %d (sums)" % (
+        args.n, s["cold_wall_s"], s["warm_wall_s"], s["inference_s"], sum(s["cold_steps"]), sum(s["warm_steps"])))
+    sel = val[np.argsort(re_all[val])]
+    sel = sel[np.linspace(0, len(sel) - 1, min(args.single_cases, len(sel))).astype(int)]
+    res["single"] = single_case_timing(net, re_all[sel], u_all[sel], args.n, dev, max_steps=args.max_steps)
+    for row in res["single"]:
+        log("single %d: Re %.1f u %.3f cold %d steps %.2f s, warm %d steps %.2f s" % (
+            args.n, row["re"], row["u"], row["cold_steps"], row["cold_s"], row["warm_steps"], row["warm_s"]))
+    if args.study_large:
+        low = val[re_all[val] <= 150]
+        low = low[np.argsort(re_all[low])]
+        sel = low[np.linspace(0, len(low) - 1, min(args.large_cases, len(low))).astype(int)] if len(low) else low
+        res["single_large"] = single_case_timing(net, re_all[sel], u_all[sel], args.study_large, dev,
+                                                 max_steps=1_500_000)
+        for row in res["single_large"]:
+            log("single %d: Re %.1f u %.3f cold %d steps %.2f s, warm %d steps %.2f s" % (
+                args.study_large, row["re"], row["u"], row["cold_steps"], row["cold_s"], row["warm_steps"],
+                row["warm_s"]))
+    with open(os.path.join(args.out, "results.json"), "w") as f:
+        json.dump(res, f, indent=1)
+    return 0
+
+
 def main(argv=None):
     ap = argparse.ArgumentParser(description="steady-cavity data, surrogate training and warm-start study")
     ap.add_argument("--samples", type=int, default=2000)
@@ -146,9 +219,19 @@ def main(argv=None):
     ap.add_argument("--max-steps", type=int, default=600_000)
     ap.add_argument("--study-large", type=int, default=1024, help="side of the upsampled study (0: skip)")
     ap.add_argument("--large-cases", type=int, default=4)
+    ap.add_argument("--single-cases", type=int, default=8, help="held-out cavities timed one at a time")
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--out", default="surrogate_out")
+    ap.add_argument("--storage", default="f32dev", help="storage of the steady runs before any FP64 refinement")
+    ap.add_argument("--switch-tol", type=float, default=None,
+                    help="run every instance to this change, then FP64 (default: FP64 only where a run stalls)")
+    ap.add_argument("--weights", default=None, help="study only: a trained network (.npz) instead of training")
+    ap.add_argument("--held-out-from", default=None,
+                    help="study only: results.json of the training run that holds the held-out (Re, u) pairs")
     args = ap.parse_args(argv)
+    set_precision(args.storage, args.switch_tol)
+    if args.weights:
+        return study_only(args)
     os.makedirs(args.out, exist_ok=True)
     dev = torch.device("cuda", torch.cuda.current_device())
     logf = open(os.path.join(args.out, "log.txt"), "a")
@@ -188,6 +271,13 @@ def main(argv=None):
     s = res["study"]
     log("study %d: cold %.1f s, warm %.1f s (inference %.3f s); steps cold %d warm %d (sums)" % (
         args.n, s["cold_wall_s"], s["warm_wall_s"], s["inference_s"], sum(s["cold_steps"]), sum(s["warm_steps"])))
+    dump()
+    sel = val[np.argsort(data["re"][val])]
+    sel = sel[np.linspace(0, len(sel) - 1, min(args.single_cases, len(sel))).astype(int)]
+    res["single"] = single_case_timing(net, data["re"][sel], data["u"][sel], args.n, dev, max_steps=args.max_steps)
+    for row in res["single"]:
+        log("single %d: Re %.1f u %.3f cold %d steps %.2f s, warm %d steps %.2f s" % (
+            args.n, row["re"], row["u"], row["cold_steps"], row["cold_s"], row["warm_steps"], row["warm_s"]))
     dump()
     if args.study_large:
         # cost grows like side^3 / Re at fixed Re: the upsampled study keeps to Re <= 150
