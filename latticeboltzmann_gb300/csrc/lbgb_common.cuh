@@ -295,11 +295,20 @@ __device__ __forceinline__ typename Packet<DT, N>::vec enc_h_sr(const float (&h)
 // ux, uy scaled by 3, uu = (ux^2 + uy^2)/6, feq_i = w_i rho (1 + cu + cu^2/2 - uu).
 __device__ __forceinline__ float recip(float x) { return __frcp_rn(x); }
 __device__ __forceinline__ double recip(double x) { return __drcp_rn(x); }
+// hardware reciprocal approximation (one MUFU op, ~1 ulp): for 16-bit storage,
+// whose own rounding is 2^-11 or coarser
+__device__ __forceinline__ float recip_approx(float x) {
+    float r;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+}
 
 // BGK relaxation of one node with its density already summed.
-template <class R>
+template <class R, bool APPROX_RCP = false>
 __device__ __forceinline__ void bgk_relax(R (&f)[9], R omega, R rho, R &ux_out, R &uy_out) {
-    const R inv = recip(rho);
+    R inv;
+    if constexpr (APPROX_RCP) inv = recip_approx(rho);
+    else inv = recip(rho);
     R ux = (f[1] - f[3] + f[5] - f[6] - f[7] + f[8]) * inv;
     R uy = (f[2] - f[4] + f[5] + f[6] - f[7] - f[8]) * inv;
     ux_out = ux;
@@ -341,6 +350,17 @@ __device__ __forceinline__ void bgk_collide(R (&f)[9], R omega) {
     bgk_collide(f, omega, a, b, c);
 }
 
+// The collision of the 16-bit storage paths: the same arithmetic with the
+// hardware reciprocal approximation of rho (the stored values round at 2^-11
+// or coarser, far above its ~1 ulp).
+__device__ __forceinline__ void bgk_collide16(float (&f)[9], float omega) {
+    float rho = f[0];
+#pragma unroll
+    for (int i = 1; i < 9; ++i) rho += f[i];
+    float ux, uy;
+    bgk_relax<float, true>(f, omega, rho, ux, uy);
+}
+
 // FP16 deviation storage, round to nearest: collide one node and return its
 // scaled mass deviation D S, D = sum_i (f_i - w_i) summed over the small
 // deviations (accurate to FP32 rounding of numbers ~1e-2, unbiased); the
@@ -351,7 +371,7 @@ __device__ __forceinline__ float collide_f16_mass(float (&f)[9], float omega) {
 #pragma unroll
     for (int i = 1; i < 9; ++i) d += f[i] - wgt<float>(i);
     float ux, uy;
-    bgk_relax(f, omega, 1.f + d, ux, uy);
+    bgk_relax<float, true>(f, omega, 1.f + d, ux, uy);
     return d * F16_SCALE;
 }
 
@@ -466,6 +486,10 @@ __device__ __forceinline__ void collide_encode(typename Codec<DT>::real (&f)[9],
             dms -= __half2float(q);
         }
         out[0] = __half_as_ushort(__float2half_rn(dms));
+    } else if constexpr (DT == LBGB_BF16DEV) {
+        bgk_collide16(f, omega);
+#pragma unroll
+        for (int i = 0; i < 9; ++i) out[i] = C::enc(f[i], i);
     } else {
         bgk_collide(f, omega);
 #pragma unroll
@@ -482,7 +506,7 @@ __device__ __forceinline__ void collide_encode_sr(float (&f)[9], float omega, un
     float dm = f[0] - wgt<float>(0);
 #pragma unroll
     for (int i = 1; i < 9; ++i) dm += f[i] - wgt<float>(i);
-    bgk_collide(f, omega);
+    bgk_collide16(f, omega);
 #pragma unroll
     for (int i = 1; i < 9; ++i) {
         const uint32_t r = sr_pair_bits(key, cell & ~1u, i);

@@ -93,8 +93,8 @@ struct PipeGeom {
 // 4 cells each.
 template <int DT> struct PipeShape { static constexpr int NCW = 8, NC = 4; };
 template <> struct PipeShape<LBGB_F64> { static constexpr int NCW = 8, NC = 2; };
-template <> struct PipeShape<LBGB_F16DEV> { static constexpr int NCW = 16, NC = 4; };
-template <> struct PipeShape<LBGB_BF16DEV> { static constexpr int NCW = 16, NC = 4; };
+template <> struct PipeShape<LBGB_F16DEV> { static constexpr int NCW = 8, NC = 8; };
+template <> struct PipeShape<LBGB_BF16DEV> { static constexpr int NCW = 8, NC = 8; };
 
 template <int DT, int BC, bool COLLIDE, int NCW_, int NC_, bool SRND>
 __global__ void __launch_bounds__((NCW_ + 1) * 32, 1)
@@ -300,7 +300,7 @@ k_step_pipe(const typename Codec<DT>::raw *__restrict__ src, typename Codec<DT>:
 #pragma unroll
                     for (int i = 1; i < 9; ++i) dm[j] += f[i] - wgt<real>(i);
                 }
-                bgk_collide(f, omega);
+                bgk_collide16(f, omega);
 #pragma unroll
                 for (int i = 0; i < 9; ++i) hpost[i][j] = f[i] - wgt<real>(i);
             }
