@@ -69,7 +69,6 @@ __device__ __forceinline__ float load_out(const float *p) { return *p; }
 __device__ __forceinline__ float load_out(const __nv_bfloat16 *p) { return __bfloat162float(*p); }
 
 constexpr int TC_M = 128;
-constexpr int TC_K = 64;
 constexpr long long TC_WAIT = 1ll << 22;
 
 // Copies rows [r0, r0+ROWS) x k [k0, k0+64) of X (element (r, k) at
@@ -77,7 +76,7 @@ constexpr long long TC_WAIT = 1ll << 22;
 // Thread-to-element mapping follows the contiguous axis so that a warp's
 // loads coalesce: 16-byte vector loads along K when K is contiguous and
 // aligned, consecutive rows per warp when the rows are contiguous.
-template <int ROWS>
+template <int ROWS, int KB>
 __device__ __forceinline__ void load_tile(unsigned char *dst, const __nv_bfloat16 *__restrict__ X, long long rs,
                                           long long ks, int r0, int R, int k0, int K, int tid,
                                           unsigned short *stage) {
@@ -87,7 +86,7 @@ __device__ __forceinline__ void load_tile(unsigned char *dst, const __nv_bfloat1
         // at one k into a [k][row] staging tile, then each thread gathers the
         // 8 k values of one row into a 16-byte core-matrix row
         constexpr int G = ROWS / 8;
-        for (int e = tid; e < TC_K * G; e += 128) {
+        for (int e = tid; e < KB * G; e += 128) {
             const int kk = e / G, g = e - kk * G;
             const int gk = k0 + kk;
             uint4 w = make_uint4(0u, 0u, 0u, 0u);
@@ -95,27 +94,27 @@ __device__ __forceinline__ void load_tile(unsigned char *dst, const __nv_bfloat1
             *reinterpret_cast<uint4 *>(stage + kk * ROWS + 8 * g) = w;
         }
         __syncthreads();
-        for (int e = tid; e < ROWS * (TC_K / 8); e += 128) {
+        for (int e = tid; e < ROWS * (KB / 8); e += 128) {
             const int r = e % ROWS, kc = e / ROWS;
             unsigned short h[8];
 #pragma unroll
             for (int q = 0; q < 8; ++q) h[q] = stage[(kc * 8 + q) * ROWS + r];
             uint4 w;
             memcpy(&w, h, 16);
-            *reinterpret_cast<uint4 *>(dst + (r >> 3) * 1024 + kc * 128 + (r & 7) * 16) = w;
+            *reinterpret_cast<uint4 *>(dst + (r >> 3) * (KB * 16) + kc * 128 + (r & 7) * 16) = w;
         }
         __syncthreads();  // the staging tile is reused by the next operand
         return;
     }
     const bool vec = ks == 1 && (rs & 7) == 0 && ((reinterpret_cast<uintptr_t>(X) & 15) == 0);
-    for (int e = tid; e < ROWS * TC_K / 8; e += 128) {
+    for (int e = tid; e < ROWS * KB / 8; e += 128) {
         int r, kc;
         if (row_contig) {
             r = e % ROWS;
             kc = e / ROWS;
         } else {
-            r = e >> 3;
-            kc = e & 7;
+            r = e / (KB / 8);
+            kc = e % (KB / 8);
         }
         const int gr = r0 + r, gk = k0 + kc * 8;
         uint4 w = make_uint4(0u, 0u, 0u, 0u);
@@ -130,22 +129,23 @@ __device__ __forceinline__ void load_tile(unsigned char *dst, const __nv_bfloat1
                 memcpy(&w, h, 16);
             }
         }
-        *reinterpret_cast<uint4 *>(dst + (r >> 3) * 1024 + kc * 128 + (r & 7) * 16) = w;
+        *reinterpret_cast<uint4 *>(dst + (r >> 3) * (KB * 16) + kc * 128 + (r & 7) * 16) = w;
     }
 }
 
-template <int NT, typename OUT>
+template <int NT, typename OUT, int KB>
 __global__ void __launch_bounds__(128, 1)
 k_gemm_tc(int M, int N, int K, const __nv_bfloat16 *__restrict__ A, long long a_rs, long long a_cs, long long a_bs,
           const __nv_bfloat16 *__restrict__ B, long long b_rs, long long b_cs, long long b_bs, OUT *__restrict__ C,
           long long c_rs, long long c_cs, long long c_bs, float alpha, float beta) {
     static_assert(NT % 16 == 0 && NT >= 32 && NT <= 256, "tile N");
-    __shared__ __align__(1024) unsigned char sA[TC_M * TC_K * 2];
-    // at least 8 KB: any reading of the descriptor's byte offsets stays inside
-    __shared__ __align__(1024) unsigned char sB[(NT < 64 ? 64 : NT) * TC_K * 2];
+    static_assert(KB == 32 || KB == 64, "K block");
+    __shared__ __align__(1024) unsigned char sA[TC_M * KB * 2];
+    __shared__ __align__(1024) unsigned char sB[NT * KB * 2];
     __shared__ __align__(8) uint64_t bar;
     __shared__ uint32_t tmem_slot;
-    // dynamic shared memory: the [k][row] staging tile of row-contiguous operands
+    // dynamic shared memory: the [k][row] staging tile of row-contiguous
+    // operands, and the staging of row-major output in the epilogue
     extern __shared__ __align__(16) unsigned short stage[];
 
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
@@ -173,23 +173,23 @@ k_gemm_tc(int M, int N, int K, const __nv_bfloat16 *__restrict__ A, long long a_
 
     uint32_t phase = 0;
     bool ok = true;
-    const int kblocks = (K + TC_K - 1) / TC_K;
+    const int kblocks = (K + KB - 1) / KB;
     for (int kb = 0; kb < kblocks && ok; ++kb) {
-        const int k0 = kb * TC_K;
-        // A tile: 128 rows x 64 k; element (r, kk) at (r/8)*1024 + (kk/8)*128 + (r%8)*16 + (kk%8)*2
-        load_tile<TC_M>(sA, A, a_rs, a_cs, m0, M, k0, K, tid, stage);
-        // B tile: NT rows (n) x 64 k, same layout; B(k, n) = B[k * b_rs + n * b_cs]
-        load_tile<NT>(sB, B, b_cs, b_rs, n0, N, k0, K, tid, stage);
+        const int k0 = kb * KB;
+        // A tile: 128 rows x KB k; element (r, kk) at (r/8)*KB*16 + (kk/8)*128 + (r%8)*16 + (kk%8)*2
+        load_tile<TC_M, KB>(sA, A, a_rs, a_cs, m0, M, k0, K, tid, stage);
+        // B tile: NT rows (n) x KB k, same layout; B(k, n) = B[k * b_rs + n * b_cs]
+        load_tile<NT, KB>(sB, B, b_cs, b_rs, n0, N, k0, K, tid, stage);
         // make the generic-proxy writes visible to the tensor core
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
         __syncthreads();
         if (tid == 0) {
             asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
 #pragma unroll
-            for (int kk = 0; kk < TC_K / 16; ++kk) {
+            for (int kk = 0; kk < KB / 16; ++kk) {
                 // K = 16 per MMA: two core matrices along K, 256 bytes
-                const uint64_t da = umma_desc(smem_u32(sA) + kk * 256, 128, 1024);
-                const uint64_t db = umma_desc(smem_u32(sB) + kk * 256, 128, 1024);
+                const uint64_t da = umma_desc(smem_u32(sA) + kk * 256, 128, KB * 16);
+                const uint64_t db = umma_desc(smem_u32(sB) + kk * 256, 128, KB * 16);
                 const uint32_t acc = (kb > 0 || kk > 0) ? 1u : 0u;
                 asm volatile(
                     "{\n\t.reg .pred p;\n\t"
@@ -217,10 +217,10 @@ k_gemm_tc(int M, int N, int K, const __nv_bfloat16 *__restrict__ A, long long a_
 
     if (ok && c_cs == 1 && c_rs != 1) {
         // row-major C: each warp stages its 32 x 16 block in shared memory (the
-        // A tile is free now; a 17-float pitch keeps the banks distinct) and
+        // dynamic staging area; a 17-float pitch keeps the banks distinct) and
         // writes it two rows per instruction, 16 consecutive columns each, so
         // the stores coalesce instead of 32 lanes hitting 32 rows
-        float *stage = reinterpret_cast<float *>(sA) + warp * (32 * 17);
+        float *ostage = reinterpret_cast<float *>(stage) + warp * (32 * 17);
 #pragma unroll 1
         for (int c0 = 0; c0 < NT; c0 += 16) {
             uint32_t v[16];
@@ -234,7 +234,7 @@ k_gemm_tc(int M, int N, int K, const __nv_bfloat16 *__restrict__ A, long long a_
                 : "r"(taddr));
             asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 #pragma unroll
-            for (int j = 0; j < 16; ++j) stage[lane * 17 + j] = __uint_as_float(v[j]);
+            for (int j = 0; j < 16; ++j) ostage[lane * 17 + j] = __uint_as_float(v[j]);
             __syncwarp();
 #pragma unroll 4
             for (int i = 0; i < 16; ++i) {
@@ -242,7 +242,7 @@ k_gemm_tc(int M, int N, int K, const __nv_bfloat16 *__restrict__ A, long long a_
                 const int row = m0 + warp * 32 + r, col = n0 + c0 + j;
                 if (row < M && col < N) {
                     OUT *cp = C + (long long)row * c_rs + col;
-                    const float acc = stage[r * 17 + j];
+                    const float acc = ostage[r * 17 + j];
                     store_out(cp, beta == 0.f ? alpha * acc : alpha * acc + beta * load_out(cp));
                 }
             }
@@ -326,6 +326,27 @@ k_gemm_simt(int M, int N, int K, const __nv_bfloat16 *__restrict__ A, long long 
         }
 }
 
+// Dynamic shared memory of one tensor-core GEMM variant: the staging area
+// (a [k][row] tile, or the epilogue's 4 x 32 x 17 floats), grown until the
+// CTAs that fit on one SM hold at most the SM's 512 tensor-memory columns, so
+// that no allocation ever waits.  Computed once per variant.
+template <int NT, typename OUT, int KB>
+static int tc_dyn_smem() {
+    static int dyn = -1;
+    if (dyn >= 0) return dyn;
+    int d = KB * TC_M * 2;
+    if (d < 4 * 32 * 17 * 4) d = 4 * 32 * 17 * 4;
+    for (;;) {
+        cudaFuncSetAttribute(k_gemm_tc<NT, OUT, KB>, cudaFuncAttributeMaxDynamicSharedMemorySize, d);
+        int nb = 0;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_gemm_tc<NT, OUT, KB>, 128, d) != cudaSuccess) break;
+        if (nb * NT <= 512 || d >= 200 * 1024) break;
+        d += 1024;
+    }
+    dyn = d;
+    return d;
+}
+
 template <typename OUT>
 static int launch_gemm(int m, int n, int k, const __nv_bfloat16 *a, long long a_rs, long long a_cs, long long a_bs,
                        const __nv_bfloat16 *b, long long b_rs, long long b_cs, long long b_bs, OUT *C, long long c_rs,
@@ -337,33 +358,25 @@ static int launch_gemm(int m, int n, int k, const __nv_bfloat16 *a, long long a_
                                               alpha, beta);
         return check_launch("k_gemm_simt");
     }
-    // tensor cores: tile N 32/64/128 by problem width.  The dynamic shared
-    // memory (16 KB: the staging tile of row-contiguous operands) also caps
-    // the CTAs resident on one SM so that their tensor memory (NT columns
-    // each) never exceeds the SM's 512 columns and no allocation waits:
-    // 24.6 KB static + 16 KB -> 5 CTAs x 32 or 64 columns; 32.8 KB + 16 KB ->
-    // 4 x 128.
-    const int pad32 = TC_K * TC_M * 2, pad64 = pad32, pad128 = pad32;
-    static bool attr_set = false;  // one flag per output type (one instantiation each)
-    if (!attr_set) {
-        cudaFuncSetAttribute(k_gemm_tc<32, OUT>, cudaFuncAttributeMaxDynamicSharedMemorySize, pad32);
-        cudaFuncSetAttribute(k_gemm_tc<64, OUT>, cudaFuncAttributeMaxDynamicSharedMemorySize, pad64);
-        cudaFuncSetAttribute(k_gemm_tc<128, OUT>, cudaFuncAttributeMaxDynamicSharedMemorySize, pad128);
-        attr_set = true;
-    }
+    // tensor cores: tile N 32/64/128 by problem width, K blocks of 32 when K
+    // is that small (most of the surrogate's products), else 64
+    dim3 grid((m + TC_M - 1) / TC_M, 1, batch);
+#define LBGB_TC(NTV, KBV)                                                                                        \
+    do {                                                                                                       \
+        grid.y = (n + NTV - 1) / NTV;                                                                          \
+        const int dyn = tc_dyn_smem<NTV, OUT, KBV>();                                                          \
+        k_gemm_tc<NTV, OUT, KBV><<<grid, 128, dyn, s>>>(m, n, k, a, a_rs, a_cs, a_bs, b, b_rs, b_cs, b_bs, C, c_rs, \
+                                                        c_cs, c_bs, alpha, beta);                              \
+    } while (0)
+    const bool k32 = k <= 32;
     if (n <= 32) {
-        dim3 grid((m + TC_M - 1) / TC_M, (n + 31) / 32, batch);
-        k_gemm_tc<32, OUT><<<grid, 128, pad32, s>>>(m, n, k, a, a_rs, a_cs, a_bs, b, b_rs, b_cs, b_bs, C, c_rs, c_cs,
-                                                  c_bs, alpha, beta);
+        if (k32) LBGB_TC(32, 32); else LBGB_TC(32, 64);
     } else if (n <= 64) {
-        dim3 grid((m + TC_M - 1) / TC_M, (n + 63) / 64, batch);
-        k_gemm_tc<64, OUT><<<grid, 128, pad64, s>>>(m, n, k, a, a_rs, a_cs, a_bs, b, b_rs, b_cs, b_bs, C, c_rs, c_cs,
-                                                  c_bs, alpha, beta);
+        if (k32) LBGB_TC(64, 32); else LBGB_TC(64, 64);
     } else {
-        dim3 grid((m + TC_M - 1) / TC_M, (n + 127) / 128, batch);
-        k_gemm_tc<128, OUT><<<grid, 128, pad128, s>>>(m, n, k, a, a_rs, a_cs, a_bs, b, b_rs, b_cs, b_bs, C, c_rs, c_cs,
-                                                   c_bs, alpha, beta);
+        if (k32) LBGB_TC(128, 32); else LBGB_TC(128, 64);
     }
+#undef LBGB_TC
     return check_launch("k_gemm_tc");
 }
 
