@@ -374,7 +374,8 @@ def random_shear_batch(n=512, seed=0, nx_range=(32, 1024), ny_range=(16, 512), o
 
 
 def shear_study(n=512, steps=5000, every=10, seed=0, amplitude=0.05, storage="f32", device=None, tune=True):
-    """Config 4: fit the viscosity of every instance from its decay series."""
+    """Batched shear-wave study (512 uneven lattices by default): fit the
+    viscosity of every instance from its decay series."""
     sizes, om = random_shear_batch(n, seed)
     bl = BatchedLattice(sizes, om, boundary="periodic", storage=storage, device=device).shear_wave(amplitude)
     tuned = bl.autotune() if tune else None

@@ -38,7 +38,8 @@ def _density_mode(lat):
 
 
 def density_wave(nx=256, ny=128, omega=1.0, steps=10000, eps=0.01, storage="f64", every=1, device=None):
-    """Config 1: acoustic decay of a density wave; returns the series and the fit."""
+    """Acoustic decay of a periodic density wave (256 x 128, omega 1.0, FP64
+    by default); returns the series and the fit."""
     lat = Lattice(nx, ny, omega, boundary="periodic", storage=storage, device=device)
     x = torch.arange(nx, dtype=torch.float64, device=lat.device)
     rho = (1 + eps * torch.sin(2 * math.pi * x / nx))[:, None].expand(nx, ny)
@@ -108,7 +109,7 @@ def _make(n, omega, u0, variant, device):
 def precision(n=1024, omegas=(1.0, 1.7, 1.95), steps=50000, u0=0.1,
               storages=("f32", "f16dev", "bf16dev", "f16dev+sr", "bf16dev+sr"), device=None,
               checkpoints=(1000, 5000, 10000, 20000, 50000)):
-    """Config 3: error of reduced-precision storage against an FP64 run.
+    """Error of reduced-precision storage against an FP64 run of the same cavity.
 
     All lattices advance together; at each checkpoint the relative L2 error of
     the velocity field against the FP64 lattice and the mass drift are

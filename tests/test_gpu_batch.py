@@ -91,7 +91,7 @@ def test_batch_graph_replay_and_autotune(cuda):
 
 
 def test_shear_amplitude_and_viscosity(cuda):
-    """Config-4 style study on a small uneven batch.
+    """The batched shear-wave viscosity study on a small uneven batch.
 
     * The fitted viscosity of the smallest instances equals the fit of the
       FP64 oracle's run of the same instance within 1e-3 (the FP32 batch vs
