@@ -102,6 +102,20 @@ LBGB_API int lbgb_stream_bounce_back(const void *src, void *dst, int nx, int ny,
 LBGB_API int lbgb_step_fused(const void *src, void *dst, int nx, int ny, int boundary,
                     double omega, double u0, int dtype, void *stream);
 
+/* Copies rows k_begin <= k < k_end of all nine channel planes of a (9, nx, ny)
+ * array between any two memories (host or device; the direction comes from
+ * the pointers), asynchronously on stream: the transfers of the pipelined
+ * host step.  No counterpart in the reference. */
+LBGB_API int lbgb_copy_rows(void *dst, const void *src, int nx, int ny, int k_begin, int k_end, int dtype,
+                            void *stream);
+
+/* lbgb_step_fused restricted to the rows k_begin <= k < k_end of dst (every
+ * row of src may be read): the pieces of a step that is pipelined with the
+ * host transfers of neighbouring rows (Lattice.step_host).  Round to nearest
+ * for 16-bit storage.  No counterpart in the reference. */
+LBGB_API int lbgb_step_fused_rows(const void *src, void *dst, int nx, int ny, int k_begin, int k_end,
+                                  int boundary, double omega, double u0, int dtype, void *stream);
+
 /* nsteps fused steps ping-ponging between a and b (a holds the initial
  * state); *which receives 0 if the result is in a, 1 if in b.  Launch-only:
  * suitable for CUDA-graph capture. */

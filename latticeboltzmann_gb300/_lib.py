@@ -48,6 +48,8 @@ SIGNATURES = {
     "lbgb_stream_periodic": (_I, [_P, _P, _I, _I, _I, _P]),
     "lbgb_stream_bounce_back": (_I, [_P, _P, _I, _I, _D, _I, _P]),
     "lbgb_step_fused": (_I, [_P, _P, _I, _I, _I, _D, _D, _I, _P]),
+    "lbgb_copy_rows": (_I, [_P, _P, _I, _I, _I, _I, _I, _P]),
+    "lbgb_step_fused_rows": (_I, [_P, _P, _I, _I, _I, _I, _I, ctypes.c_double, ctypes.c_double, _I, _P]),
     "lbgb_run_fused": (_I, [_P, _P, _I, _I, _I, _D, _D, _I, _I, ctypes.POINTER(_I), _P]),
     "lbgb_run_fused_sr": (_I, [_P, _P, _I, _I, _I, _D, _D, _I, _I, ctypes.c_uint, _P, ctypes.POINTER(_I), _P]),
     "lbgb_macroscopic": (_I, [_P, _P, _P, _P, _I64, _I64, _I, _P]),

@@ -523,6 +523,29 @@ extern "C" int lbgb_pressure_periodic(void *f, int nx, int ny, double rho_in, do
     return check_launch("k_pressure_periodic");
 }
 
+extern "C" int lbgb_copy_rows(void *dst, const void *src, int nx, int ny, int k_begin, int k_end, int dtype,
+                              void *stream) {
+    if (!dst || !src || nx <= 0 || ny <= 0 || k_begin < 0 || k_end > nx || k_begin > k_end) {
+        set_error("lbgb_copy_rows: bad arguments (nx=%d ny=%d rows [%d, %d))", nx, ny, k_begin, k_end);
+        return LBGB_EINVAL;
+    }
+    const size_t es = raw_size(dtype);
+    if (es == 0) {
+        set_error("lbgb_copy_rows: unsupported storage code %d", dtype);
+        return LBGB_EDTYPE;
+    }
+    if (k_begin == k_end) return LBGB_OK;
+    const size_t pitch = (size_t)nx * ny * es, row = (size_t)ny * es, off = (size_t)k_begin * row;
+    // nine channel planes, rows [k_begin, k_end) of each: one strided copy
+    cudaError_t e = cudaMemcpy2DAsync(static_cast<char *>(dst) + off, pitch, static_cast<const char *>(src) + off, pitch,
+                                      (size_t)(k_end - k_begin) * row, 9, cudaMemcpyDefault, (cudaStream_t)stream);
+    if (e != cudaSuccess) {
+        set_error("lbgb_copy_rows: %s", cudaGetErrorString(e));
+        return LBGB_ECUDA;
+    }
+    return LBGB_OK;
+}
+
 extern "C" int lbgb_collide(void *f, int64_t n, int64_t chan_stride, int dtype, double omega, void *stream) {
     int rc = check_cells(f, n, chan_stride, dtype, "lbgb_collide");
     if (rc) return rc;

@@ -102,7 +102,7 @@ __global__ void __launch_bounds__((NCW_ + 1) * 32, 1)
 k_step_pipe(const typename Codec<DT>::raw *__restrict__ src, typename Codec<DT>::raw *__restrict__ dst, int nx,
             int ny, int tiles_per_row, int total_tiles, int stages, typename Codec<DT>::real omega,
             typename Codec<DT>::real u0, long long wait_limit, int stall_producer,
-            const unsigned long long *__restrict__ sr_step, uint32_t sr_seed) {
+            const unsigned long long *__restrict__ sr_step, uint32_t sr_seed, int k_first) {
     using C = Codec<DT>;
     using raw = typename C::raw;
     using real = typename C::real;
@@ -141,8 +141,8 @@ k_step_pipe(const typename Codec<DT>::raw *__restrict__ src, typename Codec<DT>:
                 pipe_report(1);
                 break;
             }
-            const int k = tile / tiles_per_row;
-            const int l0 = (tile - k * tiles_per_row) * L;
+            const int k = k_first + tile / tiles_per_row;
+            const int l0 = (tile - (k - k_first) * tiles_per_row) * L;
             const int c0 = max(l0 - HALO, 0), c1 = min(l0 + L + HALO, ny);
             const uint32_t bytes = (uint32_t)(c1 - c0) * (uint32_t)sizeof(raw);
             mbar_arrive_expect_tx(&full[s], 9u * bytes);
@@ -177,8 +177,8 @@ k_step_pipe(const typename Codec<DT>::raw *__restrict__ src, typename Codec<DT>:
             pipe_report(2);
             break;
         }
-        const int k = tile / tiles_per_row;
-        const int l0 = (tile - k * tiles_per_row) * L;
+        const int k = k_first + tile / tiles_per_row;
+        const int l0 = (tile - (k - k_first) * tiles_per_row) * L;
         const int c = l0 + t * NC;  // first cell of this thread
         const bool act = c < ny;
         const raw *stage = slots + (size_t)s * 9 * SLOT;

@@ -216,12 +216,13 @@ template <int DT, int BC, bool COLLIDE, int V>
 __global__ void __launch_bounds__(256, min_blocks<DT, V>())
 k_step(const typename Codec<DT>::raw *__restrict__ src, typename Codec<DT>::raw *__restrict__ dst, int nx,
        int ny, int segs, long long tasks, typename Codec<DT>::real omega, typename Codec<DT>::real u0,
-       const unsigned long long *__restrict__ sr_step, uint32_t sr_seed) {
+       const unsigned long long *__restrict__ sr_step, uint32_t sr_seed, int k_first) {
     const int lane = threadIdx.x & 31;
     const long long nwarps = ((long long)gridDim.x * blockDim.x) >> 5;
     for (long long t = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5; t < tasks; t += nwarps) {
-        const int k = (int)(t / segs);
-        const int l0 = (int)(t - (long long)k * segs) * (32 * V) + lane * V;
+        const int kr = (int)(t / segs);
+        const int k = k_first + kr;
+        const int l0 = (int)(t - (long long)kr * segs) * (32 * V) + lane * V;
         step_segment<DT, BC, COLLIDE, V>(src, dst, nx, ny, k, l0, lane, omega, u0, sr_step, sr_seed, 0u);
     }
 }
@@ -243,13 +244,20 @@ struct SR {
     uint32_t seed = 0;
 };
 
+// Rows [first, first + count) of the lattice to update (count < 0: all).
+struct Rows {
+    int first = 0;
+    int count = -1;
+    int n(int nx) const { return count < 0 ? nx : count; }
+};
+
 template <int DT, int BC, bool COLLIDE, int V>
 static int launch_v(const void *src, void *dst, int nx, int ny, double omega, double u0, cudaStream_t s,
-                    SR sr = SR()) {
+                    SR sr = SR(), Rows rows = Rows()) {
     using C = Codec<DT>;
     const int threads = 256;
     const int segs = (ny + 32 * V - 1) / (32 * V);
-    const long long tasks = (long long)nx * segs;
+    const long long tasks = (long long)rows.n(nx) * segs;
     const long long warps_per_block = threads / 32;
     long long blocks = (tasks + warps_per_block - 1) / warps_per_block;
     // at most 16 resident-size waves of blocks; the rest is grid-stride
@@ -257,7 +265,7 @@ static int launch_v(const void *src, void *dst, int nx, int ny, double omega, do
     if (blocks > cap) blocks = cap;
     k_step<DT, BC, COLLIDE, V><<<(unsigned)blocks, threads, 0, s>>>(
         static_cast<const typename C::raw *>(src), static_cast<typename C::raw *>(dst), nx, ny, segs, tasks,
-        (typename C::real)omega, (typename C::real)u0, sr.step, sr.seed);
+        (typename C::real)omega, (typename C::real)u0, sr.step, sr.seed, rows.first);
     return check_launch("k_step");
 }
 
@@ -284,12 +292,12 @@ static int max_dyn_smem() {
 
 template <int DT, int BC, bool COLLIDE>
 static int launch_pipe(const void *src, void *dst, int nx, int ny, double omega, double u0, cudaStream_t s,
-                       SR sr) {
+                       SR sr, Rows rows) {
     using raw = typename Codec<DT>::raw;
     using SH = PipeShape<DT>;
     using G = PipeGeom<raw, SH::NCW, SH::NC>;
     const long long tpr = (ny + G::L - 1) / G::L;
-    const long long total = (long long)nx * tpr;
+    const long long total = (long long)rows.n(nx) * tpr;
     const int smax = max_dyn_smem();
     const int fit = (int)((smax - 256) / (G::STAGE_BYTES + 16));
     int stages = (int)g_tune.stages;
@@ -312,7 +320,7 @@ static int launch_pipe(const void *src, void *dst, int nx, int ny, double omega,
         kernel<<<grid, (SH::NCW + 1) * 32, smem, s>>>(
             static_cast<const raw *>(src), static_cast<raw *>(dst), nx, ny, (int)tpr, (int)total, stages,
             (typename Codec<DT>::real)omega, (typename Codec<DT>::real)u0, g_tune.wait_limit,
-            (int)g_tune.stall_producer, sr.step, sr.seed);
+            (int)g_tune.stall_producer, sr.step, sr.seed, rows.first);
         return LBGB_OK;
     };
     const int rc = srnd ? go(k_step_pipe<DT, BC, COLLIDE, SH::NCW, SH::NC, sizeof(raw) == 2 && COLLIDE>, 1)
@@ -326,28 +334,28 @@ static int launch_pipe(const void *src, void *dst, int nx, int ny, double omega,
 // vector width that divides ny and keeps every row start aligned.
 template <int DT, int BC, bool COLLIDE>
 static int launch(const void *src, void *dst, int nx, int ny, double omega, double u0, cudaStream_t s,
-                  SR sr = SR()) {
+                  SR sr = SR(), Rows rows = Rows()) {
     constexpr int VW = 16 / sizeof(typename Codec<DT>::raw);
     const bool vec_ok = ny % VW == 0 && aligned(src, 16) && aligned(dst, 16);
     const bool want_pipe = g_tune.kernel == 2 ||
                            (g_tune.kernel == 0 && (long long)nx * ny >= g_tune.pipe_min_cells);
     if (vec_ok && want_pipe) {
-        const int rc = launch_pipe<DT, BC, COLLIDE>(src, dst, nx, ny, omega, u0, s, sr);
+        const int rc = launch_pipe<DT, BC, COLLIDE>(src, dst, nx, ny, omega, u0, s, sr, rows);
         if (rc <= 0) return rc;
     }
-    if (vec_ok) return launch_v<DT, BC, COLLIDE, VW>(src, dst, nx, ny, omega, u0, s, sr);
-    return launch_v<DT, BC, COLLIDE, 1>(src, dst, nx, ny, omega, u0, s, sr);
+    if (vec_ok) return launch_v<DT, BC, COLLIDE, VW>(src, dst, nx, ny, omega, u0, s, sr, rows);
+    return launch_v<DT, BC, COLLIDE, 1>(src, dst, nx, ny, omega, u0, s, sr, rows);
 }
 
 template <int BC, bool COLLIDE>
 static int dispatch(const void *src, void *dst, int nx, int ny, int dtype, double omega, double u0,
-                    cudaStream_t s, SR sr = SR()) {
+                    cudaStream_t s, SR sr = SR(), Rows rows = Rows()) {
     switch (dtype) {
-    case LBGB_F32: return launch<LBGB_F32, BC, COLLIDE>(src, dst, nx, ny, omega, u0, s);
-    case LBGB_F64: return launch<LBGB_F64, BC, COLLIDE>(src, dst, nx, ny, omega, u0, s);
-    case LBGB_F16DEV: return launch<LBGB_F16DEV, BC, COLLIDE>(src, dst, nx, ny, omega, u0, s, sr);
-    case LBGB_BF16DEV: return launch<LBGB_BF16DEV, BC, COLLIDE>(src, dst, nx, ny, omega, u0, s, sr);
-    case LBGB_F32DEV: return launch<LBGB_F32DEV, BC, COLLIDE>(src, dst, nx, ny, omega, u0, s);
+    case LBGB_F32: return launch<LBGB_F32, BC, COLLIDE>(src, dst, nx, ny, omega, u0, s, SR(), rows);
+    case LBGB_F64: return launch<LBGB_F64, BC, COLLIDE>(src, dst, nx, ny, omega, u0, s, SR(), rows);
+    case LBGB_F16DEV: return launch<LBGB_F16DEV, BC, COLLIDE>(src, dst, nx, ny, omega, u0, s, sr, rows);
+    case LBGB_BF16DEV: return launch<LBGB_BF16DEV, BC, COLLIDE>(src, dst, nx, ny, omega, u0, s, sr, rows);
+    case LBGB_F32DEV: return launch<LBGB_F32DEV, BC, COLLIDE>(src, dst, nx, ny, omega, u0, s, SR(), rows);
     default: set_error("unsupported storage code %d", dtype); return LBGB_EDTYPE;
     }
 }
@@ -412,6 +420,25 @@ extern "C" int lbgb_step_fused(const void *src, void *dst, int nx, int ny, int b
     if (boundary == LBGB_CAVITY_LADD)
         return dispatch<LBGB_CAVITY_LADD, true>(src, dst, nx, ny, dtype, omega, u0, (cudaStream_t)stream);
     return dispatch<LBGB_PERIODIC, true>(src, dst, nx, ny, dtype, omega, 0.0, (cudaStream_t)stream);
+}
+
+extern "C" int lbgb_step_fused_rows(const void *src, void *dst, int nx, int ny, int k_begin, int k_end,
+                                    int boundary, double omega, double u0, int dtype, void *stream) {
+    int rc = check_grid(src, dst, nx, ny, dtype, boundary, "lbgb_step_fused_rows");
+    if (rc) return rc;
+    if (k_begin < 0 || k_end > nx || k_begin > k_end) {
+        set_error("lbgb_step_fused_rows: rows [%d, %d) outside [0, %d)", k_begin, k_end, nx);
+        return LBGB_EINVAL;
+    }
+    if (k_begin == k_end) return LBGB_OK;
+    Rows rows;
+    rows.first = k_begin;
+    rows.count = k_end - k_begin;
+    cudaStream_t s = (cudaStream_t)stream;
+    if (boundary == LBGB_CAVITY) return dispatch<LBGB_CAVITY, true>(src, dst, nx, ny, dtype, omega, u0, s, SR(), rows);
+    if (boundary == LBGB_CAVITY_LADD)
+        return dispatch<LBGB_CAVITY_LADD, true>(src, dst, nx, ny, dtype, omega, u0, s, SR(), rows);
+    return dispatch<LBGB_PERIODIC, true>(src, dst, nx, ny, dtype, omega, 0.0, s, SR(), rows);
 }
 
 extern "C" int lbgb_run_fused(void *a, void *b, int nx, int ny, int boundary, double omega, double u0, int dtype,

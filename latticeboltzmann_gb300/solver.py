@@ -211,6 +211,63 @@ class Lattice:
                   self.cells, self._stream())
         return out
 
+    # ------------------------------------------------------------------ host-resident populations
+    def step_host(self, f, n=1, blocks=16):
+        """Advance populations that live in host memory by ``n`` steps, in place.
+
+        ``f``: a pinned, contiguous ``(9, nx, ny)`` host tensor of the storage's
+        dtype (f32 or f64 storage).  Each step copies f to the device, steps
+        and copies the result back -- what the reference's drivers do with
+        their host array every step -- but by blocks of rows on three streams,
+        so that the upload of block j+1, the update of block j and the
+        download of block j-1 overlap (the host link carries both directions
+        at once).  Block 0 is updated last: its rows read the last row across
+        the periodic seam (and the lid density does at the corners).  The
+        device state ends up holding the same populations as ``f``.
+        """
+        if self.storage not in ("f32", "f64"):
+            raise ValueError("step_host needs f32 or f64 storage (the host array holds the populations as they are)")
+        if (not isinstance(f, torch.Tensor) or f.device.type != "cpu" or not f.is_pinned() or not f.is_contiguous()
+                or f.dtype != self.state.dtype or tuple(f.shape) != (9, self.nx, self.ny)):
+            raise ValueError("step_host: f must be a pinned, contiguous %s tensor of shape %s" % (
+                self.state.dtype, (9, self.nx, self.ny)))
+        nx, ny = self.nx, self.ny
+        nb = max(1, min(int(blocks), nx))
+        edges = [nx * j // nb for j in range(nb + 1)]
+        if not hasattr(self, "_hstreams"):
+            self._hstreams = (torch.cuda.Stream(self.device), torch.cuda.Stream(self.device))
+        s_in, s_out = self._hstreams
+        s_cmp = torch.cuda.current_stream(self.device)
+        order = list(range(1, nb)) + [0]
+        ev = lambda: torch.cuda.Event()
+        for _ in range(int(n)):
+            a, b = self._buf[self._cur], self._buf[1 - self._cur]
+            s_in.wait_stream(s_cmp)
+            s_in.wait_stream(s_out)
+            ev_in = []
+            for j in range(nb):
+                _lib.call("lbgb_copy_rows", a.data_ptr(), f.data_ptr(), nx, ny, edges[j], edges[j + 1], self.code,
+                          s_in.cuda_stream)
+                e = ev()
+                e.record(s_in)
+                ev_in.append(e)
+            ev_out = []
+            for j in order:
+                # rows of blocks j-1, j, j+1 (with wrap) must be on the device
+                need = max(j + 1 if j + 1 < nb else 0, j, j - 1 if j > 0 else nb - 1)
+                s_cmp.wait_event(ev_in[need])
+                _lib.call("lbgb_step_fused_rows", a.data_ptr(), b.data_ptr(), nx, ny, edges[j], edges[j + 1],
+                          self.bcode, self.omega, self.u0, self.code, s_cmp.cuda_stream)
+                e = ev()
+                e.record(s_cmp)
+                s_out.wait_event(e)
+                _lib.call("lbgb_copy_rows", f.data_ptr(), b.data_ptr(), nx, ny, edges[j], edges[j + 1], self.code,
+                          s_out.cuda_stream)
+            self._cur = 1 - self._cur
+            self.steps_taken += 1
+        s_cmp.wait_stream(s_out)
+        return f
+
     # ------------------------------------------------------------------ stepping
     def step(self, n=1):
         """Advance ``n`` time steps (one fused launch each)."""

@@ -114,3 +114,34 @@ def test_full_size_cavity_properties(cuda, storage):
     # y momentum is zero in exact arithmetic; 16-bit rounding of the six
     # channels with cy != 0 repeats in every lid column: <= n * 6 * 2^-17
     assert abs(py) < (1e-3 if fp32 else n * 6 * 2.0 ** -17)
+
+
+@pytest.mark.parametrize("storage", ["f32", "f64"])
+@pytest.mark.parametrize("boundary", ["cavity", "cavity-ladd", "periodic"])
+@pytest.mark.parametrize("nx,ny,blocks", [(64, 96, 5), (37, 40, 16), (3, 8, 16), (130, 2048, 7), (8, 8, 1)])
+def test_step_host_equals_device_step(cuda, storage, boundary, nx, ny, blocks):
+    """The pipelined host step (row blocks, three streams) gives the populations
+    of the fused device step bit for bit, and leaves the device state equal."""
+    rng = np.random.default_rng(nx + ny)
+    f0 = oracle.equilibrium(1 + 0.01 * rng.standard_normal((nx, ny)), 0.03 * rng.standard_normal((nx, ny)),
+                            0.03 * rng.standard_normal((nx, ny)))
+    dt = torch.float32 if storage == "f32" else torch.float64
+    a = PyLB.Lattice(nx, ny, 1.3, boundary=boundary, u0=0.07, storage=storage, device=cuda).load(torch.from_numpy(f0))
+    b = PyLB.Lattice(nx, ny, 1.3, boundary=boundary, u0=0.07, storage=storage, device=cuda).load(torch.from_numpy(f0))
+    host = torch.from_numpy(f0).to(dt).pin_memory()
+    a.step(3)
+    b.step_host(host, n=3, blocks=blocks)
+    torch.cuda.synchronize()
+    assert torch.equal(host, a.state.cpu())
+    assert torch.equal(b.state, a.state)
+    assert b.steps_taken == 3
+
+
+def test_step_host_rejects_bad_buffers(cuda):
+    lat = PyLB.Lattice(16, 16, 1.0, storage="f32", device=cuda)
+    with pytest.raises(ValueError):
+        lat.step_host(torch.zeros(9, 16, 16))  # not pinned
+    with pytest.raises(ValueError):
+        lat.step_host(torch.zeros(9, 16, 16, dtype=torch.float64).pin_memory())
+    with pytest.raises(ValueError):
+        PyLB.Lattice(16, 16, 1.0, storage="f16dev", device=cuda).step_host(torch.zeros(9, 16, 16).pin_memory())
