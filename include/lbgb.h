@@ -248,6 +248,18 @@ LBGB_API int lbgb_row_fft_amplitude(const void *f, int nx, int ny, int row, int 
 LBGB_API int lbgb_wall_bounce_back(void *f, int nx, int ny, double uw, int interior, int clear, int dtype,
                                    void *stream);
 
+/* Resting solid nodes of any shape, given as a byte mask solid[k * ny + l]
+ * (nonzero = solid): after a push stream, every population that entered a
+ * solid node returns to the fluid node it came from in the opposite
+ * direction (link-wise dry-node bounce-back), in place.  periodic != 0 wraps
+ * the neighbours.  For rows of solid nodes this equals the scripts' wall
+ * reflection wherever the flow is uniform along the wall; the scripts copy
+ * diagonals within the same column (PoiseuilleFlow.py:59-75), the obstacle
+ * channel around a rectangle (experimantal_flows/obstacle_canal.py:413-458).
+ * dtype LBGB_F32 or LBGB_F64. */
+LBGB_API int lbgb_solid_bounce_back(void *f, const void *solid, int nx, int ny, int periodic, int dtype,
+                                    void *stream);
+
 /* Pressure-periodic inlet/outlet ghost columns, in place: column 0 becomes
  * f^eq(rho_in, u of column nx-2) + (f - f^eq) of column nx-2, column nx-1
  * becomes f^eq(rho_out, u of column 1) + (f - f^eq) of column 1.

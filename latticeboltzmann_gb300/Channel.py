@@ -18,8 +18,8 @@ import torch
 from . import _lib
 from ._tensor import lattice, storage_code, stream_handle
 
-__all__ = ["bounce_back", "pressure_periodic", "couette_flow", "poiseuille_flow", "couette_profile",
-           "poiseuille_profile"]
+__all__ = ["bounce_back", "solid_bounce_back", "pressure_periodic", "couette_flow", "poiseuille_flow",
+           "couette_profile", "poiseuille_profile"]
 
 
 def bounce_back(f, uw=0.0, interior=True, clear=False):
@@ -33,6 +33,24 @@ def bounce_back(f, uw=0.0, interior=True, clear=False):
     code = storage_code(f, "bounce_back")
     _lib.call("lbgb_wall_bounce_back", f.data_ptr(), nx, ny, float(uw), int(bool(interior)), int(bool(clear)),
               code, stream_handle(f))
+
+
+def solid_bounce_back(f, solid, periodic=True):
+    """Return every population that streamed into a solid node to the fluid
+    node it came from, reversed (link-wise dry-node bounce-back), in place.
+
+    ``solid``: a CUDA bool/uint8 tensor (nx, ny), nonzero where the node is
+    solid (an obstacle, or walls of any shape).  The obstacle channel of the
+    reference (experimantal_flows/obstacle_canal.py:413-458) reflects around a
+    rectangle the same way, copying diagonals within one column.
+    """
+    nx, ny = lattice(f, "solid_bounce_back")
+    code = storage_code(f, "solid_bounce_back")
+    if not isinstance(solid, torch.Tensor) or solid.device != f.device or tuple(solid.shape) != (nx, ny):
+        raise ValueError("solid_bounce_back: solid must be an (nx, ny) tensor on the populations' device")
+    m = solid.to(torch.uint8).contiguous()
+    _lib.call("lbgb_solid_bounce_back", f.data_ptr(), m.data_ptr(), nx, ny, int(bool(periodic)), code,
+              stream_handle(f))
 
 
 def pressure_periodic(f, rho_in, rho_out):

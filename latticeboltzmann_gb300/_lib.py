@@ -62,6 +62,7 @@ SIGNATURES = {
     "lbgb_batch_velocity_change": (_I, [_P, ctypes.c_longlong, _P, _I, _I, _P, ctypes.c_longlong, _P, _P, _P]),
     "lbgb_row_fft_amplitude": (_I, [_P, _I, _I, _I, _I, _P, _P]),
     "lbgb_wall_bounce_back": (_I, [_P, _I, _I, ctypes.c_double, _I, _I, _I, _P]),
+    "lbgb_solid_bounce_back": (_I, [_P, _P, _I, _I, _I, _I, _P]),
     "lbgb_pressure_periodic": (_I, [_P, _I, _I, ctypes.c_double, ctypes.c_double, _I, _P]),
     "lbgb_chapman_enskog": (_I, [_P, _P, _P, _P, _I, _I, ctypes.c_double, ctypes.c_double, _I, _I, _I, _P]),
     "lbgb_gemm_bf16": (_I, [_I, _I, _I, _P, ctypes.c_longlong, ctypes.c_longlong, ctypes.c_longlong, _P,

@@ -521,6 +521,15 @@ __device__ __forceinline__ void collide_encode_sr(float (&f)[9], float omega, un
 void set_error(const char *fmt, ...);
 int check_launch(const char *what);
 
+// Current device, clamped into [0, MAX_DEVICES) for per-device host caches
+// (kernel attributes and device properties are per device).
+constexpr int MAX_DEVICES = 64;
+inline int current_device() {
+    int d = 0;
+    if (cudaGetDevice(&d) != cudaSuccess || d < 0) d = 0;
+    return d < MAX_DEVICES ? d : MAX_DEVICES - 1;
+}
+
 inline bool aligned(const void *p, size_t a) { return (reinterpret_cast<uintptr_t>(p) % a) == 0; }
 
 inline size_t raw_size(int dt) {

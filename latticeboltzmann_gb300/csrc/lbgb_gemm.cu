@@ -329,11 +329,13 @@ k_gemm_simt(int M, int N, int K, const __nv_bfloat16 *__restrict__ A, long long 
 // Dynamic shared memory of one tensor-core GEMM variant: the staging area
 // (a [k][row] tile, or the epilogue's 4 x 32 x 17 floats), grown until the
 // CTAs that fit on one SM hold at most the SM's 512 tensor-memory columns, so
-// that no allocation ever waits.  Computed once per variant.
+// that no allocation ever waits.  Computed once per variant and device.
 template <int NT, typename OUT, int KB>
 static int tc_dyn_smem() {
-    static int dyn = -1;
-    if (dyn >= 0) return dyn;
+    static int cache[MAX_DEVICES];
+    static bool have[MAX_DEVICES] = {};
+    const int dev = current_device();
+    if (have[dev]) return cache[dev];
     int d = KB * TC_M * 2;
     if (d < 4 * 32 * 17 * 4) d = 4 * 32 * 17 * 4;
     for (;;) {
@@ -343,7 +345,8 @@ static int tc_dyn_smem() {
         if (nb * NT <= 512 || d >= 200 * 1024) break;
         d += 1024;
     }
-    dyn = d;
+    cache[dev] = d;
+    have[dev] = true;
     return d;
 }
 

@@ -245,6 +245,33 @@ __global__ void k_wall_bounce_back(T *__restrict__ f, int nx, int ny, T uw6, int
     }
 }
 
+// Solid nodes of any shape (a mask), link-wise: after a push stream, the
+// population f_i found at a solid node x came from y = x - c_i; if y is fluid
+// it returns there as f_opp(i)(y).  Each (y, opp(i)) has one source, solid
+// nodes are only read and fluid nodes only written, so one thread per node
+// needs no ordering.
+template <class T>
+__global__ void k_solid_bounce_back(T *__restrict__ f, const unsigned char *__restrict__ solid, int nx, int ny,
+                                    int periodic) {
+    const int64_t n = (int64_t)nx * ny;
+    for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < n; c += (int64_t)gridDim.x * blockDim.x) {
+        if (!solid[c]) continue;
+        const int k = (int)(c / ny), l = (int)(c - (int64_t)k * ny);
+#pragma unroll
+        for (int i = 1; i < 9; ++i) {
+            int ks = k - cx(i), ls = l - cy(i);
+            if (periodic) {
+                ks = ks < 0 ? ks + nx : (ks >= nx ? ks - nx : ks);
+                ls = ls < 0 ? ls + ny : (ls >= ny ? ls - ny : ls);
+            } else if (ks < 0 || ks >= nx || ls < 0 || ls >= ny) {
+                continue;
+            }
+            const int64_t y = (int64_t)ks * ny + ls;
+            if (!solid[y]) f[opp(i) * n + y] = f[i * n + c];
+        }
+    }
+}
+
 // Pressure-periodic ghost columns: x = 0 takes the equilibrium at rho_in with
 // the velocity of column nx-2 plus that column's non-equilibrium part; x =
 // nx-1 the same with rho_out and column 1.  One thread per row; every input
@@ -502,6 +529,26 @@ extern "C" int lbgb_wall_bounce_back(void *f, int nx, int ny, double uw, int int
         return LBGB_EDTYPE;
     }
     return check_launch("k_wall_bounce_back");
+}
+
+extern "C" int lbgb_solid_bounce_back(void *f, const void *solid, int nx, int ny, int periodic, int dtype,
+                                      void *stream) {
+    if (!f || !solid || nx <= 0 || ny <= 0) {
+        set_error("lbgb_solid_bounce_back: bad arguments (nx=%d ny=%d)", nx, ny);
+        return LBGB_EINVAL;
+    }
+    const int64_t n = (int64_t)nx * ny;
+    cudaStream_t s = (cudaStream_t)stream;
+    const auto *m = static_cast<const unsigned char *>(solid);
+    if (dtype == LBGB_F32)
+        k_solid_bounce_back<float><<<grid_for(n, 256), 256, 0, s>>>((float *)f, m, nx, ny, periodic);
+    else if (dtype == LBGB_F64)
+        k_solid_bounce_back<double><<<grid_for(n, 256), 256, 0, s>>>((double *)f, m, nx, ny, periodic);
+    else {
+        set_error("lbgb_solid_bounce_back: storage code %d not supported (F32 or F64)", dtype);
+        return LBGB_EDTYPE;
+    }
+    return check_launch("k_solid_bounce_back");
 }
 
 extern "C" int lbgb_pressure_periodic(void *f, int nx, int ny, double rho_in, double rho_out, int dtype,

@@ -229,14 +229,14 @@ k_step(const typename Codec<DT>::raw *__restrict__ src, typename Codec<DT>::raw 
 
 // ---------------------------------------------------------------- launch
 static int sm_count() {
-    static int n = 0;
-    if (n == 0) {
-        int dev = 0;
-        cudaGetDevice(&dev);
+    static int cache[MAX_DEVICES] = {};
+    const int dev = current_device();
+    if (cache[dev] == 0) {
+        int n = 0;
         cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
-        if (n <= 0) n = 1;
+        cache[dev] = n > 0 ? n : 1;
     }
-    return n;
+    return cache[dev];
 }
 
 struct SR {
@@ -280,14 +280,14 @@ struct Tuning {
 static Tuning g_tune;
 
 static int max_dyn_smem() {
-    static int v = 0;
-    if (v == 0) {
-        int dev = 0;
-        cudaGetDevice(&dev);
+    static int cache[MAX_DEVICES] = {};
+    const int dev = current_device();
+    if (cache[dev] == 0) {
+        int v = 0;
         cudaDeviceGetAttribute(&v, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
-        if (v <= 0) v = 48 * 1024;
+        cache[dev] = v > 0 ? v : 48 * 1024;
     }
-    return v;
+    return cache[dev];
 }
 
 template <int DT, int BC, bool COLLIDE>
@@ -306,16 +306,17 @@ static int launch_pipe(const void *src, void *dst, int nx, int ny, double omega,
     const size_t smem = (size_t)stages * G::STAGE_BYTES + 16 * (size_t)stages;
     const int grid = (int)(total < sm_count() ? total : sm_count());
     const bool srnd = sizeof(raw) == 2 && COLLIDE && sr.step != nullptr;
-    // the dynamic shared-memory limit is raised once per kernel variant
-    static bool attr_set[2] = {false, false};
+    // the dynamic shared-memory limit is raised once per kernel variant and device
+    static bool attr_set[MAX_DEVICES][2] = {};
+    const int dev = current_device();
     auto go = [&](auto kernel, int variant) -> int {
-        if (!attr_set[variant]) {
+        if (!attr_set[dev][variant]) {
             cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smax);
             if (e != cudaSuccess) {
                 set_error("k_step_pipe: cannot reserve %d bytes of shared memory: %s", smax, cudaGetErrorString(e));
                 return LBGB_ECUDA;
             }
-            attr_set[variant] = true;
+            attr_set[dev][variant] = true;
         }
         kernel<<<grid, (SH::NCW + 1) * 32, smem, s>>>(
             static_cast<const raw *>(src), static_cast<raw *>(dst), nx, ny, (int)tpr, (int)total, stages,

@@ -88,3 +88,22 @@ def couette_step_cleared(f, omega, uw):
     d2q9.collide(f, omega)
     bounce_back_walls(f, uw, interior=False, clear=True)
     return f
+
+
+def solid_bounce_back(f, solid, periodic=True):
+    """Link-wise dry-node bounce-back around solid nodes (a boolean (nx, ny)
+    mask), in place: f_opp(i)(x - c_i) <- f_i(x) for solid x and fluid x - c_i.
+    (A generalisation of the scripts' wall and obstacle reflections, which copy
+    diagonals within one column; for rows of solid nodes and flow uniform along
+    them the two agree.)"""
+    _, nx, ny = f.shape
+    src = f.copy()
+    for k, l in zip(*np.nonzero(solid)):
+        for i in range(1, 9):
+            ks, ls = k - int(d2q9.CX[i]), l - int(d2q9.CY[i])
+            if periodic:
+                ks, ls = ks % nx, ls % ny
+            elif not (0 <= ks < nx and 0 <= ls < ny):
+                continue
+            if not solid[ks, ls]:
+                f[d2q9.OPP[i], ks, ls] = src[i, k, l]
