@@ -145,3 +145,29 @@ def test_step_host_rejects_bad_buffers(cuda):
         lat.step_host(torch.zeros(9, 16, 16, dtype=torch.float64).pin_memory())
     with pytest.raises(ValueError):
         PyLB.Lattice(16, 16, 1.0, storage="f16dev", device=cuda).step_host(torch.zeros(9, 16, 16).pin_memory())
+
+
+@pytest.mark.parametrize("storage", ["bf16dev", "f16dev"])
+def test_16bit_storage_at_16384(cuda, storage):
+    """16-bit storage at the 16384^2 grid of the precision study (two 4.8 GB
+    buffers): the rest state is an exact fixed point, and one step from rest
+    with the wall-density-1 lid conserves mass to the rounding of one rest
+    population per lid cell and moves x momentum 2 u0/6 per lid cell."""
+    n = 16384
+    lat = PyLB.Lattice(n, n, 1.7, boundary="cavity-ladd", u0=0.0, storage=storage, device=cuda)
+    s0 = lat.state.clone()
+    lat.step(2)
+    assert torch.equal(lat.state, s0)
+    del s0, lat
+    u0 = 0.1
+    lat = PyLB.Lattice(n, n, 1.7, boundary="cavity-ladd", u0=u0, storage=storage, device=cuda)
+    m0 = float(lat.mass_momentum()[0])
+    lat.step(1)
+    mass, px, py = lat.mass_momentum().cpu().numpy()
+    # FP16 keeps each node's mass up to the rounding of its rest population
+    # (|h_0| < 2^-5: half an ulp is 2^-16 unscaled); bfloat16 (8 bits, no
+    # mass fix) rounds every changed population of a lid cell (|h| < 2^-5)
+    half_ulp = 2.0 ** -16 if storage == "f16dev" else 9 * 2.0 ** -14
+    assert abs(mass - m0) < n * half_ulp
+    assert abs(px - u0 / 3 * n) < (2e-3 if storage == "f16dev" else 1e-2) * u0 / 3 * n
+    assert abs(py) < n * 6 * (2.0 ** -17 if storage == "f16dev" else 2.0 ** -13)
