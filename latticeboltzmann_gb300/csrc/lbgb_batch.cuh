@@ -116,18 +116,26 @@ k_batch_step_flat(const typename Codec<DT>::raw *__restrict__ src, typename Code
         const long long n = (long long)in.nx * in.ny;
         if (in.nx <= 0 || in.ny <= 0 || in.offset < 0 || in.offset + 9 * n > total_elems) continue;
         if (BC != LBGB_PERIODIC && (in.nx < 2 || in.ny < 2)) continue;
+        if (tk.z < 0) continue;
         const raw *s = src + in.offset;
         raw *d = dst + in.offset;
-        for (int r = 0; r < rounds; ++r) {
-            const long long c = (long long)tk.z + 32ll * r + lane;
-            if (tk.z < 0 || c >= n) break;
-            const int k = (int)(c / in.ny), l = (int)(c - (long long)k * in.ny);
+        // cell c -> (k, l) by one division for the first round, then stepped
+        // by 32 cells per round (no 64-bit division per cell)
+        long long c = (long long)tk.z + lane;
+        int k = (int)(c / in.ny), l = (int)(c - (long long)k * in.ny);
+        for (int r = 0; r < rounds && c < n; ++r) {
             real v[9];
             pull_cell<C, BC>(s, in.nx, in.ny, k, l, (real)in.u0, v);
             raw out[9];
             collide_encode<DT>(v, (real)in.omega, out);
 #pragma unroll
             for (int i = 0; i < 9; ++i) d[i * n + c] = out[i];
+            c += 32;
+            l += 32;
+            while (l >= in.ny) {
+                l -= in.ny;
+                ++k;
+            }
         }
     }
 }
