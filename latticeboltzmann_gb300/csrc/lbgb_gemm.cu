@@ -236,15 +236,21 @@ k_gemm_tc(int M, int N, int K, const __nv_bfloat16 *__restrict__ A, long long a_
 #pragma unroll
             for (int j = 0; j < 16; ++j) ostage[lane * 17 + j] = __uint_as_float(v[j]);
             __syncwarp();
-#pragma unroll 4
+            // the 16 old values of C (beta != 0) are all requested before any
+            // is used, so their latencies overlap
+            const int j = lane & 15, col = n0 + c0 + j;
+            float old[16];
+#pragma unroll
             for (int i = 0; i < 16; ++i) {
-                const int r = 2 * i + (lane >> 4), j = lane & 15;
-                const int row = m0 + warp * 32 + r, col = n0 + c0 + j;
-                if (row < M && col < N) {
-                    OUT *cp = C + (long long)row * c_rs + col;
-                    const float acc = ostage[r * 17 + j];
-                    store_out(cp, beta == 0.f ? alpha * acc : alpha * acc + beta * load_out(cp));
-                }
+                const int row = m0 + warp * 32 + 2 * i + (lane >> 4);
+                old[i] = (beta != 0.f && row < M && col < N) ? load_out(C + (long long)row * c_rs + col) : 0.f;
+            }
+#pragma unroll
+            for (int i = 0; i < 16; ++i) {
+                const int r = 2 * i + (lane >> 4);
+                const int row = m0 + warp * 32 + r;
+                if (row < M && col < N)
+                    store_out(C + (long long)row * c_rs + col, alpha * ostage[r * 17 + j] + beta * old[i]);
             }
             __syncwarp();
         }
@@ -264,14 +270,19 @@ k_gemm_tc(int M, int N, int K, const __nv_bfloat16 *__restrict__ A, long long a_
                 : "r"(taddr));
             asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
             if (row < M) {
+                float old[16];
 #pragma unroll
                 for (int j = 0; j < 16; ++j) {
                     const int col = n0 + c0 + j;
-                    if (col < N) {
-                        OUT *cp = C + (long long)row * c_rs + (long long)col * c_cs;
-                        const float acc = __uint_as_float(v[j]);
-                        store_out(cp, beta == 0.f ? alpha * acc : alpha * acc + beta * load_out(cp));
-                    }
+                    old[j] = (beta != 0.f && col < N) ? load_out(C + (long long)row * c_rs + (long long)col * c_cs)
+                                                      : 0.f;
+                }
+#pragma unroll
+                for (int j = 0; j < 16; ++j) {
+                    const int col = n0 + c0 + j;
+                    if (col < N)
+                        store_out(C + (long long)row * c_rs + (long long)col * c_cs,
+                                  alpha * __uint_as_float(v[j]) + beta * old[j]);
                 }
             }
         }
