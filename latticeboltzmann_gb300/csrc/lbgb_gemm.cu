@@ -133,20 +133,31 @@ __device__ __forceinline__ void load_tile(unsigned char *dst, const __nv_bfloat1
     }
 }
 
-template <int NT, typename OUT, int KB>
+// Bytes of dynamic shared memory a variant needs: its operand stages (A then
+// B, each stage 1024-byte aligned) and the staging area (a [k][row] tile of a
+// row-contiguous operand, or the epilogue's 4 x 32 x 17 floats).
+template <int NT, int KB, int ST>
+__host__ __device__ constexpr int tc_operand_bytes() { return ST * (TC_M + NT) * KB * 2; }
+template <int KB>
+__host__ __device__ constexpr int tc_stage_bytes() { return KB * TC_M * 2 > 8704 ? KB * TC_M * 2 : 8704; }
+
+template <int NT, typename OUT, int KB, int ST>
 __global__ void __launch_bounds__(128, 1)
 k_gemm_tc(int M, int N, int K, const __nv_bfloat16 *__restrict__ A, long long a_rs, long long a_cs, long long a_bs,
           const __nv_bfloat16 *__restrict__ B, long long b_rs, long long b_cs, long long b_bs, OUT *__restrict__ C,
           long long c_rs, long long c_cs, long long c_bs, float alpha, float beta) {
     static_assert(NT % 16 == 0 && NT >= 32 && NT <= 256, "tile N");
     static_assert(KB == 32 || KB == 64, "K block");
-    __shared__ __align__(1024) unsigned char sA[TC_M * KB * 2];
-    __shared__ __align__(1024) unsigned char sB[NT * KB * 2];
-    __shared__ __align__(8) uint64_t bar;
+    static_assert(ST == 1 || ST == 2, "stages");
+    constexpr int A_BYTES = TC_M * KB * 2, B_BYTES = NT * KB * 2;
+    // dynamic shared memory: ST stages of A, ST stages of B, then the staging
+    // area of row-contiguous operands and of row-major output
+    extern __shared__ __align__(1024) unsigned char dsm[];
+    unsigned char *sA0 = dsm;
+    unsigned char *sB0 = dsm + ST * A_BYTES;
+    unsigned short *stage = reinterpret_cast<unsigned short *>(dsm + tc_operand_bytes<NT, KB, ST>());
+    __shared__ __align__(8) uint64_t bar[2];
     __shared__ uint32_t tmem_slot;
-    // dynamic shared memory: the [k][row] staging tile of row-contiguous
-    // operands, and the staging of row-major output in the epilogue
-    extern __shared__ __align__(16) unsigned short stage[];
 
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const int m0 = blockIdx.x * TC_M, n0 = blockIdx.y * NT;
@@ -162,7 +173,8 @@ k_gemm_tc(int M, int N, int K, const __nv_bfloat16 *__restrict__ A, long long a_
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
     }
     if (tid == 0) {
-        mbar_init_g(&bar, 1);
+        mbar_init_g(&bar[0], 1);
+        mbar_init_g(&bar[1], 1);
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
@@ -171,11 +183,26 @@ k_gemm_tc(int M, int N, int K, const __nv_bfloat16 *__restrict__ A, long long a_
     const uint32_t tmem = tmem_slot;
     constexpr uint32_t idesc = umma_idesc_bf16(TC_M, NT);
 
-    uint32_t phase = 0;
+    // K blocks: block kb is staged in stage kb % ST and its MMAs commit to
+    // bar[kb % 2]; with two stages the loads of block kb overlap the MMAs of
+    // block kb-1, and a stage is refilled only after the MMAs of block kb-2
+    // (which read it) have completed.  Commits complete in order, so the last
+    // one completing means every MMA has.
     bool ok = true;
+    int issued = -1;
     const int kblocks = (K + KB - 1) / KB;
-    for (int kb = 0; kb < kblocks && ok; ++kb) {
+    for (int kb = 0; kb < kblocks; ++kb) {
+        const int st = ST == 2 ? (kb & 1) : 0;
+        if (kb >= ST) {
+            const int prev = kb - ST;  // the block whose MMAs read this stage last
+            const bool w = mbar_wait_g(&bar[prev & 1], (uint32_t)(prev >> 1) & 1u, TC_WAIT);
+            if (!w) atomicCAS(&g_gemm_status, 0, 1);
+            ok = __syncthreads_and(w) != 0;  // every thread leaves together if a wait gave up
+            if (!ok) break;
+            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        }
         const int k0 = kb * KB;
+        unsigned char *sA = sA0 + st * A_BYTES, *sB = sB0 + st * B_BYTES;
         // A tile: 128 rows x KB k; element (r, kk) at (r/8)*KB*16 + (kk/8)*128 + (r%8)*16 + (kk%8)*2
         load_tile<TC_M, KB>(sA, A, a_rs, a_cs, m0, M, k0, K, tid, stage);
         // B tile: NT rows (n) x KB k, same layout; B(k, n) = B[k * b_rs + n * b_cs]
@@ -199,20 +226,23 @@ k_gemm_tc(int M, int N, int K, const __nv_bfloat16 *__restrict__ A, long long a_
                     : "memory");
             }
             asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
-                             smem_u32(&bar))
+                             smem_u32(&bar[kb & 1]))
                          : "memory");
         }
-        if (!mbar_wait_g(&bar, phase, TC_WAIT)) {
+        issued = kb;
+    }
+    if (issued >= 0) {
+        // the last block's MMAs (bounded; on a timeout wait once more before
+        // the buffers and the tensor memory go away)
+        const bool w = mbar_wait_g(&bar[issued & 1], (uint32_t)(issued >> 1) & 1u, TC_WAIT);
+        if (!w) {
             atomicCAS(&g_gemm_status, 0, 1);
-            ok = false;
-            // the MMAs may still be running: wait again (bounded) before the
-            // buffers and the tensor memory go away
-            mbar_wait_g(&bar, phase, TC_WAIT);
+            mbar_wait_g(&bar[issued & 1], (uint32_t)(issued >> 1) & 1u, TC_WAIT);
         }
-        phase ^= 1u;
+        ok = __syncthreads_and(ok && w) != 0;
         asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-        // every thread leaves the loop together if any wait gave up
-        ok = __syncthreads_and(ok) != 0;
+    } else {
+        ok = false;  // K = 0 is handled on the host; nothing to read back
     }
 
     if (ok && c_cs == 1 && c_rs != 1) {
@@ -341,18 +371,18 @@ k_gemm_simt(int M, int N, int K, const __nv_bfloat16 *__restrict__ A, long long 
 // (a [k][row] tile, or the epilogue's 4 x 32 x 17 floats), grown until the
 // CTAs that fit on one SM hold at most the SM's 512 tensor-memory columns, so
 // that no allocation ever waits.  Computed once per variant and device.
-template <int NT, typename OUT, int KB>
+template <int NT, typename OUT, int KB, int ST>
 static int tc_dyn_smem() {
     static int cache[MAX_DEVICES];
     static bool have[MAX_DEVICES] = {};
     const int dev = current_device();
     if (have[dev]) return cache[dev];
-    int d = KB * TC_M * 2;
-    if (d < 4 * 32 * 17 * 4) d = 4 * 32 * 17 * 4;
+    int d = tc_operand_bytes<NT, KB, ST>() + tc_stage_bytes<KB>();
     for (;;) {
-        cudaFuncSetAttribute(k_gemm_tc<NT, OUT, KB>, cudaFuncAttributeMaxDynamicSharedMemorySize, d);
+        cudaFuncSetAttribute(k_gemm_tc<NT, OUT, KB, ST>, cudaFuncAttributeMaxDynamicSharedMemorySize, d);
         int nb = 0;
-        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_gemm_tc<NT, OUT, KB>, 128, d) != cudaSuccess) break;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_gemm_tc<NT, OUT, KB, ST>, 128, d) != cudaSuccess)
+            break;
         if (nb * NT <= 512 || d >= 200 * 1024) break;
         d += 1024;
     }
@@ -366,30 +396,36 @@ static int launch_gemm(int m, int n, int k, const __nv_bfloat16 *a, long long a_
                        const __nv_bfloat16 *b, long long b_rs, long long b_cs, long long b_bs, OUT *C, long long c_rs,
                        long long c_cs, long long c_bs, int batch, float alpha, float beta, int engine,
                        cudaStream_t s) {
-    if (engine == 1) {
+    if (engine == 1 || k == 0) {  // K = 0: C = beta C, no tensor-core work
         dim3 grid((m + 63) / 64, (n + 63) / 64, batch);
         k_gemm_simt<OUT><<<grid, 256, 0, s>>>(m, n, k, a, a_rs, a_cs, a_bs, b, b_rs, b_cs, b_bs, C, c_rs, c_cs, c_bs,
                                               alpha, beta);
         return check_launch("k_gemm_simt");
     }
-    // tensor cores: tile N 32/64/128 by problem width, K blocks of 32 when K
-    // is that small (most of the surrogate's products), else 64
+    // tensor cores: tile N 32/64/128 by problem width; K blocks of 32 when K
+    // is that small (most of the surrogate's products), else 64.  One operand
+    // stage: double-buffering the K blocks (ST = 2, the loads of block kb
+    // under the MMAs of kb-1) measured slower on the surrogate's products
+    // (training step 6.81 ms for K > 64, 6.75 ms for K > 192, 6.54 ms never)
+    // -- the larger shared-memory footprint costs more resident CTAs than the
+    // overlap gains.
     dim3 grid((m + TC_M - 1) / TC_M, 1, batch);
-#define LBGB_TC(NTV, KBV)                                                                                        \
+#define LBGB_TC(NTV, KBV, STV)                                                                                   \
     do {                                                                                                       \
         grid.y = (n + NTV - 1) / NTV;                                                                          \
-        const int dyn = tc_dyn_smem<NTV, OUT, KBV>();                                                          \
-        k_gemm_tc<NTV, OUT, KBV><<<grid, 128, dyn, s>>>(m, n, k, a, a_rs, a_cs, a_bs, b, b_rs, b_cs, b_bs, C, c_rs, \
-                                                        c_cs, c_bs, alpha, beta);                              \
+        const int dyn = tc_dyn_smem<NTV, OUT, KBV, STV>();                                                     \
+        k_gemm_tc<NTV, OUT, KBV, STV><<<grid, 128, dyn, s>>>(m, n, k, a, a_rs, a_cs, a_bs, b, b_rs, b_cs, b_bs, C, \
+                                                             c_rs, c_cs, c_bs, alpha, beta);                  \
     } while (0)
-    const bool k32 = k <= 32;
-    if (n <= 32) {
-        if (k32) LBGB_TC(32, 32); else LBGB_TC(32, 64);
-    } else if (n <= 64) {
-        if (k32) LBGB_TC(64, 32); else LBGB_TC(64, 64);
-    } else {
-        if (k32) LBGB_TC(128, 32); else LBGB_TC(128, 64);
-    }
+#define LBGB_TC_K(NTV)                                                                                         \
+    do {                                                                                                       \
+        if (k <= 32) LBGB_TC(NTV, 32, 1);                                                                      \
+        else LBGB_TC(NTV, 64, 1);                                                                              \
+    } while (0)
+    if (n <= 32) LBGB_TC_K(32);
+    else if (n <= 64) LBGB_TC_K(64);
+    else LBGB_TC_K(128);
+#undef LBGB_TC_K
 #undef LBGB_TC
     return check_launch("k_gemm_tc");
 }
@@ -407,7 +443,7 @@ extern "C" int lbgb_gemm_bf16(int m, int n, int k, const void *A, long long a_rs
         return LBGB_EINVAL;
     }
     if (m == 0 || n == 0) return LBGB_OK;
-    if (!A || !B || !C) {
+    if (!C || (k > 0 && (!A || !B))) {
         set_error("lbgb_gemm_bf16: null operand");
         return LBGB_EINVAL;
     }

@@ -71,3 +71,15 @@ def test_gemm_bf16_output_and_offsets(cuda, engine):
     _lib.call("lbgb_gemm_status", 1)
     assert (C32.double() - ref).abs().max().item() < 1e-4 * ref.abs().max().item()
     assert torch.equal(C16, C32.to(torch.bfloat16))
+
+
+@pytest.mark.parametrize("engine", [0, 1])
+def test_gemm_empty_inner_dimension(cuda, engine):
+    """K = 0: C = beta C (no tensor-core work is issued)."""
+    A = torch.zeros(64, 0, dtype=torch.bfloat16, device=cuda)
+    B = torch.zeros(0, 32, dtype=torch.bfloat16, device=cuda)
+    C = torch.full((64, 32), 3.0, device=cuda)
+    _lib.call("lbgb_gemm_bf16", 64, 32, 0, A.data_ptr(), 1, 1, 0, B.data_ptr(), 32, 1, 0, C.data_ptr(), 32, 1, 0, 1,
+              1.0, 0.5, 0, engine, torch.cuda.current_stream().cuda_stream)
+    _lib.call("lbgb_gemm_status", 1)
+    assert torch.all(C == 1.5)
