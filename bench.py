@@ -12,7 +12,8 @@ Lines printed (rank 0, one JSON line):
   e2e        MLUPS through the public API with the populations in pinned host
              memory: every step copies them host->device, runs the step, and
              copies them back, inside the timed region (Lattice.step_host:
-             the three overlap by blocks of rows)
+             the three overlap by blocks of rows); e2e.link is the ceiling
+             the host link sets, the same bytes copied both ways at once
   roofline   HBM roofline of the fused kernel: 72 B/cell/step (FP32) or
              36 B (16-bit deviations) over its CUDA-event launch time
   cpu_baseline  the oracle's C port of the reference step on the host cores
@@ -352,10 +353,15 @@ def run_ours(args):
         d.barrier()
         e_mlups, _ = aggregate_mlups(lat.cells, args.e2e_steps, el, d, dev)
         nbytes = host.numel() * host.element_size()
+        link_s = host_link_seconds(host, dev)
+        bound = lat.cells / link_s / 1e6
         e2e = {"value": round(e_mlups, 3), "unit": UNIT, "h2d_bytes_per_step": nbytes, "d2h_bytes_per_step": nbytes,
                "steps": args.e2e_steps,
                "path": "Lattice.step_host(pinned host): row blocks uploaded, updated and downloaded on three streams"
-               if host_path else "Lattice.load(pinned host) + Lattice.step + Lattice.populations(out=pinned host)"}
+               if host_path else "Lattice.load(pinned host) + Lattice.step + Lattice.populations(out=pinned host)",
+               "link": {"two_way_gbs": round(2 * nbytes / link_s / 1e9, 1), "bound": round(bound, 1),
+                        "frac": round(e_mlups / d.world / bound, 4),
+                        "how": "one step's upload and download as two concurrent copy-engine copies, no compute"}}
         del host
 
     if d.rank != 0:
@@ -388,6 +394,38 @@ def run_ours(args):
     print(json.dumps(line), flush=True)
     d.close()
     return 0
+
+
+def host_link_seconds(host, dev, reps=3):
+    """Seconds for one step's host traffic with nothing else running: the upload
+    of ``host`` and a download of the same size as two concurrent copies on
+    their own streams -- the ceiling of any per-step host round trip."""
+    import torch
+    scratch = torch.empty(host.shape, dtype=host.dtype, device=dev)
+    dev_buf = torch.empty_like(scratch)
+    back = torch.empty(host.shape, dtype=host.dtype, pin_memory=True)
+    s_up, s_down = torch.cuda.Stream(dev), torch.cuda.Stream(dev)
+    cur = torch.cuda.current_stream(dev)
+
+    def once():
+        s_up.wait_stream(cur)
+        s_down.wait_stream(cur)
+        with torch.cuda.stream(s_up):
+            scratch.copy_(host, non_blocking=True)
+        with torch.cuda.stream(s_down):
+            back.copy_(dev_buf, non_blocking=True)
+        cur.wait_stream(s_up)
+        cur.wait_stream(s_down)
+
+    once()
+    torch.cuda.synchronize(dev)
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        once()
+    torch.cuda.synchronize(dev)
+    el = (time.perf_counter() - t0) / reps
+    del scratch, dev_buf, back
+    return el
 
 
 def run_batched(args):

@@ -73,15 +73,44 @@ template <> struct Codec<LBGB_F32DEV> {
 constexpr float F16_SCALE = 16384.0f;
 constexpr float F16_UNSCALE = 1.0f / 16384.0f;
 
+// Mixed-precision FMA with 16-bit multiplicands (PTX fma.rn.f32.f16 and
+// fma.rn.f32.bf16, sm_100 and later): a b + c for 16-bit a, b and an FP32
+// addend, rounded once to FP32.  The result is the fmaf of the exactly
+// converted operands, in one instruction instead of a conversion and an FMA.
+constexpr unsigned short F16_UNSCALE_BITS = 0x0400;    // half 2^-14
+constexpr unsigned short F16_MINUS_ONE_BITS = 0xbc00;  // half -1
+constexpr unsigned short BF16_ONE_BITS = 0x3f80;       // bfloat16 1
+template <bool BF>
+__device__ __forceinline__ float fma16(unsigned short a, unsigned short b, float c) {
+    float d;
+    if constexpr (BF)
+        asm("fma.rn.f32.bf16 %0, %1, %2, %3;" : "=f"(d) : "h"(a), "h"(b), "f"(c));
+    else
+        asm("fma.rn.f32.f16 %0, %1, %2, %3;" : "=f"(d) : "h"(a), "h"(b), "f"(c));
+    return d;
+}
+// the two 16-bit values of a 32-bit word (low half first), each times b plus
+// its own addend
+template <bool BF>
+__device__ __forceinline__ void fma16x2(uint32_t a2, unsigned short b, float c_lo, float c_hi, float &lo,
+                                        float &hi) {
+    if constexpr (BF)
+        asm("{\n\t.reg .b16 l, h;\n\tmov.b32 {l, h}, %2;\n\t"
+            "fma.rn.f32.bf16 %0, l, %3, %4;\n\tfma.rn.f32.bf16 %1, h, %3, %5;\n\t}"
+            : "=f"(lo), "=f"(hi) : "r"(a2), "h"(b), "f"(c_lo), "f"(c_hi));
+    else
+        asm("{\n\t.reg .b16 l, h;\n\tmov.b32 {l, h}, %2;\n\t"
+            "fma.rn.f32.f16 %0, l, %3, %4;\n\tfma.rn.f32.f16 %1, h, %3, %5;\n\t}"
+            : "=f"(lo), "=f"(hi) : "r"(a2), "h"(b), "f"(c_lo), "f"(c_hi));
+}
+
 template <> struct Codec<LBGB_F16DEV> {
     using raw = unsigned short;
     using real = float;
     static constexpr bool DEV = false;
     static __device__ __forceinline__ real dec_h(raw x) { return __half2float(__ushort_as_half(x)) * F16_UNSCALE; }
     static __device__ __forceinline__ raw enc_h(real h) { return __half_as_ushort(__float2half_rn(h * F16_SCALE)); }
-    static __device__ __forceinline__ real dec(raw x, int i) {
-        return fmaf(__half2float(__ushort_as_half(x)), F16_UNSCALE, wgt<float>(i));
-    }
+    static __device__ __forceinline__ real dec(raw x, int i) { return fma16<false>(x, F16_UNSCALE_BITS, wgt<float>(i)); }
     static __device__ __forceinline__ raw enc(real x, int i) { return enc_h(x - wgt<float>(i)); }
     static __device__ __forceinline__ double decd(raw x, int i) { return (double)dec(x, i); }
     static __device__ __forceinline__ raw encd(double f, int i) { return enc((real)f, i); }
@@ -92,7 +121,7 @@ template <> struct Codec<LBGB_BF16DEV> {
     static constexpr bool DEV = false;
     static __device__ __forceinline__ real dec_h(raw x) { return __bfloat162float(__ushort_as_bfloat16(x)); }
     static __device__ __forceinline__ raw enc_h(real h) { return __bfloat16_as_ushort(__float2bfloat16_rn(h)); }
-    static __device__ __forceinline__ real dec(raw x, int i) { return dec_h(x) + wgt<float>(i); }
+    static __device__ __forceinline__ real dec(raw x, int i) { return fma16<true>(x, BF16_ONE_BITS, wgt<float>(i)); }
     static __device__ __forceinline__ raw enc(real x, int i) { return enc_h(x - wgt<float>(i)); }
     static __device__ __forceinline__ double decd(raw x, int i) { return (double)dec(x, i); }
     static __device__ __forceinline__ raw encd(double f, int i) { return enc((real)f, i); }
@@ -158,8 +187,8 @@ __device__ __forceinline__ void stv(RAW *p, const RAW (&v)[V]) {
 // ---------------------------------------------------------------- packets
 // A packet is the N consecutive cells of one channel that one thread moves as
 // one 8- or 16-byte vector.  The 16-bit routines convert two values per
-// instruction where the hardware allows (half2 -> float2, float2 -> half2 /
-// bfloat162); bfloat16 -> float is a 16-bit shift.
+// instruction where the hardware allows (float2 -> half2 / bfloat162); the
+// decode folds each 16-bit value into its FMA (fma16x2).
 template <int DT, int N>
 struct Packet {
     using raw = typename Codec<DT>::raw;
@@ -181,23 +210,19 @@ struct Packet {
         } else {
 #pragma unroll
             for (int q = 0; q < WORDS; ++q) {
-                if constexpr (DT == LBGB_F16DEV) {
-                    const float2 p = __half22float2(*reinterpret_cast<const __half2 *>(&wd[q]));
-                    o[2 * q] = fmaf(p.x, F16_UNSCALE, w);
-                    o[2 * q + 1] = fmaf(p.y, F16_UNSCALE, w);
-                } else {
-                    o[2 * q] = __uint_as_float(wd[q] << 16) + w;
-                    o[2 * q + 1] = __uint_as_float(wd[q] & 0xffff0000u) + w;
-                }
+                if constexpr (DT == LBGB_F16DEV)
+                    fma16x2<false>(wd[q], F16_UNSCALE_BITS, w, w, o[2 * q], o[2 * q + 1]);
+                else
+                    fma16x2<true>(wd[q], BF16_ONE_BITS, w, w, o[2 * q], o[2 * q + 1]);
             }
         }
     }
     // one stored element plus w
     static __device__ __forceinline__ real dec1(raw x, real w) {
         if constexpr (DT == LBGB_F16DEV)
-            return fmaf(__half2float(__ushort_as_half(x)), F16_UNSCALE, w);
+            return fma16<false>(x, F16_UNSCALE_BITS, w);
         else if constexpr (DT == LBGB_BF16DEV)
-            return __uint_as_float((uint32_t)x << 16) + w;
+            return fma16<true>(x, BF16_ONE_BITS, w);
         else
             return x;
     }
@@ -483,7 +508,7 @@ __device__ __forceinline__ void collide_encode(typename Codec<DT>::real (&f)[9],
         for (int i = 1; i < 9; ++i) {
             const __half q = __float2half_rn(fmaf(f[i], F16_SCALE, -wgt<float>(i) * F16_SCALE));
             out[i] = __half_as_ushort(q);
-            dms -= __half2float(q);
+            dms = fma16<false>(out[i], F16_MINUS_ONE_BITS, dms);
         }
         out[0] = __half_as_ushort(__float2half_rn(dms));
     } else if constexpr (DT == LBGB_BF16DEV) {

@@ -276,11 +276,9 @@ k_step_pipe(const typename Codec<DT>::raw *__restrict__ src, typename Codec<DT>:
                     uint32_t wd[NC / 2];
                     memcpy(wd, &pk[i], sizeof(wd));
 #pragma unroll
-                    for (int q = 0; q < NC / 2; ++q) {
-                        const float2 y = __half22float2(*reinterpret_cast<const __half2 *>(&wd[q]));
-                        hs[0][2 * q] -= y.x;
-                        hs[0][2 * q + 1] -= y.y;
-                    }
+                    for (int q = 0; q < NC / 2; ++q)
+                        fma16x2<false>(wd[q], F16_MINUS_ONE_BITS, hs[0][2 * q], hs[0][2 * q + 1], hs[0][2 * q],
+                                       hs[0][2 * q + 1]);
                 }
                 pk[0] = P::enc_scaled(hs[0]);
 #pragma unroll
