@@ -266,8 +266,14 @@ struct Packet {
 // makes every rounding unbiased, and the accumulated error a random walk.
 // The random bits are a counter-based hash of (seed, step, cell, channel), so
 // every kernel variant rounds every value identically.  Two neighbouring
-// cells (2m, 2m+1) of a channel share one 32-bit hash: 16 bits each.
-__device__ __forceinline__ uint32_t mix32(uint32_t x) {
+// cells (2m, 2m+1) of a channel share one 32-bit word: one hash of the pair
+// and the step key, then per channel a multiply by an odd multiplier of the
+// channel's own and an xorshift (both bijections, so the word stays uniform;
+// the high word of the product alone would not be: it is below the
+// multiplier, and biased rounding follows).  The rounding itself is the hardware's stochastic
+// conversion (cvt.rs.{f16x2,bf16x2}.f32, sm_100 and later), which rounds the
+// even cell with bits 15:0 and the odd cell with bits 31:16 of the word.
+__host__ __device__ constexpr uint32_t mix32(uint32_t x) {
     // integer finaliser with the constants of the public-domain "lowbias32"
     // from C. Wellons' hash-prospector
     x ^= x >> 16;
@@ -280,34 +286,69 @@ __device__ __forceinline__ uint32_t mix32(uint32_t x) {
 __device__ __forceinline__ uint32_t sr_step_key(uint32_t seed, unsigned long long step) {
     return mix32(seed ^ mix32((uint32_t)step * 0x9e3779b9u + (uint32_t)(step >> 32)));
 }
-__device__ __forceinline__ uint32_t sr_pair_bits(uint32_t key, uint32_t even_cell, int ch) {
-    return mix32((even_cell * 9u + (uint32_t)ch) ^ key);
+__device__ __forceinline__ uint32_t sr_pair_base(uint32_t key, uint32_t even_cell) { return mix32(even_cell ^ key); }
+__host__ __device__ constexpr uint32_t sr_mult(int ch) { return mix32(0x9e3779b9u * (uint32_t)(ch + 1)) | 1u; }
+__device__ __forceinline__ uint32_t sr_channel_bits(uint32_t base, int ch) {
+    const uint32_t x = base * sr_mult(ch);
+    return x ^ (x >> 16);
 }
-// f (FP32) -> 16-bit pattern with stochastic rounding, r = 16 random bits
+// two FP32 values -> one word of two 16-bit codes, stochastically rounded:
+// lo to bits 15:0 (random bits r[15:0]), hi to bits 31:16 (r[31:16]).
+// Half codes take the deviation already scaled by 2^14 (sr_dev).
 template <int DT>
-__device__ __forceinline__ uint32_t sr_round16(float h, uint32_t r) {
-    if constexpr (DT == LBGB_BF16DEV) {
-        return (__float_as_uint(h) + r) >> 16;
-    } else {
-        // keep half's 10 mantissa bits of the scaled value; the result is
-        // exactly representable, so the final conversion does not round
-        const float x = __uint_as_float((__float_as_uint(h * F16_SCALE) + (r >> 3)) & 0xffffe000u);
-        return __half_as_ushort(__float2half_rn(x));
-    }
+__device__ __forceinline__ uint32_t sr_pack2(float lo, float hi, uint32_t r) {
+    uint32_t d;
+    if constexpr (DT == LBGB_BF16DEV)
+        asm("cvt.rs.bf16x2.f32 %0, %1, %2, %3;" : "=r"(d) : "f"(hi), "f"(lo), "r"(r));
+    else
+        asm("cvt.rs.f16x2.f32 %0, %1, %2, %3;" : "=r"(d) : "f"(hi), "f"(lo), "r"(r));
+    return d;
+}
+// the value that sr_pack2 rounds for population f of channel i: f - w_i, or
+// for half codes (f - w_i) 2^14 as one FMA
+template <int DT>
+__device__ __forceinline__ float sr_dev(float f, int i) {
+    if constexpr (DT == LBGB_BF16DEV)
+        return f - wgt<float>(i);
+    else
+        return fmaf(f, F16_SCALE, -wgt<float>(i) * F16_SCALE);
+}
+// the same for the rest population's remaining mass deviation d
+template <int DT>
+__device__ __forceinline__ float sr_rest(float d) {
+    if constexpr (DT == LBGB_BF16DEV)
+        return d;
+    else
+        return d * F16_SCALE;
+}
+// d minus the deviation that a stored 16-bit code carries, one instruction
+// per value (the code times -1, or -2^-14 for scaled half, plus d)
+constexpr unsigned short F16_MINUS_UNSCALE_BITS = 0x8400;  // half -2^-14
+constexpr unsigned short BF16_MINUS_ONE_BITS = 0xbf80;     // bfloat16 -1
+template <int DT>
+__device__ __forceinline__ float sub_stored(float d, unsigned short x) {
+    if constexpr (DT == LBGB_BF16DEV)
+        return fma16<true>(x, BF16_MINUS_ONE_BITS, d);
+    else
+        return fma16<false>(x, F16_MINUS_UNSCALE_BITS, d);
+}
+template <int DT>
+__device__ __forceinline__ void sub_stored2(float &d_lo, float &d_hi, uint32_t w) {
+    if constexpr (DT == LBGB_BF16DEV)
+        fma16x2<true>(w, BF16_MINUS_ONE_BITS, d_lo, d_hi, d_lo, d_hi);
+    else
+        fma16x2<false>(w, F16_MINUS_UNSCALE_BITS, d_lo, d_hi, d_lo, d_hi);
 }
 
-// packs N deviations of a 16-bit codec with stochastic rounding; cell0 (even)
-// is the global index of the packet's first cell
+// packs N deviations of a 16-bit codec with stochastic rounding; base[q] is
+// sr_pair_base of the packet's cell pair q
 template <int DT, int N>
-__device__ __forceinline__ typename Packet<DT, N>::vec enc_h_sr(const float (&h)[N], uint32_t key, uint32_t cell0,
+__device__ __forceinline__ typename Packet<DT, N>::vec enc_h_sr(const float (&h)[N], const uint32_t (&base)[N / 2],
                                                               int ch) {
     using P = Packet<DT, N>;
     uint32_t wd[P::WORDS];
 #pragma unroll
-    for (int q = 0; q < P::WORDS; ++q) {
-        const uint32_t r = sr_pair_bits(key, cell0 + 2 * q, ch);
-        wd[q] = sr_round16<DT>(h[2 * q], r & 0xffffu) | (sr_round16<DT>(h[2 * q + 1], r >> 16) << 16);
-    }
+    for (int q = 0; q < P::WORDS; ++q) wd[q] = sr_pack2<DT>(h[2 * q], h[2 * q + 1], sr_channel_bits(base[q], ch));
     typename P::vec x;
     memcpy(&x, wd, P::BYTES);
     return x;
@@ -532,14 +573,20 @@ __device__ __forceinline__ void collide_encode_sr(float (&f)[9], float omega, un
 #pragma unroll
     for (int i = 1; i < 9; ++i) dm += f[i] - wgt<float>(i);
     bgk_collide16(f, omega);
+    const uint32_t base = sr_pair_base(key, cell & ~1u);
+    const bool odd = (cell & 1u) != 0u;
+    // the cell's own lane of the pair's word, as the packet kernels round it
+    auto round1 = [&](float h, int ch) {
+        const uint32_t r = sr_channel_bits(base, ch);
+        return odd ? (unsigned short)(sr_pack2<DT>(0.f, h, r) >> 16)
+                   : (unsigned short)(sr_pack2<DT>(h, 0.f, r) & 0xffffu);
+    };
 #pragma unroll
     for (int i = 1; i < 9; ++i) {
-        const uint32_t r = sr_pair_bits(key, cell & ~1u, i);
-        out[i] = (unsigned short)sr_round16<DT>(f[i] - wgt<float>(i), (cell & 1u) ? (r >> 16) : (r & 0xffffu));
-        dm -= Codec<DT>::dec_h(out[i]);
+        out[i] = round1(sr_dev<DT>(f[i], i), i);
+        dm = sub_stored<DT>(dm, out[i]);
     }
-    const uint32_t r = sr_pair_bits(key, cell & ~1u, 0);
-    out[0] = (unsigned short)sr_round16<DT>(dm, (cell & 1u) ? (r >> 16) : (r & 0xffffu));
+    out[0] = round1(sr_rest<DT>(dm), 0);
 }
 
 // ---------------------------------------------------------------- host side

@@ -301,35 +301,42 @@ k_step_pipe(const typename Codec<DT>::raw *__restrict__ src, typename Codec<DT>:
                 }
                 bgk_collide16(f, omega);
 #pragma unroll
-                for (int i = 0; i < 9; ++i) hpost[i][j] = f[i] - wgt<real>(i);
+                for (int i = 0; i < 9; ++i) hpost[i][j] = sr ? sr_dev<DT>(f[i], i) : f[i] - wgt<real>(i);
             }
-            uint32_t key = 0u;
-            if constexpr (SRND) key = sr_step_key(sr_seed, *sr_step);
-            const uint32_t cell0 = (uint32_t)((size_t)k * ny + c);
-            typename P::vec pk[9];
+            uint32_t base[NC / 2];
+            if constexpr (sr) {
+                const uint32_t key = sr_step_key(sr_seed, *sr_step);
+                const uint32_t cell0 = (uint32_t)((size_t)k * ny + c);
+#pragma unroll
+                for (int q = 0; q < NC / 2; ++q) base[q] = sr_pair_base(key, cell0 + 2 * q);
+            }
+            // each moving channel is stored as soon as it is encoded (fewer
+            // live registers); the rest population last, after the mass fix
 #pragma unroll
             for (int i = 1; i < 9; ++i) {
+                typename P::vec pk;
                 if constexpr (sr)
-                    pk[i] = enc_h_sr<DT, NC>(hpost[i], key, cell0, i);
+                    pk = enc_h_sr<DT, NC>(hpost[i], base, i);
                 else
-                    pk[i] = P::enc_h(hpost[i]);
+                    pk = P::enc_h(hpost[i]);
                 if constexpr (keep_mass) {
-                    real y[NC];
-                    P::dec(pk[i], real(0), y);
+                    uint32_t wd[NC / 2];
+                    memcpy(wd, &pk, sizeof(wd));
 #pragma unroll
-                    for (int j = 0; j < NC; ++j) dm[j] -= y[j];
+                    for (int q = 0; q < NC / 2; ++q) sub_stored2<DT>(dm[2 * q], dm[2 * q + 1], wd[q]);
                 }
+                st_cs(reinterpret_cast<typename P::vec *>(out_row + (size_t)i * cs), pk);
             }
             if constexpr (keep_mass) {
 #pragma unroll
-                for (int j = 0; j < NC; ++j) hpost[0][j] = dm[j];
+                for (int j = 0; j < NC; ++j) hpost[0][j] = sr ? sr_rest<DT>(dm[j]) : dm[j];
             }
+            typename P::vec pk0;
             if constexpr (sr)
-                pk[0] = enc_h_sr<DT, NC>(hpost[0], key, cell0, 0);
+                pk0 = enc_h_sr<DT, NC>(hpost[0], base, 0);
             else
-                pk[0] = P::enc_h(hpost[0]);
-#pragma unroll
-            for (int i = 0; i < 9; ++i) st_cs(reinterpret_cast<typename P::vec *>(out_row + (size_t)i * cs), pk[i]);
+                pk0 = P::enc_h(hpost[0]);
+            st_cs(reinterpret_cast<typename P::vec *>(out_row), pk0);
         } else {
             raw out[9][NC];
             if (COLLIDE) {

@@ -103,7 +103,16 @@ def _rel_l2_u(lat, ux_ref, uy_ref):
 def _make(n, omega, u0, variant, device):
     storage, _, mode = variant.partition("+")
     rounding = "stochastic" if mode == "sr" else "nearest"
-    return Lattice(n, n, omega, boundary="cavity", u0=u0, storage=storage, device=device, rounding=rounding, seed=1)
+    lat = Lattice(n, n, omega, boundary="cavity", u0=u0, storage=storage, device=device, rounding=rounding, seed=1)
+    if mode in ("perturb", "perturb-centre"):
+        # control run: the same arithmetic with the rest population of one node
+        # moved by 1e-12 -- how fast the flow itself separates two runs.  The
+        # node sits one row below the middle of the lid (in the flow from the
+        # first step) or, for "perturb-centre", at the centre of the cavity.
+        f = lat.populations(torch.float64)
+        f[0, n // 2, n // 2 if mode == "perturb-centre" else n - 2] += 1e-12
+        lat.load(f)
+    return lat
 
 
 def precision(n=1024, omegas=(1.0, 1.7, 1.95), steps=50000, u0=0.1,
@@ -113,7 +122,11 @@ def precision(n=1024, omegas=(1.0, 1.7, 1.95), steps=50000, u0=0.1,
 
     All lattices advance together; at each checkpoint the relative L2 error of
     the velocity field against the FP64 lattice and the mass drift are
-    recorded.  A "+sr" suffix selects stochastic rounding of the 16-bit codes.
+    recorded.  A "+sr" suffix selects stochastic rounding of the 16-bit codes;
+    "f64+perturb" / "f64+perturb-centre" is an FP64 control run whose start
+    differs by 1e-12 in one population next to the lid / at the centre (it
+    separates from the reference run only as fast as the flow amplifies small
+    differences).
     """
     out = []
     marks = sorted({c for c in checkpoints if c <= steps} | {steps})
@@ -148,6 +161,8 @@ def main(argv=None):
     p.add_argument("--n", type=int, default=1024)
     p.add_argument("--steps", type=int, default=0)
     p.add_argument("--omegas", type=str, default="1.0,1.7,1.95")
+    p.add_argument("--storages", type=str, default="f32,f16dev,bf16dev,f16dev+sr,bf16dev+sr",
+                   help="precision study: comma-separated storages compared with FP64")
     a = p.parse_args(argv)
     if a.study == "density":
         _, _, fit = density_wave(steps=a.steps or 10000)
@@ -155,7 +170,8 @@ def main(argv=None):
     elif a.study == "shear":
         print(json.dumps({"study": "shear_wave", **shear_wave(steps=a.steps or 2000)}))
     else:
-        for row in precision(n=a.n, omegas=[float(x) for x in a.omegas.split(",")], steps=a.steps or 50000):
+        for row in precision(n=a.n, omegas=[float(x) for x in a.omegas.split(",")], steps=a.steps or 50000,
+                             storages=tuple(a.storages.split(","))):
             print(json.dumps({"study": "precision", **row}))
 
 

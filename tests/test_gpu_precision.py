@@ -174,3 +174,22 @@ def test_16bit_stochastic_rounding_error_bound(cuda, ref64, storage, tol):
     m_ref = ref64.sum() - NX * NY
     m = float(lat.mass_momentum()[0]) - NX * NY
     assert abs(m - m_ref) <= 0.05 * abs(m_ref), (m, m_ref)
+
+
+@pytest.mark.gpu
+def test_precision_study_rows_and_perturbed_control(cuda):
+    """The precision study's rows: FP32 error against FP64 is small but not
+    zero, and the FP64 control run started 1e-12 away from the reference
+    separates from it (the flow amplifies differences) but stays far closer
+    than FP32 after a few hundred steps of a small cavity."""
+    from latticeboltzmann_gb300 import studies
+    rows = studies.precision(n=48, omegas=(1.7,), steps=400, storages=("f32", "f64+perturb"), device=cuda,
+                             checkpoints=(200, 400))
+    assert [(r["steps"], r["storage"]) for r in rows] == [(200, "f32"), (200, "f64+perturb"), (400, "f32"),
+                                                          (400, "f64+perturb")]
+    for r in rows:
+        assert r["fp64_finite"] and r["rel_l2_u"] is not None
+    f32 = [r["rel_l2_u"] for r in rows if r["storage"] == "f32"]
+    ctl = [r["rel_l2_u"] for r in rows if r["storage"] == "f64+perturb"]
+    assert all(0 < e < 1e-4 for e in f32)
+    assert all(0 < e < 1e-8 for e in ctl)
