@@ -104,27 +104,30 @@ __device__ __forceinline__ void fma16x2(uint32_t a2, unsigned short b, float c_l
             : "=f"(lo), "=f"(hi) : "r"(a2), "h"(b), "f"(c_lo), "f"(c_hi));
 }
 
+// The 16-bit codecs are DEV codecs too: the kernels work on h = f - w_i, the
+// collision in deviation form (collide_dev), so that no population is ever
+// rebuilt from its weight and every rounding acts on a small number.
 template <> struct Codec<LBGB_F16DEV> {
     using raw = unsigned short;
     using real = float;
-    static constexpr bool DEV = false;
-    static __device__ __forceinline__ real dec_h(raw x) { return __half2float(__ushort_as_half(x)) * F16_UNSCALE; }
+    static constexpr bool DEV = true;
+    static __device__ __forceinline__ real dec_h(raw x) { return fma16<false>(x, F16_UNSCALE_BITS, 0.f); }
     static __device__ __forceinline__ raw enc_h(real h) { return __half_as_ushort(__float2half_rn(h * F16_SCALE)); }
-    static __device__ __forceinline__ real dec(raw x, int i) { return fma16<false>(x, F16_UNSCALE_BITS, wgt<float>(i)); }
-    static __device__ __forceinline__ raw enc(real x, int i) { return enc_h(x - wgt<float>(i)); }
-    static __device__ __forceinline__ double decd(raw x, int i) { return (double)dec(x, i); }
-    static __device__ __forceinline__ raw encd(double f, int i) { return enc((real)f, i); }
+    static __device__ __forceinline__ real dec(raw x, int) { return dec_h(x); }
+    static __device__ __forceinline__ raw enc(real h, int) { return enc_h(h); }
+    static __device__ __forceinline__ double decd(raw x, int i) { return (double)dec_h(x) + wgt<double>(i); }
+    static __device__ __forceinline__ raw encd(double f, int i) { return enc_h((real)(f - wgt<double>(i))); }
 };
 template <> struct Codec<LBGB_BF16DEV> {
     using raw = unsigned short;
     using real = float;
-    static constexpr bool DEV = false;
-    static __device__ __forceinline__ real dec_h(raw x) { return __bfloat162float(__ushort_as_bfloat16(x)); }
+    static constexpr bool DEV = true;
+    static __device__ __forceinline__ real dec_h(raw x) { return __uint_as_float((uint32_t)x << 16); }
     static __device__ __forceinline__ raw enc_h(real h) { return __bfloat16_as_ushort(__float2bfloat16_rn(h)); }
-    static __device__ __forceinline__ real dec(raw x, int i) { return fma16<true>(x, BF16_ONE_BITS, wgt<float>(i)); }
-    static __device__ __forceinline__ raw enc(real x, int i) { return enc_h(x - wgt<float>(i)); }
-    static __device__ __forceinline__ double decd(raw x, int i) { return (double)dec(x, i); }
-    static __device__ __forceinline__ raw encd(double f, int i) { return enc((real)f, i); }
+    static __device__ __forceinline__ real dec(raw x, int) { return dec_h(x); }
+    static __device__ __forceinline__ raw enc(real h, int) { return enc_h(h); }
+    static __device__ __forceinline__ double decd(raw x, int i) { return (double)dec_h(x) + wgt<double>(i); }
+    static __device__ __forceinline__ raw encd(double f, int i) { return enc_h((real)(f - wgt<double>(i))); }
 };
 
 // Density of a node from its nine kernel values (populations, or deviations
@@ -197,8 +200,9 @@ struct Packet {
     static constexpr int WORDS = BYTES / 4;
     using vec = typename VecBits<BYTES>::t;
 
-    // values f = h + w (16-bit codecs; w = 0 gives the deviations) or f
-    static __device__ __forceinline__ void dec(const vec &x, real w, real (&o)[N]) {
+    // the kernel values of a packet: f (FP32, FP64) or h = f - w (the DEV
+    // codecs); w is unused (the weights never enter a decode)
+    static __device__ __forceinline__ void dec(const vec &x, real, real (&o)[N]) {
         uint32_t wd[WORDS];
         memcpy(wd, &x, BYTES);
         if constexpr (DT == LBGB_F32 || DT == LBGB_F32DEV) {
@@ -210,19 +214,19 @@ struct Packet {
         } else {
 #pragma unroll
             for (int q = 0; q < WORDS; ++q) {
-                if constexpr (DT == LBGB_F16DEV)
-                    fma16x2<false>(wd[q], F16_UNSCALE_BITS, w, w, o[2 * q], o[2 * q + 1]);
-                else
-                    fma16x2<true>(wd[q], BF16_ONE_BITS, w, w, o[2 * q], o[2 * q + 1]);
+                if constexpr (DT == LBGB_F16DEV) {
+                    fma16x2<false>(wd[q], F16_UNSCALE_BITS, 0.f, 0.f, o[2 * q], o[2 * q + 1]);
+                } else {
+                    o[2 * q] = __uint_as_float(wd[q] << 16);
+                    o[2 * q + 1] = __uint_as_float(wd[q] & 0xffff0000u);
+                }
             }
         }
     }
-    // one stored element plus w
-    static __device__ __forceinline__ real dec1(raw x, real w) {
-        if constexpr (DT == LBGB_F16DEV)
-            return fma16<false>(x, F16_UNSCALE_BITS, w);
-        else if constexpr (DT == LBGB_BF16DEV)
-            return fma16<true>(x, BF16_ONE_BITS, w);
+    // the kernel value of one stored element (w unused, as in dec)
+    static __device__ __forceinline__ real dec1(raw x, real) {
+        if constexpr (DT == LBGB_F16DEV || DT == LBGB_BF16DEV)
+            return Codec<DT>::dec_h(x);
         else
             return x;
     }
@@ -304,14 +308,13 @@ __device__ __forceinline__ uint32_t sr_pack2(float lo, float hi, uint32_t r) {
         asm("cvt.rs.f16x2.f32 %0, %1, %2, %3;" : "=r"(d) : "f"(hi), "f"(lo), "r"(r));
     return d;
 }
-// the value that sr_pack2 rounds for population f of channel i: f - w_i, or
-// for half codes (f - w_i) 2^14 as one FMA
+// the value that sr_pack2 rounds for deviation h: h, or h 2^14 for half codes
 template <int DT>
-__device__ __forceinline__ float sr_dev(float f, int i) {
+__device__ __forceinline__ float sr_dev(float h) {
     if constexpr (DT == LBGB_BF16DEV)
-        return f - wgt<float>(i);
+        return h;
     else
-        return fmaf(f, F16_SCALE, -wgt<float>(i) * F16_SCALE);
+        return h * F16_SCALE;
 }
 // the same for the rest population's remaining mass deviation d
 template <int DT>
@@ -416,43 +419,24 @@ __device__ __forceinline__ void bgk_collide(R (&f)[9], R omega) {
     bgk_collide(f, omega, a, b, c);
 }
 
-// The collision of the 16-bit storage paths: the same arithmetic with the
-// hardware reciprocal approximation of rho (the stored values round at 2^-11
-// or coarser, far above its ~1 ulp).
-__device__ __forceinline__ void bgk_collide16(float (&f)[9], float omega) {
-    float rho = f[0];
-#pragma unroll
-    for (int i = 1; i < 9; ++i) rho += f[i];
-    float ux, uy;
-    bgk_relax<float, true>(f, omega, rho, ux, uy);
-}
-
-// FP16 deviation storage, round to nearest: collide one node and return its
-// scaled mass deviation D S, D = sum_i (f_i - w_i) summed over the small
-// deviations (accurate to FP32 rounding of numbers ~1e-2, unbiased); the
-// density for the collision is 1 + D.  The mass fix stores the rest
-// population as D S minus what the other eight stored values carry.
-__device__ __forceinline__ float collide_f16_mass(float (&f)[9], float omega) {
-    float d = f[0] - wgt<float>(0);
-#pragma unroll
-    for (int i = 1; i < 9; ++i) d += f[i] - wgt<float>(i);
-    float ux, uy;
-    bgk_relax<float, true>(f, omega, 1.f + d, ux, uy);
-    return d * F16_SCALE;
-}
-
-// BGK in deviation form, h_i = f_i - w_i (LBGB_F32DEV): every intermediate is
-// a small number, so FP32 rounds at ~1e-9 instead of ~3e-8.  With D = sum h,
-// rho = 1 + D, j = sum c_i h_i (the weights carry no momentum), u = j / rho:
+// BGK in deviation form, h_i = f_i - w_i (the DEV codecs): every
+// intermediate is a small number, so FP32 rounds at ~1e-9 instead of ~3e-8.
+// With D = sum h, rho = 1 + D, j = sum c_i h_i (the weights carry no
+// momentum), u = j / rho:
 //   h_i^eq = w_i (D + rho (cu + cu^2/2 - uu))   (same polynomial as feq)
 //   h_i' = h_i + omega (h_i^eq - h_i),  and h_0' = D - sum_{i>0} h_i' so the
 // node keeps its mass exactly in exact arithmetic of the stored values.
-__device__ __forceinline__ void collide_dev(float (&h)[9], float omega) {
+// APPROX_RCP: 1/rho by the hardware approximation (16-bit storage, whose
+// rounding at 2^-11 or coarser is far above its ~1 ulp).  REST = false leaves
+// h_0 to the caller, which writes it from the rounded stored values.
+// Returns D.
+template <bool APPROX_RCP = false, bool REST = true>
+__device__ __forceinline__ float collide_dev(float (&h)[9], float omega) {
     float d = h[0];
 #pragma unroll
     for (int i = 1; i < 9; ++i) d += h[i];
     const float rho = 1.f + d;
-    const float inv = recip(rho);
+    const float inv = APPROX_RCP ? recip_approx(rho) : recip(rho);
     float ux = (h[1] - h[3] + h[5] - h[6] - h[7] + h[8]) * inv;
     float uy = (h[2] - h[4] + h[5] + h[6] - h[7] - h[8]) * inv;
     ux *= 3.f;
@@ -478,7 +462,8 @@ __device__ __forceinline__ void collide_dev(float (&h)[9], float omega) {
         h[i] += omega * (heq - h[i]);
         rest -= h[i];
     }
-    h[0] = rest;
+    if constexpr (REST) h[0] = rest;
+    return d;
 }
 
 // Equilibrium of one node (same formulation as above).
@@ -514,11 +499,11 @@ __device__ __forceinline__ void equilibrium1(R rho, R ux, R uy, R (&feq)[9]) {
 //    moving populations summed as small numbers (exactly zero at rest, so
 //    the rest state stays a fixed point; resting-wall drift ~5e-6 instead
 //    of ~1e-2, for 16 additions);
-//  * half deviations: h_0 = sum_i h_i(before) - sum_{i>0} h_i(stored), the
-//    stored values decoded back (drift 7e-5 instead of 3e-2; moving-lid mass
-//    error against FP64 5x smaller);
-//  * bfloat16 deviations are rounded as they are: with 8 significant bits
-//    the correction made the moving-lid mass error larger, not smaller.
+//  * 16-bit deviations (half and bfloat16): h_0 = sum_i h_i(before) -
+//    sum_{i>0} h_i(stored), the stored values decoded back.  Against FP64
+//    (64^2 cavity, moving lid, 1000 steps, CPU emulation of the kernels'
+//    arithmetic) the mass drift is then reproduced within 0.5 % (bfloat16)
+//    and 0.1 % (half); without the fix bfloat16 misses it by 42 %.
 template <int DT>
 __device__ __forceinline__ void collide_encode(typename Codec<DT>::real (&f)[9], typename Codec<DT>::real omega,
                                                typename Codec<DT>::raw (&out)[9]) {
@@ -540,22 +525,25 @@ __device__ __forceinline__ void collide_encode(typename Codec<DT>::real (&f)[9],
 #pragma unroll
         for (int i = 0; i < 9; ++i) out[i] = f[i];
     } else if constexpr (DT == LBGB_F16DEV) {
-        // Scaled deviations h S = f S - w S (one FMA each); the rest population
-        // takes the node's mass deviation minus what the other eight stored
-        // values carry, so the node keeps its mass up to the rounding of h_0
-        // alone.  The pipelined kernel does the same operations.
-        real dms = collide_f16_mass(f, omega);
+        // f holds deviations.  The rest population takes the node's scaled
+        // mass deviation D S minus what the other eight stored values carry,
+        // so the node keeps its mass up to the rounding of h_0 alone.  The
+        // pipelined kernel does the same operations.
+        real dms = collide_dev<true, false>(f, omega) * F16_SCALE;
 #pragma unroll
         for (int i = 1; i < 9; ++i) {
-            const __half q = __float2half_rn(fmaf(f[i], F16_SCALE, -wgt<float>(i) * F16_SCALE));
-            out[i] = __half_as_ushort(q);
+            out[i] = C::enc_h(f[i]);
             dms = fma16<false>(out[i], F16_MINUS_ONE_BITS, dms);
         }
         out[0] = __half_as_ushort(__float2half_rn(dms));
     } else if constexpr (DT == LBGB_BF16DEV) {
-        bgk_collide16(f, omega);
+        real dm = collide_dev<true, false>(f, omega);
 #pragma unroll
-        for (int i = 0; i < 9; ++i) out[i] = C::enc(f[i], i);
+        for (int i = 1; i < 9; ++i) {
+            out[i] = C::enc_h(f[i]);
+            dm = sub_stored<DT>(dm, out[i]);
+        }
+        out[0] = C::enc_h(dm);
     } else {
         bgk_collide(f, omega);
 #pragma unroll
@@ -563,16 +551,13 @@ __device__ __forceinline__ void collide_encode(typename Codec<DT>::real (&f)[9],
     }
 }
 
-// 16-bit storage with stochastic rounding (see above): the moving populations
+// 16-bit storage with stochastic rounding (see above): the moving deviations
 // are rounded stochastically, then the rest population carries the node's
 // remaining mass (for both 16-bit codecs) and is rounded stochastically too.
 template <int DT>
 __device__ __forceinline__ void collide_encode_sr(float (&f)[9], float omega, unsigned short (&out)[9], uint32_t key,
                                                   uint32_t cell) {
-    float dm = f[0] - wgt<float>(0);
-#pragma unroll
-    for (int i = 1; i < 9; ++i) dm += f[i] - wgt<float>(i);
-    bgk_collide16(f, omega);
+    float dm = collide_dev<true, false>(f, omega);
     const uint32_t base = sr_pair_base(key, cell & ~1u);
     const bool odd = (cell & 1u) != 0u;
     // the cell's own lane of the pair's word, as the packet kernels round it
@@ -583,7 +568,7 @@ __device__ __forceinline__ void collide_encode_sr(float (&f)[9], float omega, un
     };
 #pragma unroll
     for (int i = 1; i < 9; ++i) {
-        out[i] = round1(sr_dev<DT>(f[i], i), i);
+        out[i] = round1(sr_dev<DT>(f[i]), i);
         dm = sub_stored<DT>(dm, out[i]);
     }
     out[0] = round1(sr_rest<DT>(dm), 0);

@@ -257,17 +257,17 @@ k_step_pipe(const typename Codec<DT>::raw *__restrict__ src, typename Codec<DT>:
             constexpr bool sr = SRND;
             if constexpr (DT == LBGB_F16DEV && !SRND) {
                 // FP16, round to nearest: the operations of collide_encode<F16DEV>
-                // (mass deviation summed once, scaled deviations by one FMA), two
-                // values per conversion
+                // (deviation-form collision, scaled deviations), two values per
+                // conversion
                 real hs[9][NC];
 #pragma unroll
                 for (int j = 0; j < NC; ++j) {
-                    real f[9];
+                    real h[9];
 #pragma unroll
-                    for (int i = 0; i < 9; ++i) f[i] = v[i][j];
-                    hs[0][j] = collide_f16_mass(f, omega);
+                    for (int i = 0; i < 9; ++i) h[i] = v[i][j];
+                    hs[0][j] = collide_dev<true, false>(h, omega) * F16_SCALE;
 #pragma unroll
-                    for (int i = 1; i < 9; ++i) hs[i][j] = fmaf(f[i], F16_SCALE, -wgt<float>(i) * F16_SCALE);
+                    for (int i = 1; i < 9; ++i) hs[i][j] = h[i] * F16_SCALE;
                 }
                 typename P::vec pk[9];
 #pragma unroll
@@ -286,22 +286,19 @@ k_step_pipe(const typename Codec<DT>::raw *__restrict__ src, typename Codec<DT>:
                     st_cs(reinterpret_cast<typename P::vec *>(out_row + (size_t)i * cs), pk[i]);
                 continue;
             }
-            constexpr bool keep_mass = SRND || DT == LBGB_F16DEV;
+            // the rest population keeps the node's mass through the stored
+            // values (both roundings, see collide_encode)
+            constexpr bool keep_mass = true;
             real hpost[9][NC];
             real dm[NC];
 #pragma unroll
             for (int j = 0; j < NC; ++j) {
-                real f[9];
+                real h[9];
 #pragma unroll
-                for (int i = 0; i < 9; ++i) f[i] = v[i][j];
-                if constexpr (keep_mass) {
-                    dm[j] = f[0] - wgt<real>(0);
+                for (int i = 0; i < 9; ++i) h[i] = v[i][j];
+                dm[j] = collide_dev<true, !keep_mass>(h, omega);
 #pragma unroll
-                    for (int i = 1; i < 9; ++i) dm[j] += f[i] - wgt<real>(i);
-                }
-                bgk_collide16(f, omega);
-#pragma unroll
-                for (int i = 0; i < 9; ++i) hpost[i][j] = sr ? sr_dev<DT>(f[i], i) : f[i] - wgt<real>(i);
+                for (int i = 0; i < 9; ++i) hpost[i][j] = sr ? sr_dev<DT>(h[i]) : h[i];
             }
             uint32_t base[NC / 2];
             if constexpr (sr) {
