@@ -89,16 +89,19 @@ struct PipeGeom {
 };
 
 // Shapes per storage code: FP32 8 warps x 4 cells, FP64 8 x 2; the 16-bit
-// codecs have twice the cells per byte and are issue-bound, so 8 warps hold
-// 8 cells each (more work per thread between the per-tile fixed costs;
-// 168 registers, no spills; measured faster than 16 warps x 4 cells).
-template <int DT> struct PipeShape { static constexpr int NCW = 8, NC = 4; };
-template <> struct PipeShape<LBGB_F64> { static constexpr int NCW = 8, NC = 2; };
-template <> struct PipeShape<LBGB_F16DEV> { static constexpr int NCW = 8, NC = 8; };
-template <> struct PipeShape<LBGB_BF16DEV> { static constexpr int NCW = 8, NC = 8; };
+// codecs have twice the cells per byte, so 8 warps hold 8 cells each (more
+// work per thread between the per-tile fixed costs; 168 registers, no
+// spills).  CTAS: resident CTAs per SM (the launch bound and the persistent
+// grid).  Measured at 8192^2 (FP16, FP16 stochastic, BF16 MLUPS): 8 x 8 with
+// one CTA 163.8k / 154.7k / 168.4k; 8 x 4 with two CTAs (96 registers)
+// 153.4k / 136.8k / 151.8k; 16 x 4 with one CTA 158.4k / 146.6k / 160.6k.
+template <int DT> struct PipeShape { static constexpr int NCW = 8, NC = 4, CTAS = 1; };
+template <> struct PipeShape<LBGB_F64> { static constexpr int NCW = 8, NC = 2, CTAS = 1; };
+template <> struct PipeShape<LBGB_F16DEV> { static constexpr int NCW = 8, NC = 8, CTAS = 1; };
+template <> struct PipeShape<LBGB_BF16DEV> { static constexpr int NCW = 8, NC = 8, CTAS = 1; };
 
 template <int DT, int BC, bool COLLIDE, int NCW_, int NC_, bool SRND>
-__global__ void __launch_bounds__((NCW_ + 1) * 32, 1)
+__global__ void __launch_bounds__((NCW_ + 1) * 32, PipeShape<DT>::CTAS)
 k_step_pipe(const typename Codec<DT>::raw *__restrict__ src, typename Codec<DT>::raw *__restrict__ dst, int nx,
             int ny, int tiles_per_row, int total_tiles, int stages, typename Codec<DT>::real omega,
             typename Codec<DT>::real u0, long long wait_limit, int stall_producer,

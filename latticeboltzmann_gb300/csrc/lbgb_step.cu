@@ -299,12 +299,13 @@ static int launch_pipe(const void *src, void *dst, int nx, int ny, double omega,
     const long long tpr = (ny + G::L - 1) / G::L;
     const long long total = (long long)rows.n(nx) * tpr;
     const int smax = max_dyn_smem();
-    const int fit = (int)((smax - 256) / (G::STAGE_BYTES + 16));
+    const int fit = (int)((smax / SH::CTAS - 256) / (G::STAGE_BYTES + 16));
     int stages = (int)g_tune.stages;
     if (stages > fit) stages = fit;
     if (stages < 2 || total > INT_MAX) return 1;  // caller falls back to the register kernel
     const size_t smem = (size_t)stages * G::STAGE_BYTES + 16 * (size_t)stages;
-    const int grid = (int)(total < sm_count() ? total : sm_count());
+    const long long slots = (long long)sm_count() * SH::CTAS;
+    const int grid = (int)(total < slots ? total : slots);
     const bool srnd = sizeof(raw) == 2 && COLLIDE && sr.step != nullptr;
     // the dynamic shared-memory limit is raised once per kernel variant and device
     static bool attr_set[MAX_DEVICES][2] = {};
