@@ -214,12 +214,29 @@ __global__ void k_adam(float *__restrict__ w, const float *__restrict__ g, float
     }
 }
 
-// out[i] = beta * out[i] + sum_s parts[s * n + i]   (split-K partial sums)
-__global__ void k_sum_splits(const float *__restrict__ parts, float *__restrict__ out, int S, long long n, float beta) {
-    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
-        float acc = beta == 0.f ? 0.f : beta * out[i];
-        for (int s = 0; s < S; ++s) acc += parts[(long long)s * n + i];
-        out[i] = acc;
+// out[i] = beta * out[i] + sum_s parts[s * n + i]   (split-K partial sums).
+// A block of 32 x SUM_GROUPS threads takes 32 consecutive outputs: thread
+// (x, y) adds the splits s = y, y + SUM_GROUPS, ... (loads coalesced over x),
+// then the group sums are added in the fixed order y = 0, 1, ...  (One
+// thread per output walking all S splits left the few hundred threads of a
+// weight gradient waiting on S dependent additions.)
+constexpr int SUM_GROUPS = 8;
+__global__ void __launch_bounds__(32 * SUM_GROUPS)
+k_sum_splits(const float *__restrict__ parts, float *__restrict__ out, int S, long long n, float beta) {
+    __shared__ float part[SUM_GROUPS][33];
+    const long long i = blockIdx.x * 32ll + threadIdx.x;
+    float acc = 0.f;
+    if (i < n) {
+#pragma unroll 4
+        for (int s = threadIdx.y; s < S; s += SUM_GROUPS) acc += parts[(long long)s * n + i];
+    }
+    part[threadIdx.y][threadIdx.x] = acc;
+    __syncthreads();
+    if (threadIdx.y == 0 && i < n) {
+        float t = beta == 0.f ? 0.f : beta * out[i];
+#pragma unroll
+        for (int y = 0; y < SUM_GROUPS; ++y) t += part[y][threadIdx.x];
+        out[i] = t;
     }
 }
 
@@ -319,6 +336,15 @@ extern "C" int lbgb_fno_adam(float *w, const float *g, float *m, float *v, void 
 
 extern "C" int lbgb_fno_sum_splits(const float *parts, float *out, int S, long long n, float beta, void *stream) {
     if (n <= 0) return LBGB_OK;
-    k_sum_splits<<<blocks_for(n), 256, 0, (cudaStream_t)stream>>>(parts, out, S, n, beta);
+    if (S <= 0) {
+        set_error("lbgb_fno_sum_splits: S must be positive");
+        return LBGB_EINVAL;
+    }
+    const long long blocks = (n + 31) / 32;
+    if (blocks > 2147483647ll) {
+        set_error("lbgb_fno_sum_splits: too many outputs");
+        return LBGB_EINVAL;
+    }
+    k_sum_splits<<<(unsigned)blocks, dim3(32, SUM_GROUPS), 0, (cudaStream_t)stream>>>(parts, out, S, n, beta);
     return check_launch("k_sum_splits");
 }

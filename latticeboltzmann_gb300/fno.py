@@ -83,13 +83,16 @@ class FNO2d:
     """
 
     def __init__(self, width=32, modes=12, layers=4, hidden=128, cin=4, cout=3, pad=0.25, device=None, seed=0,
-                 engine=ENGINE_TENSOR_CORES):
+                 engine=ENGINE_TENSOR_CORES, max_splits=1024):
         self.device = torch.device(device) if device is not None else torch.device("cuda", torch.cuda.current_device())
         if self.device.type != "cuda":
             raise TypeError("FNO2d runs on a CUDA device (there is no CPU path)")
         _lib.load()
         self.width, self.modes, self.layers, self.hidden, self.cin, self.cout = width, modes, layers, hidden, cin, cout
         self.pad, self.engine = float(pad), int(engine)
+        if max_splits < 1 or max_splits & (max_splits - 1):
+            raise ValueError("max_splits must be a power of two")
+        self.max_splits = int(max_splits)  # weight gradients: split-K count over the pixels
         shapes = [("P", (width, cin)), ("pb", (width,))]
         for l in range(layers):
             shapes += [("W%d" % l, (width, width)), ("b%d" % l, (width,)),
@@ -176,7 +179,9 @@ class FNO2d:
                   1.0, beta, int(bf16_out), self.engine, self._s())
 
     def _splits(self, K):
-        s = 256
+        """Split count of a weight gradient over K pixels: the largest power of
+        two up to ``max_splits`` that divides K and leaves >= 256 per split."""
+        s = self.max_splits
         while s > 1 and (K % s or K // s < 256):
             s //= 2
         return s
@@ -229,8 +234,8 @@ class FNO2d:
                        "dv": torch.empty(C, N, **f32),
                        "dzb": torch.empty(C, N, **bf), "dYm": torch.empty(C * B * q2 * m2, **f32),
                        "dP": torch.empty(C * B * m2 * q2, **bf),
-                       "parts": torch.empty(256 * max(self.hidden * C, C * C, C * self.cin, self.cout * self.hidden),
-                                            **f32),
+                       "parts": torch.empty(self.max_splits * max(self.hidden * C, C * C, C * self.cin,
+                                                                    self.cout * self.hidden), **f32),
                        "mse": torch.empty(1024, dtype=torch.float64, device=self.device),
                        "rowsum": torch.empty(64 * max(self.hidden, C, self.cout), **f32)})
         self._ws[key] = ws
@@ -409,9 +414,11 @@ def main(argv=None):
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--engine", choices=["tensor", "cuda"], default="tensor")
+    ap.add_argument("--max-splits", type=int, default=1024, help="split-K count cap of the weight gradients")
     args = ap.parse_args(argv)
     dev = torch.device("cuda", torch.cuda.current_device())
-    net = FNO2d(device=dev, engine=ENGINE_TENSOR_CORES if args.engine == "tensor" else ENGINE_CUDA_CORES)
+    net = FNO2d(device=dev, engine=ENGINE_TENSOR_CORES if args.engine == "tensor" else ENGINE_CUDA_CORES,
+                max_splits=args.max_splits)
     rng = np.random.default_rng(0)
     re = np.exp(rng.uniform(math.log(RE_RANGE[0]), math.log(RE_RANGE[1]), args.batch))
     a = net.inputs(re, rng.uniform(*U_RANGE, args.batch), args.n, args.n)
@@ -431,7 +438,8 @@ def main(argv=None):
         net.forward(a)
     torch.cuda.synchronize(dev)
     fwd = (time.perf_counter() - t0) / max(args.steps, 1)
-    print(json.dumps({"batch": args.batch, "n": args.n, "engine": args.engine, "train_step_ms": round(train * 1e3, 3),
+    print(json.dumps({"batch": args.batch, "n": args.n, "engine": args.engine, "max_splits": net.max_splits,
+                      "train_step_ms": round(train * 1e3, 3),
                       "forward_ms": round(fwd * 1e3, 3), "params": int(sum(np.prod(s) for s in net.shapes.values()))}))
 
 
