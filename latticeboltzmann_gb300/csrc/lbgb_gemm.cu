@@ -75,23 +75,37 @@ constexpr long long TC_WAIT = 1ll << 22;
 // X[r * rs + k * ks], zero outside R x K) into the core-matrix K-major layout.
 // Thread-to-element mapping follows the contiguous axis so that a warp's
 // loads coalesce: 16-byte vector loads along K when K is contiguous and
-// aligned, consecutive rows per warp when the rows are contiguous.
+// aligned, consecutive rows per warp when the rows are contiguous.  Every
+// thread moves exactly ITERS 16-byte pieces (the tile sizes are multiples of
+// 128 pieces): all its loads are issued before the first shared-memory store,
+// so their DRAM latencies overlap instead of adding up.
 template <int ROWS, int KB>
 __device__ __forceinline__ void load_tile(unsigned char *dst, const __nv_bfloat16 *__restrict__ X, long long rs,
                                           long long ks, int r0, int R, int k0, int K, int tid,
                                           unsigned short *stage) {
+    constexpr int ITERS = ROWS * KB / 8 / 128;
+    static_assert(ITERS >= 1 && ROWS * KB / 8 == ITERS * 128, "tile of whole 128-piece rounds");
     const bool row_contig = rs == 1 && ks != 1;
     if (row_contig && (ks & 7) == 0 && r0 + ROWS <= R && (reinterpret_cast<uintptr_t>(X) & 15) == 0) {
         // rows contiguous (an M- or N-major operand): 16-byte loads of 8 rows
         // at one k into a [k][row] staging tile, then each thread gathers the
         // 8 k values of one row into a 16-byte core-matrix row
         constexpr int G = ROWS / 8;
-        for (int e = tid; e < KB * G; e += 128) {
+        uint4 w[ITERS];
+#pragma unroll
+        for (int it = 0; it < ITERS; ++it) {
+            const int e = tid + it * 128;
             const int kk = e / G, g = e - kk * G;
             const int gk = k0 + kk;
-            uint4 w = make_uint4(0u, 0u, 0u, 0u);
-            if (gk < K) w = __ldg(reinterpret_cast<const uint4 *>(X + (long long)(r0 + 8 * g) + (long long)gk * ks));
-            *reinterpret_cast<uint4 *>(stage + kk * ROWS + 8 * g) = w;
+            w[it] = make_uint4(0u, 0u, 0u, 0u);
+            if (gk < K)
+                w[it] = __ldg(reinterpret_cast<const uint4 *>(X + (long long)(r0 + 8 * g) + (long long)gk * ks));
+        }
+#pragma unroll
+        for (int it = 0; it < ITERS; ++it) {
+            const int e = tid + it * 128;
+            const int kk = e / G, g = e - kk * G;
+            *reinterpret_cast<uint4 *>(stage + kk * ROWS + 8 * g) = w[it];
         }
         __syncthreads();
         for (int e = tid; e < ROWS * (KB / 8); e += 128) {
@@ -107,6 +121,23 @@ __device__ __forceinline__ void load_tile(unsigned char *dst, const __nv_bfloat1
         return;
     }
     const bool vec = ks == 1 && (rs & 7) == 0 && ((reinterpret_cast<uintptr_t>(X) & 15) == 0);
+    if (vec && k0 + KB <= K) {
+        // K contiguous and the whole K block inside X: 16-byte loads only
+        // (rows past R are zeros)
+        uint4 w[ITERS];
+#pragma unroll
+        for (int it = 0; it < ITERS; ++it) {
+            const int e = tid + it * 128, r = e / (KB / 8), kc = e % (KB / 8);
+            w[it] = make_uint4(0u, 0u, 0u, 0u);
+            if (r0 + r < R) w[it] = __ldg(reinterpret_cast<const uint4 *>(X + (long long)(r0 + r) * rs + (k0 + kc * 8)));
+        }
+#pragma unroll
+        for (int it = 0; it < ITERS; ++it) {
+            const int e = tid + it * 128, r = e / (KB / 8), kc = e % (KB / 8);
+            *reinterpret_cast<uint4 *>(dst + (r >> 3) * (KB * 16) + kc * 128 + (r & 7) * 16) = w[it];
+        }
+        return;
+    }
     for (int e = tid; e < ROWS * KB / 8; e += 128) {
         int r, kc;
         if (row_contig) {
