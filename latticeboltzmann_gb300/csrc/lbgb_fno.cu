@@ -48,17 +48,78 @@ __global__ void k_gelu_back(const float *__restrict__ dy, const float *__restric
     }
 }
 
+// Four consecutive elements per thread: 16-byte loads and stores, 8-byte
+// stores of the BF16 copies.  The launchers take these when every row is a
+// whole number of float4 and every pointer is aligned; the per-element
+// arithmetic is that of the scalar kernels above, so results are identical.
+__device__ __forceinline__ uint2 pack_bf16x4(float4 y) {
+    const __nv_bfloat162 lo = __floats2bfloat162_rn(y.x, y.y), hi = __floats2bfloat162_rn(y.z, y.w);
+    uint2 r;
+    memcpy(&r.x, &lo, 4);
+    memcpy(&r.y, &hi, 4);
+    return r;
+}
+
+__global__ void k_to_bf16_4(const float4 *__restrict__ x, uint2 *__restrict__ y, long long n4) {
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n4; i += (long long)gridDim.x * blockDim.x)
+        y[i] = pack_bf16x4(x[i]);
+}
+
+__global__ void k_bias_act4(float4 *__restrict__ z, const float *__restrict__ bias, const float4 *__restrict__ extra,
+                            float4 *__restrict__ v, uint2 *__restrict__ vb, long long cols4, int act) {
+    const int c = blockIdx.y;
+    const float b = bias ? bias[c] : 0.f;
+    const long long base = (long long)c * cols4;
+    for (long long j = blockIdx.x * (long long)blockDim.x + threadIdx.x; j < cols4;
+         j += (long long)gridDim.x * blockDim.x) {
+        const long long i = base + j;
+        float4 x = z[i];
+        const float4 e = extra ? extra[i] : make_float4(0.f, 0.f, 0.f, 0.f);
+        x.x = x.x + b + e.x;
+        x.y = x.y + b + e.y;
+        x.z = x.z + b + e.z;
+        x.w = x.w + b + e.w;
+        z[i] = x;
+        const float4 y = act ? make_float4(gelu_f(x.x), gelu_f(x.y), gelu_f(x.z), gelu_f(x.w)) : x;
+        if (v) v[i] = y;
+        if (vb) vb[i] = pack_bf16x4(y);
+    }
+}
+
+__global__ void k_gelu_back4(const float4 *__restrict__ dy, const float4 *__restrict__ z, float4 *__restrict__ dz,
+                             uint2 *__restrict__ dzb, long long n4) {
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n4; i += (long long)gridDim.x * blockDim.x) {
+        const float4 d = dy[i], x = z[i];
+        const float4 g = make_float4(d.x * gelu_df(x.x), d.y * gelu_df(x.y), d.z * gelu_df(x.z), d.w * gelu_df(x.w));
+        dz[i] = g;
+        if (dzb) dzb[i] = pack_bf16x4(g);
+    }
+}
+
 // db[c] = sum_j dy[c, j]: block (chunk, c) sums one of ROWSUM_CHUNKS slices
 // of row c into part[c][chunk]; k_row_sum_finish adds the slices in order
 // (deterministic, and every SM busy however few channels there are).
 constexpr int ROWSUM_CHUNKS = 64;
 
+// V = 4: the row is read as float4 (cols a multiple of 4, dy aligned)
+template <int V>
 __global__ void __launch_bounds__(256) k_row_sum(const float *__restrict__ dy, float *__restrict__ part, long long cols) {
     const int c = blockIdx.y, chunk = blockIdx.x;
-    const long long len = (cols + ROWSUM_CHUNKS - 1) / ROWSUM_CHUNKS;
-    const long long j0 = chunk * len, j1 = j0 + len < cols ? j0 + len : cols;
+    const long long units = cols / V;
+    const long long len = (units + ROWSUM_CHUNKS - 1) / ROWSUM_CHUNKS;
+    const long long j0 = chunk * len, j1 = j0 + len < units ? j0 + len : units;
     float acc = 0.f;
-    for (long long j = j0 + threadIdx.x; j < j1; j += blockDim.x) acc += dy[c * cols + j];
+    for (long long j = j0 + threadIdx.x; j < j1; j += blockDim.x) {
+        if constexpr (V == 4) {
+            const float4 x = reinterpret_cast<const float4 *>(dy + c * cols)[j];
+            acc += x.x;
+            acc += x.y;
+            acc += x.z;
+            acc += x.w;
+        } else {
+            acc += dy[c * cols + j];
+        }
+    }
     __shared__ float sm[256];
     sm[threadIdx.x] = acc;
     __syncthreads();
@@ -252,6 +313,11 @@ using namespace lbgb;
 
 extern "C" int lbgb_fno_to_bf16(const float *x, void *y, long long n, void *stream) {
     if (n <= 0) return LBGB_OK;
+    if (n % 4 == 0 && aligned(x, 16) && aligned(y, 8)) {
+        k_to_bf16_4<<<blocks_for(n / 4), 256, 0, (cudaStream_t)stream>>>(reinterpret_cast<const float4 *>(x),
+                                                                           static_cast<uint2 *>(y), n / 4);
+        return check_launch("k_to_bf16_4");
+    }
     k_to_bf16<<<blocks_for(n), 256, 0, (cudaStream_t)stream>>>(x, static_cast<__nv_bfloat16 *>(y), n);
     return check_launch("k_to_bf16");
 }
@@ -264,9 +330,18 @@ extern "C" int lbgb_fno_bias_act(float *z, const float *bias, const float *extra
         set_error("lbgb_fno_bias_act: at most 65535 channels");
         return LBGB_EINVAL;
     }
-    long long per = (cols + 255) / 256;
+    const bool v4 = cols % 4 == 0 && aligned(z, 16) && (!extra || aligned(extra, 16)) && (!v || aligned(v, 16)) &&
+                    (!vb || aligned(vb, 8));
+    const long long units = v4 ? cols / 4 : cols;
+    long long per = (units + 255) / 256;
     const long long cap = (8192 + channels - 1) / channels;  // ~8192 blocks in all
     const int gx = (int)(per < cap ? (per < 1 ? 1 : per) : cap);
+    if (v4) {
+        k_bias_act4<<<dim3(gx, channels), 256, 0, (cudaStream_t)stream>>>(
+            reinterpret_cast<float4 *>(z), bias, reinterpret_cast<const float4 *>(extra), reinterpret_cast<float4 *>(v),
+            static_cast<uint2 *>(vb), units, act);
+        return check_launch("k_bias_act4");
+    }
     k_bias_act<<<dim3(gx, channels), 256, 0, (cudaStream_t)stream>>>(z, bias, extra, v, static_cast<__nv_bfloat16 *>(vb),
                                                                      cols, act);
     return check_launch("k_bias_act");
@@ -274,6 +349,12 @@ extern "C" int lbgb_fno_bias_act(float *z, const float *bias, const float *extra
 
 extern "C" int lbgb_fno_gelu_back(const float *dy, const float *z, float *dz, void *dzb, long long n, void *stream) {
     if (n <= 0) return LBGB_OK;
+    if (n % 4 == 0 && aligned(dy, 16) && aligned(z, 16) && aligned(dz, 16) && (!dzb || aligned(dzb, 8))) {
+        k_gelu_back4<<<blocks_for(n / 4), 256, 0, (cudaStream_t)stream>>>(
+            reinterpret_cast<const float4 *>(dy), reinterpret_cast<const float4 *>(z), reinterpret_cast<float4 *>(dz),
+            static_cast<uint2 *>(dzb), n / 4);
+        return check_launch("k_gelu_back4");
+    }
     k_gelu_back<<<blocks_for(n), 256, 0, (cudaStream_t)stream>>>(dy, z, dz, static_cast<__nv_bfloat16 *>(dzb), n);
     return check_launch("k_gelu_back");
 }
@@ -285,7 +366,10 @@ extern "C" int lbgb_fno_row_sum(const float *dy, float *db, float *partials, int
         return LBGB_EINVAL;
     }
     cudaStream_t s = (cudaStream_t)stream;
-    k_row_sum<<<dim3(ROWSUM_CHUNKS, channels), 256, 0, s>>>(dy, partials, cols);
+    if (cols % 4 == 0 && aligned(dy, 16))
+        k_row_sum<4><<<dim3(ROWSUM_CHUNKS, channels), 256, 0, s>>>(dy, partials, cols);
+    else
+        k_row_sum<1><<<dim3(ROWSUM_CHUNKS, channels), 256, 0, s>>>(dy, partials, cols);
     int rc = check_launch("k_row_sum");
     if (rc) return rc;
     k_row_sum_finish<<<(channels + 127) / 128, 128, 0, s>>>(partials, db, channels);
