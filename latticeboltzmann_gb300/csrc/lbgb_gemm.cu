@@ -79,10 +79,12 @@ constexpr long long TC_WAIT = 1ll << 22;
 // thread moves exactly ITERS 16-byte pieces (the tile sizes are multiples of
 // 128 pieces): all its loads are issued before the first shared-memory store,
 // so their DRAM latencies overlap instead of adding up.
+// zero_rows: write the zeros of rows past R too; a stage whose zero rows were
+// written by an earlier K block still holds them (they never change).
 template <int ROWS, int KB>
 __device__ __forceinline__ void load_tile(unsigned char *dst, const __nv_bfloat16 *__restrict__ X, long long rs,
                                           long long ks, int r0, int R, int k0, int K, int tid,
-                                          unsigned short *stage) {
+                                          unsigned short *stage, bool zero_rows) {
     constexpr int ITERS = ROWS * KB / 8 / 128;
     static_assert(ITERS >= 1 && ROWS * KB / 8 == ITERS * 128, "tile of whole 128-piece rounds");
     const bool row_contig = rs == 1 && ks != 1;
@@ -134,7 +136,8 @@ __device__ __forceinline__ void load_tile(unsigned char *dst, const __nv_bfloat1
 #pragma unroll
         for (int it = 0; it < ITERS; ++it) {
             const int e = tid + it * 128, r = e / (KB / 8), kc = e % (KB / 8);
-            *reinterpret_cast<uint4 *>(dst + (r >> 3) * (KB * 16) + kc * 128 + (r & 7) * 16) = w[it];
+            if (zero_rows || r0 + r < R)
+                *reinterpret_cast<uint4 *>(dst + (r >> 3) * (KB * 16) + kc * 128 + (r & 7) * 16) = w[it];
         }
         return;
     }
@@ -235,9 +238,9 @@ k_gemm_tc(int M, int N, int K, const __nv_bfloat16 *__restrict__ A, long long a_
         const int k0 = kb * KB;
         unsigned char *sA = sA0 + st * A_BYTES, *sB = sB0 + st * B_BYTES;
         // A tile: 128 rows x KB k; element (r, kk) at (r/8)*KB*16 + (kk/8)*128 + (r%8)*16 + (kk%8)*2
-        load_tile<TC_M, KB>(sA, A, a_rs, a_cs, m0, M, k0, K, tid, stage);
+        load_tile<TC_M, KB>(sA, A, a_rs, a_cs, m0, M, k0, K, tid, stage, kb < ST);
         // B tile: NT rows (n) x KB k, same layout; B(k, n) = B[k * b_rs + n * b_cs]
-        load_tile<NT, KB>(sB, B, b_cs, b_rs, n0, N, k0, K, tid, stage);
+        load_tile<NT, KB>(sB, B, b_cs, b_rs, n0, N, k0, K, tid, stage, kb < ST);
         // make the generic-proxy writes visible to the tensor core
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
         __syncthreads();

@@ -20,7 +20,8 @@ def gemm(A, B, C, alpha=1.0, beta=0.0, engine=0, batch=1, a_bs=0, b_bs=0, c_bs=0
 
 @pytest.mark.parametrize("m,n,k", [(128, 32, 64), (128, 64, 64), (256, 128, 128), (200, 48, 100), (1, 3, 5),
                                    (1000, 24, 256), (384, 96, 32), (130, 130, 70), (4096, 128, 32), (512, 3, 128),
-                                   (512, 24, 24), (300, 64, 33), (2048, 32, 8), (256, 200, 16)])
+                                   (512, 24, 24), (300, 64, 33), (2048, 32, 8), (256, 200, 16),
+                                   (32, 32, 1600), (40, 4, 1000), (160, 32, 704)])
 @pytest.mark.parametrize("layout", ["nn", "nt", "tn", "tt"])
 @pytest.mark.parametrize("engine", [1, 2])
 def test_gemm_matches_float64(cuda, m, n, k, layout, engine):
