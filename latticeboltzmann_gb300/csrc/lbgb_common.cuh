@@ -37,8 +37,9 @@ __host__ __device__ constexpr R wgt(int i) {
 // store h_i = f_i - w_i as 16-bit bits (IEEE half or bfloat16).
 template <int DT> struct Codec;
 
-// DEV: the kernels' values are deviations h_i = f_i - w_i (LBGB_F32DEV) rather
-// than populations; decd/encd convert to and from the population in FP64.
+// DEV: the kernels' values are deviations h_i = f_i - w_i (LBGB_F32DEV and the
+// two 16-bit codecs) rather than populations; decd/encd convert to and from
+// the population in FP64.
 template <> struct Codec<LBGB_F32> {
     using raw = float;
     using real = float;
@@ -79,7 +80,6 @@ constexpr float F16_UNSCALE = 1.0f / 16384.0f;
 // converted operands, in one instruction instead of a conversion and an FMA.
 constexpr unsigned short F16_UNSCALE_BITS = 0x0400;    // half 2^-14
 constexpr unsigned short F16_MINUS_ONE_BITS = 0xbc00;  // half -1
-constexpr unsigned short BF16_ONE_BITS = 0x3f80;       // bfloat16 1
 template <bool BF>
 __device__ __forceinline__ float fma16(unsigned short a, unsigned short b, float c) {
     float d;
@@ -373,11 +373,9 @@ __device__ __forceinline__ float recip_approx(float x) {
 }
 
 // BGK relaxation of one node with its density already summed.
-template <class R, bool APPROX_RCP = false>
+template <class R>
 __device__ __forceinline__ void bgk_relax(R (&f)[9], R omega, R rho, R &ux_out, R &uy_out) {
-    R inv;
-    if constexpr (APPROX_RCP) inv = recip_approx(rho);
-    else inv = recip(rho);
+    const R inv = recip(rho);
     R ux = (f[1] - f[3] + f[5] - f[6] - f[7] + f[8]) * inv;
     R uy = (f[2] - f[4] + f[5] + f[6] - f[7] - f[8]) * inv;
     ux_out = ux;
