@@ -234,6 +234,46 @@ def cpu_port_sample(nx, ny, omega, u0, storage, boundary, budget_s):
     return mlups, cores, sample
 
 
+def _numpy_opt1_worker(job):
+    """One process of the numpy sample: the oracle's numpy step (the
+    reference's cavity_opt1.py arithmetic, bit for bit) on its own strip,
+    started at the common wall-clock time ``go``; returns its end time."""
+    rows, ny, omega, u0, boundary, steps, go = job
+    import numpy as np
+    from oracle import d2q9
+    one, zero = np.ones((rows, ny), np.float32), np.zeros((rows, ny), np.float32)
+    f = d2q9.equilibrium(one, zero, zero)
+    om = np.float32(omega)
+    while time.time() < go:
+        time.sleep(0.001)
+    for _ in range(steps):
+        if boundary == "periodic":
+            d2q9.periodic_step(f, om)
+        else:
+            d2q9.cavity_step(f, om, u0)
+    return time.time()
+
+
+def numpy_opt1_sample(ny, omega, u0, boundary, rows=128, steps=4):
+    """The reference's numpy step (opt1) on the host: one single-threaded
+    process per core, each on its own ``rows`` x ``ny`` strip, all started at
+    one wall-clock time; MLUPS = all processes' cell updates / (last end -
+    start).  The pool is spawned (the parent has a CUDA context)."""
+    import multiprocessing as mp
+    n = os.cpu_count() or 1
+    ctx = mp.get_context("spawn")
+    with ctx.Pool(n) as pool:
+        pool.map(abs, range(n))  # start every worker (interpreter + numpy import) first
+        go = time.time() + 2.0
+        ends = pool.map(_numpy_opt1_worker, [(rows, ny, omega, u0, boundary, steps, go)] * n)
+    el = max(ends) - go
+    mlups = n * rows * ny * steps / el / 1e6
+    script = "shear_wave_opt1.py" if boundary == "periodic" else "cavity_opt1.py"
+    sample = "%d processes x %d steps of a %d x %d %s strip (f32), %.1f s; numpy step of the reference's " \
+             "%s arithmetic, one core per process" % (n, steps, rows, ny, boundary, el, script)
+    return mlups, n, sample
+
+
 def run_reference(args):
     d = Dist(backend="gloo")
     if d.rank != 0:
@@ -383,6 +423,12 @@ def run_ours(args):
         c_mlups, cores, sample = cpu_port_sample(args.nx, args.ny, args.omega, args.u0, args.storage, args.boundary,
                                                  args.cpu_seconds)
         cpu = {"value": round(c_mlups, 3), "unit": UNIT, "cores": cores, "kind": "port", "sample": sample}
+        if args.storage == "f32" and args.boundary in ("cavity", "periodic"):
+            try:
+                n_mlups, n_cores, n_sample = numpy_opt1_sample(args.ny, args.omega, args.u0, args.boundary)
+                cpu["numpy_opt1"] = {"value": round(n_mlups, 3), "unit": UNIT, "cores": n_cores, "sample": n_sample}
+            except Exception as e:  # a baseline that could not run is reported, not hidden
+                cpu["numpy_opt1"] = {"error": "%s: %s" % (type(e).__name__, e)}
     line = {
         "metric": METRIC, "value": round(mlups, 1), "unit": UNIT, "n_gpus": d.world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": round(t_max / args.steps * 1e3, 4), "higher_is_better": True,

@@ -58,3 +58,12 @@ def test_single_process_needs_no_process_group(monkeypatch):
     assert d.world == 1 and d.dist is None
     mlups, t = bench.aggregate_mlups(2_000_000, 5, 0.5, d)
     assert t == 0.5 and abs(mlups - 20.0) < 1e-12
+
+
+def test_numpy_opt1_baseline_runs_one_process_per_core():
+    """The numpy (opt1) CPU baseline: one spawned process per core, each on its
+    own strip, reported as an aggregate over all of them."""
+    import bench
+    mlups, n, sample = bench.numpy_opt1_sample(64, 1.7, 0.1, "cavity", rows=16, steps=2)
+    assert n == (os.cpu_count() or 1)
+    assert mlups > 0 and "%d processes" % n in sample and "cavity_opt1.py" in sample
