@@ -254,7 +254,7 @@ def _numpy_opt1_worker(job):
     return time.time()
 
 
-def numpy_opt1_sample(ny, omega, u0, boundary, rows=128, steps=4):
+def numpy_opt1_sample(ny, omega, u0, boundary, rows=128, steps=12):
     """The reference's numpy step (opt1) on the host: one single-threaded
     process per core, each on its own ``rows`` x ``ny`` strip, all started at
     one wall-clock time; MLUPS = all processes' cell updates / (last end -
