@@ -16,7 +16,9 @@ Lines printed (rank 0, one JSON line):
              the host link sets, the same bytes copied both ways at once
   roofline   HBM roofline of the fused kernel: 72 B/cell/step (FP32) or
              36 B (16-bit deviations) over its CUDA-event launch time
-  cpu_baseline  the oracle's C port of the reference step on the host cores
+  cpu_baseline  the oracle's C port of the reference step on the host cores;
+             cpu_baseline.numpy_opt1: the reference's numpy step, one process
+             per host core
 
 ``--impl reference`` times the CPU implementation of the reference step (the
 C port of the oracle; the reference's own C++ extension needs Eigen, which is
