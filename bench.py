@@ -236,11 +236,29 @@ def cpu_port_sample(nx, ny, omega, u0, storage, boundary, budget_s):
     return mlups, cores, sample
 
 
+def cpu_model():
+    """The host CPU's model name (lscpu), or the machine type."""
+    import platform
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for line in out.splitlines():
+            if line.lower().startswith("model name"):
+                return line.split(":", 1)[1].strip()
+    except (OSError, subprocess.SubprocessError):
+        pass
+    return platform.machine()
+
+
 def _numpy_opt1_worker(job):
-    """One process of the numpy sample: the oracle's numpy step (the
-    reference's cavity_opt1.py arithmetic, bit for bit) on its own strip,
+    """One process of the numpy sample, pinned to its own core: the oracle's
+    numpy step (the reference's opt1 arithmetic, bit for bit) on its own strip,
     started at the common wall-clock time ``go``; returns its end time."""
-    rows, ny, omega, u0, boundary, steps, go = job
+    rows, ny, omega, u0, boundary, steps, go, core = job
+    if core is not None and hasattr(os, "sched_setaffinity"):
+        try:
+            os.sched_setaffinity(0, {core})
+        except OSError:
+            pass
     import numpy as np
     from oracle import d2q9
     one, zero = np.ones((rows, ny), np.float32), np.zeros((rows, ny), np.float32)
@@ -262,17 +280,20 @@ def numpy_opt1_sample(ny, omega, u0, boundary, rows=128, steps=12):
     one wall-clock time; MLUPS = all processes' cell updates / (last end -
     start).  The pool is spawned (the parent has a CUDA context)."""
     import multiprocessing as mp
-    n = os.cpu_count() or 1
+    cores = sorted(os.sched_getaffinity(0)) if hasattr(os, "sched_getaffinity") else list(range(os.cpu_count() or 1))
+    n = len(cores)
     ctx = mp.get_context("spawn")
     with ctx.Pool(n) as pool:
-        pool.map(abs, range(n))  # start every worker (interpreter + numpy import) first
+        pool.map(abs, range(n), chunksize=1)  # start every worker (interpreter + numpy import) first
         go = time.time() + 2.0
-        ends = pool.map(_numpy_opt1_worker, [(rows, ny, omega, u0, boundary, steps, go)] * n)
+        jobs = [(rows, ny, omega, u0, boundary, steps, go, c) for c in cores]
+        ends = pool.map(_numpy_opt1_worker, jobs, chunksize=1)
     el = max(ends) - go
     mlups = n * rows * ny * steps / el / 1e6
     script = "shear_wave_opt1.py" if boundary == "periodic" else "cavity_opt1.py"
     sample = "%d processes x %d steps of a %d x %d %s strip (f32), %.1f s; numpy step of the reference's " \
-             "%s arithmetic, one core per process" % (n, steps, rows, ny, boundary, el, script)
+             "%s arithmetic, one process pinned to each core of %s" % (n, steps, rows, ny, boundary, el, script,
+                                                                      cpu_model())
     return mlups, n, sample
 
 
@@ -424,7 +445,8 @@ def run_ours(args):
     if not args.no_cpu_baseline:
         c_mlups, cores, sample = cpu_port_sample(args.nx, args.ny, args.omega, args.u0, args.storage, args.boundary,
                                                  args.cpu_seconds)
-        cpu = {"value": round(c_mlups, 3), "unit": UNIT, "cores": cores, "kind": "port", "sample": sample}
+        cpu = {"value": round(c_mlups, 3), "unit": UNIT, "cores": cores, "kind": "port", "sample": sample,
+               "cpu_model": cpu_model()}
         if args.storage == "f32" and args.boundary in ("cavity", "periodic"):
             try:
                 n_mlups, n_cores, n_sample = numpy_opt1_sample(args.ny, args.omega, args.u0, args.boundary)
