@@ -115,7 +115,8 @@ def test_resting_walls_conserve_mass(cuda, storage):
     m0 = float(lat.mass_momentum()[0])
     lat.step(500)
     m1 = float(lat.mass_momentum()[0])
-    # CPU emulation of the same arithmetic: f32 5e-6, f16dev 7e-5, bf16dev 1.9e-2
+    # CPU emulation of the same arithmetic: f32 5e-6, f16dev 3.4e-5, bf16dev 1.1e-3
+    # (deviation-form 16-bit collision with the stored-value mass fix)
     tol = {"f32": 1e-4, "f16dev": 1e-3, "bf16dev": 4e-2, "f32dev": 1e-5}[storage]
     assert abs(m1 - m0) < tol, (storage, m1 - m0)
 
