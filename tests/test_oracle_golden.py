@@ -161,3 +161,25 @@ def test_chapman_enskog_beats_equilibrium_on_a_steady_cavity():
     one = np.ones((5, 7))
     np.testing.assert_allclose(oracle.chapman_enskog(one, 0.03 * one, -0.01 * one, 1.2, periodic=True),
                                oracle.equilibrium(one, 0.03 * one, -0.01 * one), atol=1e-16)
+
+
+@pytest.mark.parametrize("impl", ["numpy", "c_port"])
+def test_equilibrium_moments(impl):
+    """Equilibrium moments (the invariants the reference's collide tests rely
+    on): sum f = rho, sum c f = rho u, and sum c_a c_b f = rho (u_a u_b +
+    delta_ab / 3), in both restatements."""
+    rng = np.random.default_rng(5)
+    rho = 1 + 0.05 * rng.standard_normal((6, 7))
+    ux, uy = 0.1 * rng.standard_normal((6, 7)), 0.1 * rng.standard_normal((6, 7))
+    if impl == "numpy":
+        f = oracle.equilibrium(rho, ux, uy)
+    else:
+        f = np.empty((9, 6, 7))
+        port.equilibrium(rho.ravel(), ux.ravel(), uy.ravel(), f.reshape(9, -1), nthreads=1)
+    cx, cy = oracle.CX[:, None, None], oracle.CY[:, None, None]
+    assert np.allclose(f.sum(axis=0), rho, rtol=0, atol=1e-15)
+    assert np.allclose((cx * f).sum(axis=0), rho * ux, rtol=0, atol=1e-15)
+    assert np.allclose((cy * f).sum(axis=0), rho * uy, rtol=0, atol=1e-15)
+    assert np.allclose((cx * cx * f).sum(axis=0), rho * (ux * ux + 1 / 3), rtol=0, atol=1e-14)
+    assert np.allclose((cy * cy * f).sum(axis=0), rho * (uy * uy + 1 / 3), rtol=0, atol=1e-14)
+    assert np.allclose((cx * cy * f).sum(axis=0), rho * ux * uy, rtol=0, atol=1e-14)
