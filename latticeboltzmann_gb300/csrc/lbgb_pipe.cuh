@@ -251,12 +251,11 @@ k_step_pipe(const typename Codec<DT>::raw *__restrict__ src, typename Codec<DT>:
 
         raw *out_row = dst + (size_t)k * ny + c;
         if constexpr (COLLIDE && sizeof(raw) == 2) {
-            // 16-bit deviations: collide in FP32, pack two values per
-            // conversion.  Round to nearest: half storage writes the rest
-            // population last so that each node keeps its mass (see
-            // collide_encode).  Stochastic rounding (sr_step set): both codecs
-            // round every value stochastically and keep the mass the same way
-            // (see collide_encode_sr).
+            // 16-bit deviations: collide in FP32 in deviation form, pack two
+            // values per conversion.  Both codecs write the rest population
+            // last, from the stored values, so that each node keeps its mass
+            // (see collide_encode); with stochastic rounding (sr_step set)
+            // every value is rounded stochastically (see collide_encode_sr).
             constexpr bool sr = SRND;
             if constexpr (DT == LBGB_F16DEV && !SRND) {
                 // FP16, round to nearest: the operations of collide_encode<F16DEV>
