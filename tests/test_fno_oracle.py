@@ -43,3 +43,19 @@ def test_gradients_match_finite_differences():
             x[idx] = old
             fd = (lp - lm) / (2 * eps)
             assert abs(fd - g[name][idx]) <= 1e-6 * max(1.0, abs(fd)), (name, idx, fd, g[name][idx])
+
+
+@pytest.mark.parametrize("H,W,m,pad", [(20, 28, 5, 0.25), (256, 256, 12, 0.25), (32, 24, 4, 0.0)])
+def test_product_dft_matrices_equal_oracle(H, W, m, pad):
+    """The network's transform matrices and padded period (host side of
+    latticeboltzmann_gb300.fno) are the oracle's."""
+    from latticeboltzmann_gb300 import fno as F
+    Hp, Wp = F.padded_size(H, pad), F.padded_size(W, pad)
+    assert (Hp, Wp) == (fno.padded_size(H, pad), fno.padded_size(W, pad))
+    assert Hp % 8 == 0 or pad == 0
+    assert np.array_equal(F.ky_modes(Hp, m), fno.ky_modes(Hp, m))
+    fw, G, iw = F.dft_matrices(H, W, m, Hp, Wp)
+    ofw, ch, sh, oiw = fno.dft_mats(H, W, m, Hp, Wp)
+    np.testing.assert_allclose(fw, ofw, atol=1e-15)
+    np.testing.assert_allclose(G, np.concatenate([ch, sh]), atol=1e-15)
+    np.testing.assert_allclose(iw, oiw, atol=1e-15)

@@ -33,14 +33,6 @@ def setup(cuda, B=2, H=32, W=24, engine=0, seed=0, layers=4):
     return net, a, t, mats, dev_a, dev_t
 
 
-def test_dft_matrices_equal_oracle():
-    fw, G, iw = F.dft_matrices(20, 28, 5, 32, 40)
-    ofw, ch, sh, oiw = ofno.dft_mats(20, 28, 5, 32, 40)
-    np.testing.assert_allclose(fw, ofw, atol=1e-15)
-    np.testing.assert_allclose(G, np.concatenate([ch, sh]), atol=1e-15)
-    np.testing.assert_allclose(iw, oiw, atol=1e-15)
-
-
 @pytest.mark.parametrize("engine", [0, 1])
 @pytest.mark.parametrize("shape", [(2, 32, 24), (3, 40, 40)])
 def test_forward_matches_oracle(cuda, engine, shape):
