@@ -83,3 +83,17 @@ def test_seeded_uneven_batch():
     assert om.min() >= 0.3 and om.max() <= 1.9
     # log-uniform: the median sits near the geometric mean of the range
     assert 100 < np.median(nx) < 330 and 50 < np.median(ny) < 165
+
+
+def test_surrogate_training_parameters():
+    """The surrogate's data set: Re log-uniform over [10, 1000], lid speed
+    uniform over [0.05, 0.1], reproducible from the seed."""
+    from latticeboltzmann_gb300 import surrogate as S
+    re, u = S.sample_parameters(2000, seed=0)
+    re2, u2 = S.sample_parameters(2000, seed=0)
+    assert np.array_equal(re, re2) and np.array_equal(u, u2)
+    assert re.min() >= 10 and re.max() <= 1000 and u.min() >= 0.05 and u.max() <= 0.1
+    # log-uniform: log10(Re) has mean ~2 and each decade holds about half
+    assert abs(np.log10(re).mean() - 2.0) < 0.05
+    assert 0.45 < (re < 100).mean() < 0.55
+    assert abs(u.mean() - 0.075) < 0.002
