@@ -150,8 +150,8 @@ class BatchedLattice:
         return self._init(fields, True)
 
     def _init(self, fields, ce):
-        # FP64 fields for f64 and for FP32 deviations (see Lattice._fill_real)
-        real = torch.float64 if self.storage in ("f64", "f32dev") else torch.float32
+        # FP64 fields for f64 and for every deviation storage (see Lattice._fill_real)
+        real = torch.float32 if self.storage == "f32" else torch.float64
         code = _lib.F64 if real == torch.float64 else _lib.F32
         for b, (nx, ny) in enumerate(self.sizes):
             rho, ux, uy = (torch.as_tensor(x, dtype=real, device=self.device).expand(nx, ny).contiguous()

@@ -130,8 +130,9 @@ class Lattice:
         if self.storage in ("f32", "f64") and f.dtype == self.state.dtype and f.is_contiguous():
             self.state.copy_(f, non_blocking=f.device.type == "cpu" and f.is_pinned())
             return self
-        # FP32 deviations take a float64 input as it is (f - w in FP64, then rounded)
-        real = torch.float64 if self.storage == "f32dev" and f.dtype == torch.float64 else _REAL[self.storage]
+        # deviation storages take a float64 input as it is (f - w in FP64, then rounded)
+        dev = self.storage in ("f32dev", "f16dev", "bf16dev")
+        real = torch.float64 if dev and f.dtype == torch.float64 else _REAL[self.storage]
         src = f.to(device=self.device, dtype=real).contiguous()
         if self.storage in ("f32", "f64"):
             self.state.copy_(src)
@@ -143,9 +144,10 @@ class Lattice:
 
     def _fill_real(self):
         """Arithmetic type of the fields and start populations: FP64 for f64 and
-        for FP32 deviations (whose h = f - w must not inherit the rounding of
-        an FP32 population, e.g. w_i in FP32 at rest), FP32 otherwise."""
-        return torch.float64 if self.storage in ("f64", "f32dev") else torch.float32
+        for every deviation storage (whose h = f - w must not inherit the
+        rounding of an FP32 population: at rest h is then exactly 0, not the
+        ~1e-8 of w_i in FP32), FP32 for f32."""
+        return torch.float32 if self.storage == "f32" else torch.float64
 
     def _fields(self, rho, ux, uy):
         real = self._fill_real()
