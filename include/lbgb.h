@@ -73,11 +73,27 @@ LBGB_API int lbgb_equilibrium(const void *rho, const void *ux, const void *uy, v
                      int64_t n, int64_t chan_stride, int dtype, void *stream);
 
 /* BGK collision in place on f (9 rows of n cells, channel stride chan_stride).
- * Any storage code.
+ * Any storage code.  LBGB_F32 and LBGB_F64 compute exactly the operations of
+ * the reference's native kernel in its order (every operation rounded on
+ * its own, IEEE division, Eigen's fixed-size sum order for rho): the result
+ * equals d2q9_colliden<T> bit for bit.  The deviation codes (LBGB_F32DEV and
+ * the 16-bit codes) collide in deviation form with the mass-preserving store.
  * Replaces: PyLB.Collision.collide -> d2q9_colliden<T>
  *           (PyLB/Collision.py:21, c/d2q9.h:121-131, c/_lbkernels.cpp:40,47). */
 LBGB_API int lbgb_collide(void *f, int64_t n, int64_t chan_stride, int dtype,
                  double omega, void *stream);
+
+/* lbgb_collide with options.  flags = 0: as lbgb_collide.
+ * LBGB_COLLIDE_KEEP_MASS: the fused solver's collision instead, whose FP32
+ * store writes the rest population last as f_0 + sum_{i>0} (f_i - f_i'), so
+ * that each node keeps its mass up to the rounding of that one value (the
+ * native float path drifts by ~1e-2 in 500 steps of a 48 x 40 box with
+ * resting walls, this one by ~5e-6).  Other bits: LBGB_EINVAL.
+ * Same reference interface as lbgb_collide (c/d2q9.h:121-131); the flag has
+ * no counterpart there. */
+#define LBGB_COLLIDE_KEEP_MASS 1
+LBGB_API int lbgb_collide_ex(void *f, int64_t n, int64_t chan_stride, int dtype,
+                    double omega, int flags, void *stream);
 
 /* Periodic streaming, pull form, out of place: dst_i(k,l) = src_i(k-cx_i, l-cy_i)
  * with periodic wrap.  src and dst are (9, nx, ny) and must not overlap.
@@ -165,7 +181,10 @@ LBGB_API int lbgb_mass_momentum(const void *f, int64_t n, int64_t chan_stride, i
  * library until the process exits).  n must not exceed
  * LBGB_NOALLOC_MAX_CELLS (LBGB_EINVAL otherwise).  The first call on a device
  * looks up the array's device address with that device current; make that
- * first call before any stream capture.  All calls share the array: calls
+ * first call before any stream capture.  The address is kept for the life of
+ * the process: a cudaDeviceReset, or anything else that destroys the
+ * device's primary context, invalidates it, so do not call this entry point
+ * on a device after such a reset.  All calls share the array: calls
  * whose kernels overlap on the GPU race and must be ordered (one stream, or
  * events).  No counterpart in the reference (it has no GPU path). */
 #define LBGB_NOALLOC_MAX_CELLS 268435456LL

@@ -14,7 +14,7 @@ from ._tensor import population_view, require_cuda, storage_code, stream_handle
 __all__ = ["collide", "equilibrium"]
 
 
-def collide(f, omega):
+def collide(f, omega, keep_mass=False):
     """Relax populations towards equilibrium, in place (c/d2q9.h:121-131).
 
     Parameters
@@ -25,6 +25,12 @@ def collide(f, omega):
         Modified in place.
     omega : float
         Relaxation parameter.
+    keep_mass : bool
+        False (default): the native kernel's arithmetic operation by
+        operation, so the result equals ``d2q9_colliden`` bit for bit in
+        float32 and float64.  True: the fused solver's collision, whose
+        float32 store writes the rest population last so that each node keeps
+        its mass up to one rounding (no counterpart in the reference).
 
     Returns None, like the reference binding.
     """
@@ -32,7 +38,8 @@ def collide(f, omega):
     code = storage_code(f, "collide")
     if n == 0:
         return None
-    _lib.call("lbgb_collide", f.data_ptr(), n, cs, code, float(omega), stream_handle(f))
+    flags = _lib.COLLIDE_KEEP_MASS if keep_mass else 0
+    _lib.call("lbgb_collide_ex", f.data_ptr(), n, cs, code, float(omega), flags, stream_handle(f))
     return None
 
 

@@ -15,6 +15,8 @@ LIB_PATH = os.path.join(HERE, "liblbgb.so")
 F32, F64, F16DEV, BF16DEV, F32DEV = 0, 1, 2, 3, 4
 # boundary codes
 PERIODIC, CAVITY, CAVITY_LADD = 0, 1, 2
+# lbgb_collide_ex flags
+COLLIDE_KEEP_MASS = 1
 # return codes
 OK, EINVAL, EDTYPE, ECUDA, EWORKSPACE, ETIMEOUT = 0, -1, -2, -3, -4, -5
 
@@ -45,6 +47,7 @@ SIGNATURES = {
     "lbgb_last_error": (_I, [ctypes.c_char_p, _SZ]),
     "lbgb_equilibrium": (_I, [_P, _P, _P, _P, _I64, _I64, _I, _P]),
     "lbgb_collide": (_I, [_P, _I64, _I64, _I, _D, _P]),
+    "lbgb_collide_ex": (_I, [_P, _I64, _I64, _I, _D, _I, _P]),
     "lbgb_stream_periodic": (_I, [_P, _P, _I, _I, _I, _P]),
     "lbgb_stream_bounce_back": (_I, [_P, _P, _I, _I, _D, _I, _P]),
     "lbgb_step_fused": (_I, [_P, _P, _I, _I, _I, _D, _D, _I, _P]),
@@ -146,5 +149,18 @@ def get_tuning(key):
 
 
 def device_status(reset=True):
-    """Synchronize and raise LBGBTimeout if a bounded device-side wait gave up."""
+    """Synchronize and raise LBGBTimeout if a bounded device-side wait of the
+    pipelined step kernels gave up (their output is then incomplete)."""
     check(load().lbgb_device_status(1 if reset else 0), "lbgb_device_status")
+
+
+def gemm_status(reset=True):
+    """Synchronize and raise LBGBTimeout if a bounded wait of the tensor-core
+    GEMM gave up (its output is then incomplete)."""
+    check(load().lbgb_gemm_status(1 if reset else 0), "lbgb_gemm_status")
+
+
+def all_status(reset=True):
+    """Both status words: call at a point that synchronizes anyway."""
+    device_status(reset)
+    gemm_status(reset)

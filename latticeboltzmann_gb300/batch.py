@@ -429,6 +429,10 @@ def _run_to_steady(bl, tol, every, max_steps, log=None, what="", patience=0):
         bl.step(every)
         done += every
         ch = bl.velocity_change().cpu().numpy()
+        # the copy above synchronized: a bounded device-side wait that gave
+        # up (incomplete populations) raises here instead of being reported
+        # as a result
+        _lib.device_status()
         live = state == 0
         change[live] = ch[live]
         conv = live & (ch < tol)

@@ -92,8 +92,8 @@ __device__ __forceinline__ void pull_cell(const typename C::raw *__restrict__ sr
         auto g = [&](int ch, int row, int col) { return C::dec(ld1(src + ch * n + (long long)row * ny + col), ch); };
         const real gN = g(CN, k, T), gNW = g(CNW, k, T), gNE = g(CNE, k, T);
         const real rho_lid = gNW + gN + gNE + g(CNW, ke, T - 1) + g(CN, k, T - 1) + g(CNE, kw, T - 1) + g(CW, ke, T) +
-                             g(C0, k, T) + g(CE, kw, T) + (C::DEV ? real(1) : real(0));
-        const real lid = (real(6) * real(1.0 / 36.0)) * rho_lid * u0;
+                             g(C0, k, T) + g(CE, kw, T);
+        const real lid = lid_from_sum<C>(rho_lid, u0);
         if (k != 0) v[CSE] = gNW + lid;
         if (k != nx - 1) v[CSW] = gNE - lid;
     }

@@ -8,6 +8,9 @@
 #include <stdint.h>
 #include <string.h>
 
+#include <atomic>
+#include <mutex>
+
 #include "lbgb.h"
 
 namespace lbgb {
@@ -417,51 +420,150 @@ __device__ __forceinline__ void bgk_collide(R (&f)[9], R omega) {
     bgk_collide(f, omega, a, b, c);
 }
 
-// BGK in deviation form, h_i = f_i - w_i (the DEV codecs): every
-// intermediate is a small number, so FP32 rounds at ~1e-9 instead of ~3e-8.
-// With D = sum h, rho = 1 + D, j = sum c_i h_i (the weights carry no
-// momentum), u = j / rho:
-//   h_i^eq = w_i (D + rho (cu + cu^2/2 - uu))   (same polynomial as feq)
-//   h_i' = h_i + omega (h_i^eq - h_i),  and h_0' = D - sum_{i>0} h_i' so the
-// node keeps its mass exactly in exact arithmetic of the stored values.
-// APPROX_RCP: 1/rho by the hardware approximation (16-bit storage, whose
-// rounding at 2^-11 or coarser is far above its ~1 ulp).  REST = false leaves
-// h_0 to the caller, which writes it from the rounded stored values.
-// Returns D.
-template <bool APPROX_RCP = false, bool REST = true>
-__device__ __forceinline__ float collide_dev(float (&h)[9], float omega) {
-    float d = h[0];
-#pragma unroll
-    for (int i = 1; i < 9; ++i) d += h[i];
-    const float rho = 1.f + d;
-    const float inv = APPROX_RCP ? recip_approx(rho) : recip(rho);
-    float ux = (h[1] - h[3] + h[5] - h[6] - h[7] + h[8]) * inv;
-    float uy = (h[2] - h[4] + h[5] + h[6] - h[7] - h[8]) * inv;
-    ux *= 3.f;
-    uy *= 3.f;
-    const float uu = (ux * ux + uy * uy) * (1.f / 6.f);
-    const float cu5 = ux + uy, cu6 = uy - ux;
-    const float hx = 0.5f * ux * ux, hy = 0.5f * uy * uy;
-    const float h5 = 0.5f * cu5 * cu5, h6 = 0.5f * cu6 * cu6;
-    float q[9];
-    q[0] = -uu;
-    q[1] = ux + hx - uu;
-    q[2] = uy + hy - uu;
-    q[3] = -ux + hx - uu;
-    q[4] = -uy + hy - uu;
-    q[5] = cu5 + h5 - uu;
-    q[6] = cu6 + h6 - uu;
-    q[7] = -cu5 + h5 - uu;
-    q[8] = -cu6 + h6 - uu;
-    float rest = d;
+// IEEE operations rounded one by one: the compiler may not contract them into
+// FMAs or replace a division by a reciprocal multiply.
+template <class R> struct Ieee;
+template <> struct Ieee<float> {
+    static __device__ __forceinline__ float add(float a, float b) { return __fadd_rn(a, b); }
+    static __device__ __forceinline__ float sub(float a, float b) { return __fsub_rn(a, b); }
+    static __device__ __forceinline__ float mul(float a, float b) { return __fmul_rn(a, b); }
+    static __device__ __forceinline__ float div(float a, float b) { return __fdiv_rn(a, b); }
+};
+template <> struct Ieee<double> {
+    static __device__ __forceinline__ double add(double a, double b) { return __dadd_rn(a, b); }
+    static __device__ __forceinline__ double sub(double a, double b) { return __dsub_rn(a, b); }
+    static __device__ __forceinline__ double mul(double a, double b) { return __dmul_rn(a, b); }
+    static __device__ __forceinline__ double div(double a, double b) { return __ddiv_rn(a, b); }
+};
+
+// The BGK collision of the reference's native kernel, operation by operation
+// (d2q9_colliden, c/d2q9.h:121-131, with d2q9_equilibrium1, c/d2q9.h:59-81):
+//   rho = f_i.sum()  -- Eigen 3.4 reduces a fixed-size 9-vector by an
+//                       unrolled halving split: ((f0+f1)+(f2+f3)) +
+//                       ((f4+f5)+(f6+(f7+f8)))
+//   ux = (f1-f3+f5-f6-f7+f8)/rho, uy = (f2-f4+f5+f6-f7-f8)/rho (left to right)
+//   w0 = 4 rho/9, w1 = rho/9, w5 = rho/36; ux *= 3; uy *= 3
+//   uu = (ux ux + uy uy)/6; feq_i = w_i (((1 + cu) + cu cu/2) - uu)
+//   f_i += omega (feq_i - f_i)
+// Every operation is rounded on its own (the x86-64 build of the reference
+// has no FMA), so FP32 and FP64 results equal the native kernel's bit for bit.
+// d2q9_equilibrium1 (c/d2q9.h:59-81) operation by operation.
+template <class R>
+__device__ __forceinline__ void equilibrium_native(R rho, R ux, R uy, R (&feq)[9]) {
+    using O = Ieee<R>;
+    const R w0 = O::div(O::mul(R(4), rho), R(9)), w1 = O::div(rho, R(9)), w5 = O::div(rho, R(36));
+    ux = O::mul(ux, R(3));
+    uy = O::mul(uy, R(3));
+    const R cu[9] = {R(0), ux, uy, -ux, -uy, O::add(ux, uy), O::add(-ux, uy), O::sub(-ux, uy), O::sub(ux, uy)};
+    const R uu = O::div(O::add(O::mul(ux, ux), O::mul(uy, uy)), R(6));
+    feq[0] = O::mul(w0, O::sub(R(1), uu));
 #pragma unroll
     for (int i = 1; i < 9; ++i) {
-        const float heq = wgt<float>(i) * fmaf(rho, q[i], d);
-        h[i] += omega * (heq - h[i]);
-        rest -= h[i];
+        // 1 - ux is rounded as 1 + (-ux): the same IEEE result
+        const R p = O::sub(O::add(O::add(R(1), cu[i]), O::div(O::mul(cu[i], cu[i]), R(2))), uu);
+        feq[i] = O::mul(i <= 4 ? w1 : w5, p);
     }
-    if constexpr (REST) h[0] = rest;
+}
+
+template <class R>
+__device__ __forceinline__ void bgk_collide_native(R (&f)[9], R omega) {
+    using O = Ieee<R>;
+    const R rho = O::add(O::add(O::add(f[0], f[1]), O::add(f[2], f[3])),
+                         O::add(O::add(f[4], f[5]), O::add(f[6], O::add(f[7], f[8]))));
+    R jx = O::sub(f[1], f[3]);
+    jx = O::sub(O::sub(O::add(jx, f[5]), f[6]), f[7]);
+    jx = O::add(jx, f[8]);
+    R jy = O::sub(f[2], f[4]);
+    jy = O::sub(O::add(O::add(jy, f[5]), f[6]), f[7]);
+    jy = O::sub(jy, f[8]);
+    R feq[9];
+    equilibrium_native(rho, O::div(jx, rho), O::div(jy, rho), feq);
+#pragma unroll
+    for (int i = 0; i < 9; ++i) f[i] = O::add(f[i], O::mul(omega, O::sub(feq[i], f[i])));
+}
+
+// BGK in deviation form, h_i = f_i - w_i (the DEV codecs and the FP32
+// kernels), arranged so that the collision conserves momentum by construction.
+//
+// FP32 rounding of the constants (w_i = 1/9, 1/36; 2/3 = 6 w_1) makes a
+// directly evaluated equilibrium carry the momentum j (1 + delta) with
+// delta ~ 3e-8, at every node and step: a systematic error that adds up
+// (64^2 cavity, omega 1.7, 1000 steps: 4e-6 relative L2 of u against FP64,
+// where the rounding of the stored deviations alone gives 8e-8).  Only
+// errors in the conserved moments accumulate -- an error in any other moment
+// is relaxed away -- so the collision works on the even and odd parts of
+// each pair of opposite channels,
+//   a_ij = h_i - h_j,  b_ij = h_i + h_j     (pairs 1|3, 2|4, 5|7, 6|8),
+// with D = h_0 + sum b, j_x = a13 + a57 - a68, j_y = a24 + a57 + a68,
+// rho = 1 + D, u = j / rho:
+//   even part (no momentum):  g = w (D - 1.5 j.u + 4.5 (c.j)(c.u)) - b/2
+//   odd part of the diagonals: d57 = (j_x + j_y)/12 - a57/2,
+//                              d68 = (j_y - j_x)/12 - a68/2
+//   odd part of the axes, from the diagonals' (exact algebra of
+//   w_i rho 3 c.u with the axis pairs taking the rest of j):
+//                              d13 = d68 - d57,  d24 = -(d57 + d68)
+//   h_i' = h_i + omega (g +/- d)  (+ for the first channel of the pair).
+// The momentum change 2 omega (d13 + d57 - d68, d24 + d57 + d68) is then zero
+// whatever the rounding of d57 and d68, and only the final stores round
+// momentum.  1/rho enters second-order terms alone (hardware approximation).
+// h_0' = D - sum_{i>0} h_i' keeps the node's mass in exact arithmetic of the
+// stored values.  In the CPU emulation of this arithmetic the 64^2 cavity is
+// at 9e-8 after 1000 and 2000 steps, the storage floor.  Same equilibrium as
+// w_i rho (1 + 3 c.u + 4.5 (c.u)^2 - 1.5 u^2) (c/d2q9.h:59-81) in exact
+// arithmetic.  REST = false leaves h_0 to the caller, which writes it from
+// the rounded stored values.  Returns D.
+template <bool REST = true>
+__device__ __forceinline__ float collide_dev(float (&h)[9], float omega) {
+    const float a13 = h[1] - h[3], b13 = h[1] + h[3];
+    const float a24 = h[2] - h[4], b24 = h[2] + h[4];
+    const float a57 = h[5] - h[7], b57 = h[5] + h[7];
+    const float a68 = h[6] - h[8], b68 = h[6] + h[8];
+    const float d = (((h[0] + b13) + b24) + b57) + b68;
+    const float jx = (a13 + a57) - a68, jy = (a24 + a57) + a68;
+    const float inv = recip_approx(1.f + d);
+    const float ux = jx * inv, uy = jy * inv;
+    const float base = fmaf(-1.5f, fmaf(jx, ux, jy * uy), d);
+    const float sx = jx + jy, sy = jy - jx;
+    const float g13 = fmaf(-0.5f, b13, (1.f / 9.f) * fmaf(4.5f * jx, ux, base));
+    const float g24 = fmaf(-0.5f, b24, (1.f / 9.f) * fmaf(4.5f * jy, uy, base));
+    const float g57 = fmaf(-0.5f, b57, (1.f / 36.f) * fmaf(4.5f * sx, ux + uy, base));
+    const float g68 = fmaf(-0.5f, b68, (1.f / 36.f) * fmaf(4.5f * sy, uy - ux, base));
+    const float d57 = fmaf(sx, 1.f / 12.f, -0.5f * a57);
+    const float d68 = fmaf(sy, 1.f / 12.f, -0.5f * a68);
+    const float d13 = d68 - d57, d24 = -(d57 + d68);
+    h[1] = fmaf(omega, g13 + d13, h[1]);
+    h[3] = fmaf(omega, g13 - d13, h[3]);
+    h[2] = fmaf(omega, g24 + d24, h[2]);
+    h[4] = fmaf(omega, g24 - d24, h[4]);
+    h[5] = fmaf(omega, g57 + d57, h[5]);
+    h[7] = fmaf(omega, g57 - d57, h[7]);
+    h[6] = fmaf(omega, g68 + d68, h[6]);
+    h[8] = fmaf(omega, g68 - d68, h[8]);
+    if constexpr (REST) {
+        float rest = d;
+#pragma unroll
+        for (int i = 1; i < 9; ++i) rest -= h[i];
+        h[0] = rest;
+    }
     return d;
+}
+
+// The reference lid's Ladd term ((6 w) rho_lid) u0 (cavity_opt1.py:211-212),
+// each product rounded on its own, so that the following g +/- term cannot
+// be contracted into an FMA: the FP32 and FP64 results then equal the
+// reference's rounding of the same expression.
+template <class R>
+__device__ __forceinline__ R lid_term(R rho_lid, R u0) {
+    return Ieee<R>::mul(Ieee<R>::mul(R(6) * R(1.0 / 36.0), rho_lid), u0);
+}
+
+// The same term for deviation storage, where the nine summed lid values are
+// deviations and rho_lid = 1 + s: c + c s with c = (6 w) u0 rounded once, so
+// that the low bits of s are not lost in a rounding of 1 + s (which would
+// repeat itself at every lid node and step).
+__device__ __forceinline__ float lid_term_dev(float s, float u0) {
+    const float c = (6.f * (1.f / 36.f)) * u0;
+    return fmaf(c, s, c);
 }
 
 // Equilibrium of one node (same formulation as above).
@@ -486,6 +588,16 @@ __device__ __forceinline__ void equilibrium1(R rho, R ux, R uy, R (&feq)[9]) {
     feq[8] = w5 * (base - cu6 + h6);
 }
 
+// The lid's Ladd term from the sum s of the nine lid values of the lid
+// density (populations: s = rho_lid; deviations: s = rho_lid - 1).
+template <class C>
+__device__ __forceinline__ typename C::real lid_from_sum(typename C::real s, typename C::real u0) {
+    if constexpr (C::DEV)
+        return lid_term_dev(s, u0);
+    else
+        return lid_term(s, u0);
+}
+
 // ---------------------------------------------------------------- conservation
 // BGK conserves mass exactly; rounding the nine relaxed values does not, and in
 // a slowly varying flow the same rounding repeats step after step and adds up
@@ -508,14 +620,22 @@ __device__ __forceinline__ void collide_encode(typename Codec<DT>::real (&f)[9],
     using C = Codec<DT>;
     using real = typename C::real;
     if constexpr (DT == LBGB_F32) {
-        real pre[9];
+        // FP32 populations collide in the deviation pair form too: h = f - w
+        // (w as stored by the rest state, so the rest state stays a fixed
+        // point), collide_dev, f' = h' + w; the populations' own rounding is
+        // then the only systematic error left
+        real h[9];
 #pragma unroll
-        for (int i = 0; i < 9; ++i) pre[i] = f[i];
-        bgk_collide(f, omega);
-        real d = pre[1] - f[1];
+        for (int i = 0; i < 9; ++i) h[i] = f[i] - wgt<float>(i);
+        collide_dev<false>(h, omega);
+        real d = 0.f;
 #pragma unroll
-        for (int i = 2; i < 9; ++i) d += pre[i] - f[i];
-        f[0] = pre[0] + d;
+        for (int i = 1; i < 9; ++i) {
+            const real fi = h[i] + wgt<float>(i);
+            d += f[i] - fi;
+            f[i] = fi;
+        }
+        f[0] += d;
 #pragma unroll
         for (int i = 0; i < 9; ++i) out[i] = f[i];
     } else if constexpr (DT == LBGB_F32DEV) {
@@ -527,7 +647,7 @@ __device__ __forceinline__ void collide_encode(typename Codec<DT>::real (&f)[9],
         // mass deviation D S minus what the other eight stored values carry,
         // so the node keeps its mass up to the rounding of h_0 alone.  The
         // pipelined kernel does the same operations.
-        real dms = collide_dev<true, false>(f, omega) * F16_SCALE;
+        real dms = collide_dev<false>(f, omega) * F16_SCALE;
 #pragma unroll
         for (int i = 1; i < 9; ++i) {
             out[i] = C::enc_h(f[i]);
@@ -535,7 +655,7 @@ __device__ __forceinline__ void collide_encode(typename Codec<DT>::real (&f)[9],
         }
         out[0] = __half_as_ushort(__float2half_rn(dms));
     } else if constexpr (DT == LBGB_BF16DEV) {
-        real dm = collide_dev<true, false>(f, omega);
+        real dm = collide_dev<false>(f, omega);
 #pragma unroll
         for (int i = 1; i < 9; ++i) {
             out[i] = C::enc_h(f[i]);
@@ -555,7 +675,7 @@ __device__ __forceinline__ void collide_encode(typename Codec<DT>::real (&f)[9],
 template <int DT>
 __device__ __forceinline__ void collide_encode_sr(float (&f)[9], float omega, unsigned short (&out)[9], uint32_t key,
                                                   uint32_t cell) {
-    float dm = collide_dev<true, false>(f, omega);
+    float dm = collide_dev<false>(f, omega);
     const uint32_t base = sr_pair_base(key, cell & ~1u);
     const bool odd = (cell & 1u) != 0u;
     // the cell's own lane of the pair's word, as the packet kernels round it
@@ -583,6 +703,16 @@ inline int current_device() {
     int d = 0;
     if (cudaGetDevice(&d) != cudaSuccess || d < 0) d = 0;
     return d < MAX_DEVICES ? d : MAX_DEVICES - 1;
+}
+
+// One lock for the first-use set-up of the per-device host caches (kernel
+// attributes, device properties).  The caches are atomics read without the
+// lock; a thread that finds an entry unset takes the lock, sets it up and
+// publishes it, so no kernel is launched before its set-up is complete when
+// two host threads launch the same variant at once.
+inline std::mutex &setup_mutex() {
+    static std::mutex m;
+    return m;
 }
 
 inline bool aligned(const void *p, size_t a) { return (reinterpret_cast<uintptr_t>(p) % a) == 0; }

@@ -407,10 +407,11 @@ k_gemm_simt(int M, int N, int K, const __nv_bfloat16 *__restrict__ A, long long 
 // that no allocation ever waits.  Computed once per variant and device.
 template <int NT, typename OUT, int KB, int ST>
 static int tc_dyn_smem() {
-    static int cache[MAX_DEVICES];
-    static bool have[MAX_DEVICES] = {};
+    static std::atomic<int> cache[MAX_DEVICES];
     const int dev = current_device();
-    if (have[dev]) return cache[dev];
+    const int have = cache[dev].load(std::memory_order_acquire);
+    if (have) return have;
+    std::lock_guard<std::mutex> lock(setup_mutex());
     int d = tc_operand_bytes<NT, KB, ST>() + tc_stage_bytes<KB>();
     for (;;) {
         cudaFuncSetAttribute(k_gemm_tc<NT, OUT, KB, ST>, cudaFuncAttributeMaxDynamicSharedMemorySize, d);
@@ -420,8 +421,7 @@ static int tc_dyn_smem() {
         if (nb * NT <= 512 || d >= 200 * 1024) break;
         d += 1024;
     }
-    cache[dev] = d;
-    have[dev] = true;
+    cache[dev].store(d, std::memory_order_release);
     return d;
 }
 

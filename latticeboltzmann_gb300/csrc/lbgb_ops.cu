@@ -36,12 +36,14 @@ static int grid_for(int64_t items, int threads) {
 }
 
 // ---------------------------------------------------------------- equilibrium
+// The native kernel's operations in its order (d2q9_equilibriumn,
+// c/d2q9.h:98-108): bit for bit the reference's float and double results.
 template <class T>
 __global__ void k_equilibrium(const T *__restrict__ rho, const T *__restrict__ ux, const T *__restrict__ uy,
                               T *__restrict__ f, int64_t n, int64_t cs) {
     for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < n; c += (int64_t)gridDim.x * blockDim.x) {
         T feq[9];
-        equilibrium1<T>(rho[c], ux[c], uy[c], feq);
+        equilibrium_native<T>(rho[c], ux[c], uy[c], feq);
 #pragma unroll
         for (int i = 0; i < 9; ++i) f[i * cs + c] = feq[i];
     }
@@ -94,8 +96,11 @@ __global__ void k_chapman_enskog(const T *__restrict__ rho, const T *__restrict_
 
 // ---------------------------------------------------------------- collide
 // One thread relaxes V consecutive cells; vector access when the channel
-// stride and the pointer allow it, else element by element.
-template <int DT, int V>
+// stride and the pointer allow it, else element by element.  NATIVE (FP32
+// and FP64 only): the reference native kernel's arithmetic, operation by
+// operation (bgk_collide_native); otherwise the solver's collision with its
+// mass-preserving store (collide_encode).
+template <int DT, int V, bool NATIVE>
 __global__ void k_collide(typename Codec<DT>::raw *__restrict__ f, int64_t n, int64_t cs,
                           typename Codec<DT>::real omega) {
     using C = Codec<DT>;
@@ -128,7 +133,13 @@ __global__ void k_collide(typename Codec<DT>::raw *__restrict__ f, int64_t n, in
             raw r[9];
 #pragma unroll
             for (int i = 0; i < 9; ++i) x[i] = v[i][j];
-            collide_encode<DT>(x, omega, r);
+            if constexpr (NATIVE) {
+                bgk_collide_native(x, omega);
+#pragma unroll
+                for (int i = 0; i < 9; ++i) r[i] = x[i];
+            } else {
+                collide_encode<DT>(x, omega, r);
+            }
 #pragma unroll
             for (int i = 0; i < 9; ++i) out[i][j] = r[i];
         }
@@ -142,16 +153,16 @@ __global__ void k_collide(typename Codec<DT>::raw *__restrict__ f, int64_t n, in
     }
 }
 
-template <int DT>
+template <int DT, bool NATIVE>
 static int launch_collide(void *f, int64_t n, int64_t cs, double omega, cudaStream_t s) {
     using C = Codec<DT>;
     constexpr int VW = 16 / sizeof(typename C::raw);
     if (cs % VW == 0 && aligned(f, 16)) {
-        k_collide<DT, VW><<<grid_for((n + VW - 1) / VW, 256), 256, 0, s>>>(static_cast<typename C::raw *>(f), n,
-                                                                          cs, (typename C::real)omega);
+        k_collide<DT, VW, NATIVE><<<grid_for((n + VW - 1) / VW, 256), 256, 0, s>>>(
+            static_cast<typename C::raw *>(f), n, cs, (typename C::real)omega);
     } else {
-        k_collide<DT, 1><<<grid_for(n, 256), 256, 0, s>>>(static_cast<typename C::raw *>(f), n, cs,
-                                                          (typename C::real)omega);
+        k_collide<DT, 1, NATIVE><<<grid_for(n, 256), 256, 0, s>>>(static_cast<typename C::raw *>(f), n, cs,
+                                                                  (typename C::real)omega);
     }
     return check_launch("k_collide");
 }
@@ -593,19 +604,34 @@ extern "C" int lbgb_copy_rows(void *dst, const void *src, int nx, int ny, int k_
     return LBGB_OK;
 }
 
-extern "C" int lbgb_collide(void *f, int64_t n, int64_t chan_stride, int dtype, double omega, void *stream) {
+extern "C" int lbgb_collide_ex(void *f, int64_t n, int64_t chan_stride, int dtype, double omega, int flags,
+                               void *stream) {
     int rc = check_cells(f, n, chan_stride, dtype, "lbgb_collide");
     if (rc) return rc;
+    if (flags & ~LBGB_COLLIDE_KEEP_MASS) {
+        set_error("lbgb_collide_ex: unknown flags 0x%x", flags);
+        return LBGB_EINVAL;
+    }
     if (n == 0) return LBGB_OK;
     cudaStream_t s = (cudaStream_t)stream;
+    const bool keep = (flags & LBGB_COLLIDE_KEEP_MASS) != 0;
     switch (dtype) {
-    case LBGB_F32: return launch_collide<LBGB_F32>(f, n, chan_stride, omega, s);
-    case LBGB_F64: return launch_collide<LBGB_F64>(f, n, chan_stride, omega, s);
-    case LBGB_F16DEV: return launch_collide<LBGB_F16DEV>(f, n, chan_stride, omega, s);
-    case LBGB_BF16DEV: return launch_collide<LBGB_BF16DEV>(f, n, chan_stride, omega, s);
-    case LBGB_F32DEV: return launch_collide<LBGB_F32DEV>(f, n, chan_stride, omega, s);
+    case LBGB_F32:
+        return keep ? launch_collide<LBGB_F32, false>(f, n, chan_stride, omega, s)
+                    : launch_collide<LBGB_F32, true>(f, n, chan_stride, omega, s);
+    case LBGB_F64:
+        return keep ? launch_collide<LBGB_F64, false>(f, n, chan_stride, omega, s)
+                    : launch_collide<LBGB_F64, true>(f, n, chan_stride, omega, s);
+    // the deviation storages always keep each node's mass through the stored values
+    case LBGB_F16DEV: return launch_collide<LBGB_F16DEV, false>(f, n, chan_stride, omega, s);
+    case LBGB_BF16DEV: return launch_collide<LBGB_BF16DEV, false>(f, n, chan_stride, omega, s);
+    case LBGB_F32DEV: return launch_collide<LBGB_F32DEV, false>(f, n, chan_stride, omega, s);
     }
     return LBGB_EDTYPE;
+}
+
+extern "C" int lbgb_collide(void *f, int64_t n, int64_t chan_stride, int dtype, double omega, void *stream) {
+    return lbgb_collide_ex(f, n, chan_stride, dtype, omega, 0, stream);
 }
 
 extern "C" int lbgb_macroscopic(const void *f, void *rho, void *ux, void *uy, int64_t n, int64_t chan_stride,

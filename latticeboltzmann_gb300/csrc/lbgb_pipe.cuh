@@ -14,8 +14,9 @@
 // then in shared memory.  Only the cells of the first and last column of a
 // row fetch their wrap-around or wall values from global memory.
 //
-// With ~37 KB per stage and 5 stages about 185 KB per SM are in flight,
-// independent of how long the consumers spend in the collision.
+// A stage holds ~37 KB (FP32: 9 channels x 1032 cells); with the default
+// two stages ~74 KB per SM are in flight, independent of how long the
+// consumers spend in the collision (deeper rings measured slower).
 //
 // Every mbarrier wait is bounded.  A wait that gives up records a code in a
 // device-side status word and makes its warp leave the tile loop; the
@@ -240,8 +241,8 @@ k_step_pipe(const typename Codec<DT>::raw *__restrict__ src, typename Codec<DT>:
                     const int ke = (k == nx - 1) ? 0 : k + 1;
                     const real gN = g(CN, k, T), gNW = g(CNW, k, T), gNE = g(CNE, k, T);
                     const real rho_lid = gNW + gN + gNE + g(CNW, ke, T - 1) + g(CN, k, T - 1) + g(CNE, kw, T - 1) +
-                                         g(CW, ke, T) + g(C0, k, T) + g(CE, kw, T) + (C::DEV ? real(1) : real(0));
-                    const real lid = (real(6) * real(1.0 / 36.0)) * rho_lid * u0;
+                                         g(CW, ke, T) + g(C0, k, T) + g(CE, kw, T);
+                    const real lid = lid_from_sum<C>(rho_lid, u0);
                     v[CS][NC - 1] = gN;
                     v[CSE][NC - 1] = (k == 0) ? gNW : gNW + lid;
                     v[CSW][NC - 1] = (k == nx - 1) ? gNE : gNE - lid;
@@ -267,7 +268,7 @@ k_step_pipe(const typename Codec<DT>::raw *__restrict__ src, typename Codec<DT>:
                     real h[9];
 #pragma unroll
                     for (int i = 0; i < 9; ++i) h[i] = v[i][j];
-                    hs[0][j] = collide_dev<true, false>(h, omega) * F16_SCALE;
+                    hs[0][j] = collide_dev<false>(h, omega) * F16_SCALE;
 #pragma unroll
                     for (int i = 1; i < 9; ++i) hs[i][j] = h[i] * F16_SCALE;
                 }
@@ -298,7 +299,7 @@ k_step_pipe(const typename Codec<DT>::raw *__restrict__ src, typename Codec<DT>:
                 real h[9];
 #pragma unroll
                 for (int i = 0; i < 9; ++i) h[i] = v[i][j];
-                dm[j] = collide_dev<true, !keep_mass>(h, omega);
+                dm[j] = collide_dev<!keep_mass>(h, omega);
 #pragma unroll
                 for (int i = 0; i < 9; ++i) hpost[i][j] = sr ? sr_dev<DT>(h[i]) : h[i];
             }

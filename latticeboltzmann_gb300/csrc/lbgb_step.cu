@@ -168,8 +168,8 @@ __device__ __forceinline__ void step_segment(const typename Codec<DT>::raw *__re
                                      load_one<C>(src, cs, ny, CN, k, T - 1) +
                                      load_one<C>(src, cs, ny, CNE, kw, T - 1) +
                                      load_one<C>(src, cs, ny, CW, ke, T) + load_one<C>(src, cs, ny, C0, k, T) +
-                                     load_one<C>(src, cs, ny, CE, kw, T) + (C::DEV ? real(1) : real(0));
-                const real lid = (real(6) * real(1.0 / 36.0)) * rho_lid * u0;
+                                     load_one<C>(src, cs, ny, CE, kw, T);
+                const real lid = lid_from_sum<C>(rho_lid, u0);
                 v[CS][V - 1] = gN;
                 v[CSE][V - 1] = (k == 0) ? gNW : gNW + lid;
                 v[CSW][V - 1] = (k == nx - 1) ? gNE : gNE - lid;
@@ -229,14 +229,16 @@ k_step(const typename Codec<DT>::raw *__restrict__ src, typename Codec<DT>::raw 
 
 // ---------------------------------------------------------------- launch
 static int sm_count() {
-    static int cache[MAX_DEVICES] = {};
+    static std::atomic<int> cache[MAX_DEVICES];
     const int dev = current_device();
-    if (cache[dev] == 0) {
-        int n = 0;
-        cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
-        cache[dev] = n > 0 ? n : 1;
-    }
-    return cache[dev];
+    int v = cache[dev].load(std::memory_order_acquire);
+    if (v) return v;
+    std::lock_guard<std::mutex> lock(setup_mutex());
+    int n = 0;
+    cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+    v = n > 0 ? n : 1;
+    cache[dev].store(v, std::memory_order_release);
+    return v;
 }
 
 struct SR {
@@ -280,14 +282,16 @@ struct Tuning {
 static Tuning g_tune;
 
 static int max_dyn_smem() {
-    static int cache[MAX_DEVICES] = {};
+    static std::atomic<int> cache[MAX_DEVICES];
     const int dev = current_device();
-    if (cache[dev] == 0) {
-        int v = 0;
-        cudaDeviceGetAttribute(&v, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
-        cache[dev] = v > 0 ? v : 48 * 1024;
-    }
-    return cache[dev];
+    int v = cache[dev].load(std::memory_order_acquire);
+    if (v) return v;
+    std::lock_guard<std::mutex> lock(setup_mutex());
+    int n = 0;
+    cudaDeviceGetAttribute(&n, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    v = n > 0 ? n : 48 * 1024;
+    cache[dev].store(v, std::memory_order_release);
+    return v;
 }
 
 template <int DT, int BC, bool COLLIDE>
@@ -308,16 +312,17 @@ static int launch_pipe(const void *src, void *dst, int nx, int ny, double omega,
     const int grid = (int)(total < slots ? total : slots);
     const bool srnd = sizeof(raw) == 2 && COLLIDE && sr.step != nullptr;
     // the dynamic shared-memory limit is raised once per kernel variant and device
-    static bool attr_set[MAX_DEVICES][2] = {};
+    static std::atomic<bool> attr_set[MAX_DEVICES][2];
     const int dev = current_device();
     auto go = [&](auto kernel, int variant) -> int {
-        if (!attr_set[dev][variant]) {
+        if (!attr_set[dev][variant].load(std::memory_order_acquire)) {
+            std::lock_guard<std::mutex> lock(setup_mutex());
             cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smax);
             if (e != cudaSuccess) {
                 set_error("k_step_pipe: cannot reserve %d bytes of shared memory: %s", smax, cudaGetErrorString(e));
                 return LBGB_ECUDA;
             }
-            attr_set[dev][variant] = true;
+            attr_set[dev][variant].store(true, std::memory_order_release);
         }
         kernel<<<grid, (SH::NCW + 1) * 32, smem, s>>>(
             static_cast<const raw *>(src), static_cast<raw *>(dst), nx, ny, (int)tpr, (int)total, stages,

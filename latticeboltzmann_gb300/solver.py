@@ -214,7 +214,7 @@ class Lattice:
         return out
 
     # ------------------------------------------------------------------ host-resident populations
-    def step_host(self, f, n=1, blocks=48):
+    def step_host(self, f, n=1, blocks=48, check=True):
         """Advance populations that live in host memory by ``n`` steps, in place.
 
         ``f``: a pinned, contiguous ``(9, nx, ny)`` host tensor of the storage's
@@ -228,6 +228,12 @@ class Lattice:
         device state ends up holding the same populations as ``f``.  At
         8192^2 FP32, 32-64 blocks run at 15.3 ms per step (8 blocks: 18.0 ms;
         the transfers alone take 14.1 ms at the link's two-way rate).
+
+        check=True (default): wait for the last download and raise
+        LBGBTimeout if a bounded device-side wait of a step gave up, so that
+        ``f`` is complete and valid when the call returns; check=False
+        returns at once, with the downloads still in flight on the current
+        stream.
         """
         if self.storage not in ("f32", "f64"):
             raise ValueError("step_host needs f32 or f64 storage (the host array holds the populations as they are)")
@@ -270,7 +276,17 @@ class Lattice:
             self._cur = 1 - self._cur
             self.steps_taken += 1
         s_cmp.wait_stream(s_out)
+        if check:
+            _lib.device_status()
         return f
+
+    def check(self):
+        """Synchronize and raise LBGBTimeout if a bounded device-side wait of
+        a step launched so far gave up (the populations are then incomplete).
+        ``step`` stays asynchronous; call this where the caller synchronizes
+        anyway (before reading results)."""
+        _lib.device_status()
+        return self
 
     # ------------------------------------------------------------------ stepping
     def step(self, n=1):

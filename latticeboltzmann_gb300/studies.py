@@ -92,9 +92,17 @@ def shear_wave(nx=64, ny=128, omega=1.0, steps=2000, amplitude=0.05, storage="f6
     return {"nu_fit": float(-slope / k ** 2), "nu_theory": viscosity_from_omega(omega)}
 
 
+def _u64(lat):
+    """Velocity of the stored populations, decoded and computed in FP64 (an
+    FP32 velocity would add its own rounding, ~1e-7 relative, to the error
+    being measured)."""
+    from .solver import macroscopic
+    _, ux, uy = macroscopic(lat.populations(torch.float64))
+    return ux, uy
+
+
 def _rel_l2_u(lat, ux_ref, uy_ref):
-    _, ux, uy = lat.macroscopic()
-    ux, uy = ux.double(), uy.double()
+    ux, uy = _u64(lat)
     num = torch.sqrt(((ux - ux_ref) ** 2 + (uy - uy_ref) ** 2).sum())
     den = torch.sqrt((ux_ref ** 2 + uy_ref ** 2).sum())
     return float(num / den)
@@ -141,7 +149,7 @@ def precision(n=1024, omegas=(1.0, 1.7, 1.95), steps=50000, u0=0.1,
                 lat.step(mark - done)
             done = mark
             ref = lats["f64"]
-            _, ux_ref, uy_ref = ref.macroscopic()
+            ux_ref, uy_ref = _u64(ref)
             finite = bool(torch.isfinite(ux_ref).all())
             m_ref = float(ref.mass_momentum()[0]) - m0["f64"]
             for st in storages:
@@ -150,7 +158,7 @@ def precision(n=1024, omegas=(1.0, 1.7, 1.95), steps=50000, u0=0.1,
                 ok = finite and bool(torch.isfinite(ux).all())
                 out.append({"n": n, "omega": omega, "steps": mark, "storage": st, "fp64_finite": finite,
                             "mass_drift_fp64": m_ref, "mass_drift": float(lat.mass_momentum()[0]) - m0[st],
-                            "rel_l2_u": _rel_l2_u(lat, ux_ref.double(), uy_ref.double()) if ok else None})
+                            "rel_l2_u": _rel_l2_u(lat, ux_ref, uy_ref) if ok else None})
         del lats
     return out
 
@@ -163,6 +171,8 @@ def main(argv=None):
     p.add_argument("--omegas", type=str, default="1.0,1.7,1.95")
     p.add_argument("--storages", type=str, default="f32,f16dev,bf16dev,f16dev+sr,bf16dev+sr",
                    help="precision study: comma-separated storages compared with FP64")
+    p.add_argument("--checkpoints", type=str, default="1000,5000,10000,20000,50000",
+                   help="precision study: comma-separated step counts at which the error is recorded")
     a = p.parse_args(argv)
     if a.study == "density":
         _, _, fit = density_wave(steps=a.steps or 10000)
@@ -171,7 +181,8 @@ def main(argv=None):
         print(json.dumps({"study": "shear_wave", **shear_wave(steps=a.steps or 2000)}))
     else:
         for row in precision(n=a.n, omegas=[float(x) for x in a.omegas.split(",")], steps=a.steps or 50000,
-                             storages=tuple(a.storages.split(","))):
+                             storages=tuple(a.storages.split(",")),
+                             checkpoints=tuple(int(x) for x in a.checkpoints.split(","))):
             print(json.dumps({"study": "precision", **row}))
 
 

@@ -28,6 +28,7 @@ import time
 import numpy as np
 import torch
 
+from . import _lib
 from . import batch as B
 from .fno import FNO2d, RE_RANGE, U_RANGE
 
@@ -97,6 +98,9 @@ def train(net, data, idx, epochs=100, batch=16, lr=1e-3, lr_min=1e-5, log=None, 
             cur = lr_min + 0.5 * (lr - lr_min) * (1 + math.cos(math.pi * k / total))
             net.adam(cur)
             k += 1
+        # once per epoch: a GEMM whose bounded wait gave up left weights or
+        # gradients incomplete; stop instead of training on them
+        _lib.gemm_status()
         if log is not None and (ep % 10 == 0 or ep == epochs - 1):
             vl = evaluate(net, data, val_idx) if val_idx is not None and len(val_idx) else float("nan")
             tl = float(acc) / steps_per_epoch
@@ -116,6 +120,7 @@ def evaluate(net, data, idx, batch=16):
         num = ((ux - f[:, 1]) ** 2 + (uy - f[:, 2]) ** 2).sum(dim=(1, 2)).sqrt()
         den = (f[:, 1] ** 2 + f[:, 2] ** 2).sum(dim=(1, 2)).sqrt()
         errs.append((num / den).cpu())
+    _lib.gemm_status()
     return float(torch.cat(errs).mean())
 
 

@@ -103,17 +103,29 @@ def collide(f, omega):
     return rho, ux, uy
 
 
+def eigen_sum9(v):
+    """Sum of the nine rows of ``v`` in the order Eigen 3.4.0 (the reference's
+    pinned, un-vendored dependency, setup.py:32) reduces a fixed-size
+    9-vector: the unrolled reduction splits a run of n coefficients into its
+    first n//2 and the rest and adds the two sums, i.e.
+    ``((v0+v1)+(v2+v3)) + ((v4+v5)+(v6+(v7+v8)))``."""
+    def part(a, n):
+        if n == 1:
+            return v[a]
+        h = n // 2
+        return part(a, h) + part(a + h, n - h)
+    return part(0, 9)
+
+
 def collide_cxx(f2d, omega):
     """BGK collision in place on a ``(9, N)`` view, C++ order (c/d2q9.h:121-131).
 
-    The density is accumulated channel by channel (0..8) as the native loop
-    does; returns ``None`` like the native binding.
+    The density is ``f_i.sum()`` of a fixed-size Eigen vector (``eigen_sum9``);
+    returns ``None`` like the native binding.
     """
     dt = f2d.dtype
     omega = dt.type(omega)
-    rho = f2d[0].copy()
-    for i in range(1, 9):
-        rho = rho + f2d[i]
+    rho = eigen_sum9(f2d)
     ux = (f2d[1] - f2d[3] + f2d[5] - f2d[6] - f2d[7] + f2d[8]) / rho
     uy = (f2d[2] - f2d[4] + f2d[5] + f2d[6] - f2d[7] - f2d[8]) / rho
     feq = equilibrium_cxx(rho, ux, uy)

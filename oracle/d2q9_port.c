@@ -7,8 +7,12 @@
  * Arithmetic follows the reference's native kernel operation by operation:
  *   equilibrium  -> c/d2q9.h:59-81   (ux*=3, uy*=3, uu=(ux^2+uy^2)/6,
  *                                     f_i = w_i rho (1 + cu + cu^2/2 - uu))
- *   collide      -> c/d2q9.h:121-131 (rho summed channel 0..8, then ux, uy,
+ *   collide      -> c/d2q9.h:121-131 (rho = f_i.sum() in the order of
+ *                                     Eigen 3.4's unrolled fixed-size
+ *                                     reduction, then ux, uy,
  *                                     f += omega (feq - f))
+ * Built with -ffp-contract=off: every operation rounds on its own, as in the
+ * reference's x86-64 build (no FMA), on x86-64 and aarch64 hosts alike.
  * Streaming follows PyLB/Streaming.py:33-46 (periodic) and
  * simulators/parallel_lid_drive_cavity/cavity_opt1.py:177-245 (half-way
  * bounce-back on four walls, Ladd moving lid, the reference's corner order
@@ -65,8 +69,8 @@ static inline void eq1_##SUF(T rho, T ux, T uy, T *o) {                         
     o[8] = w5 * (1 + cu8 + cu8 * cu8 / 2 - uu);                                      \
 }                                                                                    \
 static inline void collide1_##SUF(T *v, T omega) {                                  \
-    T rho = v[0];                                                                    \
-    for (int i = 1; i < 9; ++i) rho += v[i];                                         \
+    /* f_i.sum() of a fixed-size Eigen 3.4 vector: halving split */                  \
+    T rho = ((v[0] + v[1]) + (v[2] + v[3])) + ((v[4] + v[5]) + (v[6] + (v[7] + v[8]))); \
     T ux = (v[1] - v[3] + v[5] - v[6] - v[7] + v[8]) / rho;                          \
     T uy = (v[2] - v[4] + v[5] + v[6] - v[7] - v[8]) / rho;                          \
     T e[9];                                                                          \

@@ -192,4 +192,7 @@ def main(ref):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else os.environ.get("LB_REFERENCE", "/root/reference"))
+    ref = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("LB_REFERENCE")
+    if not ref:
+        sys.exit("usage: %s REFERENCE_CHECKOUT (or set LB_REFERENCE)" % sys.argv[0])
+    main(ref)

@@ -124,3 +124,23 @@ def test_save_npy_round_trip(tmp_path):
 
     with pytest.raises(NotImplementedError):
         IO.save_mpiio(TwoRanks(), fn, a)
+
+
+def test_reference_package_name_imports():
+    """``importlib.import_module("PyLB")`` succeeds (tests/01-ImportTest.py:36-44)
+    and the reference's imports (cavity_opt2.py:42-43) resolve to the GPU
+    operators."""
+    import importlib
+    mod = importlib.import_module("PyLB")
+    import PyLB as D2Q9
+    from PyLB.IO import save_mpiio
+    from PyLB.Streaming import c_ic, stream, stream_and_bounce_back
+    assert mod is D2Q9
+    assert D2Q9.collide is PyLB.collide and D2Q9.equilibrium is PyLB.equilibrium and D2Q9.stream is stream
+    assert D2Q9.Collision.collide is PyLB.Collision.collide
+    assert stream_and_bounce_back is PyLB.Streaming.stream_and_bounce_back
+    assert save_mpiio is IO.save_mpiio
+    assert c_ic.shape == (9, 2)
+    # host arrays are rejected like the binding rejects a wrong type: no CPU path
+    with pytest.raises(TypeError):
+        D2Q9.collide(np.zeros((9, 4)), 1.0)

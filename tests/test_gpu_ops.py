@@ -37,6 +37,10 @@ def test_equilibrium_golden(cuda, golden, shape):
     f32 = torch.zeros((9, rho.size), dtype=torch.float32, device=cuda)
     PyLB.Collision.equilibrium(*(T(a.ravel().astype(np.float32), cuda) for a in (rho, ux, uy)), f32)
     assert np.abs(f32.cpu().numpy().reshape(ref.shape) - ref).max() < 2e-6
+    # the native kernel's operation order: bit for bit in both precisions
+    for dt, g in ((np.float64, f), (np.float32, f32)):
+        args = [a.ravel().astype(dt) for a in (rho, ux, uy)]
+        np.testing.assert_array_equal(g.cpu().numpy(), oracle.equilibrium_cxx(*args))
 
 
 def test_equilibrium_scalar_overload(cuda):
@@ -45,7 +49,9 @@ def test_equilibrium_scalar_overload(cuda):
     ref = oracle.equilibrium(np.array(1.0), np.array(0.05), np.array(-0.02))
     assert np.abs(e.cpu().numpy() - ref).max() < 1e-7
     e64 = PyLB.equilibrium(torch.tensor(1.0, dtype=torch.float64, device=cuda), 0.05, -0.02)
-    assert e64.dtype == torch.float64 and np.abs(e64.cpu().numpy() - ref).max() < 1e-16
+    assert e64.dtype == torch.float64 and np.abs(e64.cpu().numpy() - ref).max() < 1e-15
+    np.testing.assert_array_equal(e64.cpu().numpy(), oracle.equilibrium_cxx(np.array(1.0), np.array(0.05),
+                                                                            np.array(-0.02)))
 
 
 @pytest.mark.parametrize("omega", [0.5, 1.7])
@@ -66,19 +72,42 @@ def test_collide_ragged_and_strided(cuda, n, dtype):
         oracle.collide_cxx(ref, 1.3)
     g = T(f, cuda)
     PyLB.collide(g, 1.3)
-    # float32: the rest population is written as rho - sum of the others,
-    # a few ulps of 1 away from the native kernel's value
-    tol = 1e-15 if dtype == np.float64 else 6e-7
+    # the native kernel's operations in its order, each rounded on its own:
+    # bit for bit in float32 and float64
     if n:
-        assert np.abs(g.cpu().numpy() - ref).max() < tol
+        np.testing.assert_array_equal(g.cpu().numpy(), ref)
     # channel rows spaced wider than N (a view into a bigger buffer), odd stride
     big = torch.zeros((9, n + 3), dtype=g.dtype, device=cuda)
     big[:, :n] = T(f, cuda)
     view = big[:, :n]
     PyLB.collide(view, 1.3)
     if n:
-        assert np.abs(view.cpu().numpy() - ref).max() < tol
+        np.testing.assert_array_equal(view.cpu().numpy(), ref)
     assert (big[:, n:] == 0).all()
+
+
+@pytest.mark.parametrize("n", [1, 5, 4099])
+@pytest.mark.parametrize("dtype", [np.float64, np.float32])
+def test_collide_keep_mass_option(cuda, n, dtype):
+    """keep_mass=True: the fused solver's collision.  float32 writes the rest
+    population as f_0 + sum_{i>0}(f_i - f_i'), a few ulps of 1 away from the
+    native value, and keeps each node's mass closer than the native order."""
+    rng = np.random.default_rng(n + 7)
+    f = (0.02 + 0.2 * rng.random((9, n))).astype(dtype)
+    ref = f.copy()
+    oracle.collide_cxx(ref, 1.3)
+    g = T(f, cuda)
+    PyLB.collide(g, 1.3, keep_mass=True)
+    out = g.cpu().numpy()
+    tol = 1e-15 if dtype == np.float64 else 6e-7
+    assert np.abs(out - ref).max() < tol
+    if dtype == np.float32:
+        m0 = f.astype(np.float64).sum(axis=0)
+        assert np.abs(out.astype(np.float64).sum(axis=0) - m0).max() <= np.abs(
+            ref.astype(np.float64).sum(axis=0) - m0).max() + 1e-7
+    with pytest.raises(ValueError):
+        _lib.call("lbgb_collide_ex", g.data_ptr(), n, n, _lib.F32 if dtype == np.float32 else _lib.F64, 1.3, 6,
+                  torch.cuda.current_stream().cuda_stream)
 
 
 def test_collide_rejects_bad_dtype_and_layout(cuda):

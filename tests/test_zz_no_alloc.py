@@ -19,7 +19,9 @@ from latticeboltzmann_gb300 import _lib
 
 pytestmark = pytest.mark.gpu
 
-CODES = {torch.float32: _lib.F32, torch.float64: _lib.F64}
+STORAGES = {"f32": (_lib.F32, torch.float32), "f64": (_lib.F64, torch.float64),
+            "f16dev": (_lib.F16DEV, torch.int16), "bf16dev": (_lib.BF16DEV, torch.int16),
+            "f32dev": (_lib.F32DEV, torch.float32)}
 
 
 def with_workspace(lib, f, n, cs, code, stream):
@@ -31,29 +33,70 @@ def with_workspace(lib, f, n, cs, code, stream):
     return out
 
 
-def test_no_alloc_reduction_matches_workspace_reduction(cuda):
+def stored(lib, pops, storage, stream):
+    """The populations pops (float64, (9, nx, ny)) in the given storage."""
+    code, dtype = STORAGES[storage]
+    n = pops.shape[1] * pops.shape[2]
+    f = torch.empty(pops.shape, dtype=dtype, device=pops.device)
+    rc = lib.lbgb_convert(pops.data_ptr(), _lib.F64, n, f.data_ptr(), code, n, n, stream)
+    assert rc == _lib.OK, _lib.last_error()
+    return f
+
+
+def decoded_sums(lib, f, storage, stream):
+    """(mass, x momentum, y momentum) of the stored values, decoded to float64
+    and summed on the host."""
+    code, _ = STORAGES[storage]
+    n = f.shape[1] * f.shape[2]
+    h = torch.empty(f.shape, dtype=torch.float64, device=f.device)
+    rc = lib.lbgb_convert(f.data_ptr(), code, n, h.data_ptr(), _lib.F64, n, n, stream)
+    assert rc == _lib.OK, _lib.last_error()
+    torch.cuda.synchronize()
+    h = h.cpu().numpy()
+    cx = np.array([0, 1, 0, -1, 0, 1, -1, -1, 1])[:, None, None]
+    cy = np.array([0, 0, 1, 0, -1, 1, 1, -1, -1])[:, None, None]
+    return np.array([h.sum(), (cx * h).sum(), (cy * h).sum()])
+
+
+@pytest.mark.parametrize("storage", list(STORAGES))
+def test_no_alloc_reduction_matches_workspace_reduction(cuda, storage):
+    """Every storage code, on two calls in a row with different lattices:
+    the second must not see the first call's partial sums left in the shared
+    array.  The second lattice has more than 256 partials (9 x 1024 x 1100:
+    275 blocks of 4096 cells), which the final pass sums in a strided loop."""
     lib = _lib.load()
+    code, _ = STORAGES[storage]
     stream = torch.cuda.current_stream(cuda).cuda_stream
     rng = np.random.default_rng(2024)
-    # two calls in a row on different lattices: the second must not see the
-    # first call's partial sums left in the shared array
-    cases = [((9, 300, 257), torch.float64), ((9, 64, 4096), torch.float32)]
-    for shape, dtype in cases:
-        f = torch.from_numpy(0.02 + 0.2 * rng.random(shape)).to(dtype=dtype, device=cuda)
+    for shape in [(9, 300, 257), (9, 1024, 1100)]:
+        pops = torch.from_numpy(0.02 + 0.2 * rng.random(shape)).to(cuda)
+        f = stored(lib, pops, storage, stream)
         n = shape[1] * shape[2]
-        ref = with_workspace(lib, f, n, n, CODES[dtype], stream)
+        ref = with_workspace(lib, f, n, n, code, stream)
         out = torch.full((3,), float("nan"), dtype=torch.float64, device=cuda)
-        rc = lib.lbgb_mass_momentum_noalloc(f.data_ptr(), n, n, CODES[dtype], out.data_ptr(), stream)
+        rc = lib.lbgb_mass_momentum_noalloc(f.data_ptr(), n, n, code, out.data_ptr(), stream)
         assert rc == _lib.OK, _lib.last_error()
         torch.cuda.synchronize()
         a, b = out.cpu().numpy(), ref.cpu().numpy()
-        # same tolerance as the workspace reduction's own test against the oracle
-        assert np.abs(a - b).max() < 1e-9, (a, b)
-        # and both agree with a float64 sum on the host
-        h = f.double().cpu().numpy()
-        cx = np.array([0, 1, 0, -1, 0, 1, -1, -1, 1])[:, None, None]
-        cy = np.array([0, 0, 1, 0, -1, 1, 1, -1, -1])[:, None, None]
-        assert np.abs(a - [h.sum(), (cx * h).sum(), (cy * h).sum()]).max() < 1e-9
+        # FP64 sums of ~1e5-1e6 values in two fixed orders
+        tol = 1e-12 * np.abs(b).max() + 1e-9
+        assert np.abs(a - b).max() < tol, (storage, a, b)
+        # and both agree with a float64 sum of the decoded values on the host
+        assert np.abs(a - decoded_sums(lib, f, storage, stream)).max() < tol, storage
+
+
+def test_no_alloc_reduction_empty_lattice(cuda):
+    """n = 0 after a call that filled the array: the sums are exactly zero."""
+    lib = _lib.load()
+    stream = torch.cuda.current_stream(cuda).cuda_stream
+    f = torch.full((9, 64, 64), 0.25, dtype=torch.float64, device=cuda)
+    out = torch.empty(3, dtype=torch.float64, device=cuda)
+    assert lib.lbgb_mass_momentum_noalloc(f.data_ptr(), 4096, 4096, _lib.F64, out.data_ptr(), stream) == _lib.OK
+    out.fill_(float("nan"))
+    rc = lib.lbgb_mass_momentum_noalloc(f.data_ptr(), 0, 0, _lib.F64, out.data_ptr(), stream)
+    assert rc == _lib.OK, _lib.last_error()
+    torch.cuda.synchronize()
+    assert out.cpu().numpy().tolist() == [0.0, 0.0, 0.0]
 
 
 def test_no_alloc_reduction_rejects_oversized_lattices(cuda):
