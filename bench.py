@@ -19,6 +19,13 @@ Lines printed (rank 0, one JSON line):
   cpu_baseline  the oracle's C port of the reference step on the host cores;
              cpu_baseline.numpy_opt1: the reference's numpy step, one process
              per host core
+  fp16_store FP32 against FP16/BF16 deviation storage (round to nearest and
+             stochastic) on the 16384^2 cavity: CUDA-event MLUPS, HBM
+             fraction and clock record per storage, ratio to FP32, and each
+             mode's error against an FP64 run (1024^2, 1000 steps)
+  operator_path  MLUPS of the reference's loop body through the drop-in
+             operators (stream_and_bounce_back with its scratch copy, then
+             collide), next to the fused step
 
 ``--impl reference`` times the CPU implementation of the reference step (the
 C port of the oracle; the reference's own C++ extension needs Eigen, which is
@@ -67,6 +74,10 @@ def parse(argv=None):
     p.add_argument("--workload", choices=["cavity", "batched-shear"], default="cavity",
                    help="cavity: one lattice (default); batched-shear: 512 uneven periodic shear-wave lattices "
                         "advanced by one launch per step (autotuned)")
+    p.add_argument("--no-extras", action="store_true",
+                   help="skip the 16-bit storage comparison, the operator-path timing and the warm-start study")
+    p.add_argument("--store-n", type=int, default=16384, help="lattice side of the 16-bit storage comparison")
+    p.add_argument("--store-steps", type=int, default=60, help="timed steps per storage in that comparison")
     return p.parse_args(argv)
 
 
@@ -397,8 +408,9 @@ def run_ours(args):
 
         def e2e_step():
             if host_path:
-                # upload, update and download pipelined by row blocks (public API)
-                lat.step_host(host)
+                # upload, update and download pipelined by row blocks (public
+                # API); the device status is checked once after the loop
+                lat.step_host(host, check=False)
             else:
                 lat.load(host)
                 lat.step(1)
@@ -413,6 +425,7 @@ def run_ours(args):
             e2e_step()
         torch.cuda.synchronize(dev)
         el = time.perf_counter() - t0
+        _lib.device_status()
         d.barrier()
         e_mlups, _ = aggregate_mlups(lat.cells, args.e2e_steps, el, d, dev)
         nbytes = host.numel() * host.element_size()
@@ -441,6 +454,10 @@ def run_ours(args):
                 "algorithmic_bytes": bpc * lat.cells, "kernel": "k_step (fused pull stream + bounce-back/lid + BGK)",
                 "peak_source": peak_src,
                 "traffic_source": None if prof is None else prof.get("source")}
+    extras = {}
+    if not args.no_extras and args.boundary == "cavity":
+        extras["operator_path"] = operator_path(args, dev)
+        extras["fp16_store"] = storage_comparison(args, dev, d.local_rank)
     cpu = None
     if not args.no_cpu_baseline:
         c_mlups, cores, sample = cpu_port_sample(args.nx, args.ny, args.omega, args.u0, args.storage, args.boundary,
@@ -461,9 +478,112 @@ def run_ours(args):
         "e2e": e2e, "gpu_launches": args.steps, "roofline": roofline, "cpu_baseline": cpu, "clocks": clk,
         "hbm_gbs": round(achieved, 1),
     }
+    line.update(extras)
     print(json.dumps(line), flush=True)
     d.close()
     return 0
+
+
+def time_storage(n, storage, dev, steps, warmup, gpu_index, omega=1.7, u0=0.1, rounding="nearest"):
+    """CUDA-event MLUPS of the fused cavity step at n x n in one storage (one
+    launch per step), with the clock record of its own timed region."""
+    import torch
+    import latticeboltzmann_gb300 as PyLB
+    from latticeboltzmann_gb300 import _lib
+    lat = PyLB.Lattice(n, n, omega, boundary="cavity", u0=u0, storage=storage, device=dev, rounding=rounding)
+    stream = torch.cuda.current_stream(dev)
+    lat.step(warmup)
+    torch.cuda.synchronize(dev)
+    clocks = ClockSampler(gpu_index)
+    clocks.start()
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(steps + 1)]
+    ev[0].record(stream)
+    for i in range(steps):
+        lat.step(1)
+        ev[i + 1].record(stream)
+    torch.cuda.synchronize(dev)
+    clk = clocks.stop()
+    _lib.device_status()
+    total_s = ev[0].elapsed_time(ev[-1]) / 1e3
+    bpc = lat.bytes_per_cell_update
+    achieved = bpc * lat.cells * steps / total_s / 1e9
+    peak, _ = hbm_peak()
+    out = {"mlups": round(lat.cells * steps / total_s / 1e6, 1), "ms_per_step": round(total_s / steps * 1e3, 4),
+           "bytes_per_cell": bpc, "achieved_gbs": round(achieved, 1), "frac": round(achieved / peak, 4),
+           "rounding": rounding if storage in ("f16dev", "bf16dev") else None, "steps": steps, "clocks": clk}
+    del lat
+    torch.cuda.empty_cache()
+    return out
+
+
+def storage_comparison(args, dev, gpu_index):
+    """FP32 against 16-bit deviation storage on the n x n cavity (the
+    reference's cavity_opt1.py:177-245 lid, omega 1.7, u0 0.1), plus the
+    error of each 16-bit mode against an FP64 run of the same kernel at
+    1024^2 after 1000 steps (relative L2 of u, total-mass drift)."""
+    from latticeboltzmann_gb300 import studies
+    n = args.store_n
+    rows = {}
+    for storage, rounding in (("f32", "nearest"), ("f16dev", "nearest"), ("bf16dev", "nearest"),
+                              ("f16dev", "stochastic"), ("bf16dev", "stochastic")):
+        key = storage + ("+sr" if rounding == "stochastic" else "")
+        rows[key] = time_storage(n, storage, dev, args.store_steps, max(3, args.warmup), gpu_index,
+                                 rounding=rounding)
+    f32 = rows["f32"]["mlups"]
+    err = {}
+    for r in studies.precision(n=1024, omegas=(1.7,), steps=1000, storages=("f32", "f32dev", "f16dev", "bf16dev",
+                                                                            "f16dev+sr", "bf16dev+sr"),
+                               device=dev, checkpoints=(1000,)):
+        err[r["storage"]] = {"rel_l2_u": r["rel_l2_u"], "mass_drift": round(r["mass_drift"], 6),
+                             "mass_drift_fp64": round(r["mass_drift_fp64"], 6)}
+    return {"workload": "cavity %dx%d, omega 1.7, u_lid 0.1, from rest; 16-bit storage holds f_i - w_i, "
+                        "FP32 arithmetic" % (n, n),
+            "rows": rows, "ratio_vs_f32": {k: round(v["mlups"] / f32, 3) for k, v in rows.items() if k != "f32"},
+            "error_vs_fp64": {"case": "cavity 1024^2, omega 1.7, u_lid 0.1, 1000 steps, against the FP64 "
+                                      "kernel (itself within 1e-12 of the FP64 oracle)", "by_storage": err}}
+
+
+def operator_path(args, dev):
+    """MLUPS of the reference's loop body through the drop-in operators
+    (cavity_opt2.py:276-277): Streaming.stream_and_bounce_back (out of place
+    into scratch, copied back) then Collision.collide, on the benchmark
+    lattice in FP32.  216 bytes per cell per step (stream 72, copy 72,
+    collide 72) against the fused step's 72."""
+    import torch
+    import latticeboltzmann_gb300 as PyLB
+    from latticeboltzmann_gb300 import _lib
+    nx, ny = args.nx, args.ny
+    f = torch.empty((9, nx, ny), dtype=torch.float32, device=dev)
+    one = torch.ones(nx * ny, dtype=torch.float32, device=dev)
+    zero = torch.zeros(nx * ny, dtype=torch.float32, device=dev)
+    PyLB.equilibrium(one, zero, zero, f.reshape(9, -1))
+    del one, zero
+    stream = torch.cuda.current_stream(dev)
+
+    def step():
+        PyLB.Streaming.stream_and_bounce_back(f, args.u0)
+        PyLB.collide(f.reshape(9, -1), args.omega)
+
+    for _ in range(max(3, args.warmup)):
+        step()
+    steps = max(5, min(args.steps, 20))
+    torch.cuda.synchronize(dev)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(steps):
+        step()
+    e1.record(stream)
+    torch.cuda.synchronize(dev)
+    _lib.device_status()
+    secs = e0.elapsed_time(e1) / 1e3
+    peak, _ = hbm_peak()
+    del f
+    torch.cuda.empty_cache()
+    return {"mlups": round(nx * ny * steps / secs / 1e6, 1), "ms_per_step": round(secs / steps * 1e3, 4),
+            "bytes_per_cell": 216, "frac": round(216 * nx * ny * steps / secs / 1e9 / peak, 4), "steps": steps,
+            "launches_per_step": 3,
+            "path": "PyLB.Streaming.stream_and_bounce_back (kernel into scratch + copy back) + PyLB.collide, "
+                    "float32 (%dx%d)" % (nx, ny)}
 
 
 def host_link_seconds(host, dev, reps=3):

@@ -1,15 +1,23 @@
 """Precision of the fused solver against float64 runs of the oracle.
 
-Stated tolerances (lid-driven cavity 64 x 64, omega = 1.7, u0 = 0.1, from rest,
-1000 steps; relative L2 error of the velocity field against the float64
-oracle):
+Stated tolerances (lid-driven cavity, omega = 1.7, u0 = 0.1, from rest;
+relative L2 error of the velocity field against the float64 oracle, the
+tolerance of the benchmark spec being 1e-6 for FP32):
 
-* f64 storage:     populations within 1e-12 absolute of the float64 oracle.
-* f32 storage:     rel-L2(u) <= 1e-5, and no worse than 1.5x the error of the
-                   reference's own float32 arithmetic (cavity_opt1.py run with
-                   dtype=float32, reproduced bit-exactly by oracle/d2q9.py).
-                   The floor is FP32 rounding inside the collision; the
-                   reference's float32 path measures about 6e-6 here.
+* f64 storage:     populations within 1e-12 absolute of the float64 oracle
+                   (64^2, 1000 steps).
+* f32dev storage:  FP32 deviations h = f - w, FP32 arithmetic in the
+                   momentum-exact pair form: <= 2.5e-7 after every checkpoint
+                   up to 20,000 steps at 256^2 (measured 1e-7; at 1024^2 the
+                   error stays below 1e-6 up to 7,500 steps and at 8192^2 up
+                   to 5,000, where the unsteady flow starts to amplify
+                   differences), and <= 2e-7 after 1000 steps at 64^2.
+* f32 storage:     <= 1.2e-6 after 1000 steps at 64^2 and <= 1.8e-6 at 256^2
+                   up to 20,000 steps: the FP32 rounding of the populations
+                   f themselves (~3e-8 at 0.44) is the floor (FP64 arithmetic
+                   with FP32 populations gives 9e-7 at 64^2); at most a
+                   quarter of the error of the reference's own float32
+                   arithmetic (cavity_opt1.py with dtype=float32, 6.2e-6).
 * f16dev storage:  rel-L2(u) <= 2e-3    (half deviations f_i - w_i)
 * bf16dev storage: rel-L2(u) <= 1.5e-2  (bfloat16 deviations)
 """
@@ -63,23 +71,43 @@ def test_f64_matches_oracle(cuda, ref64):
 
 
 def test_f32_error_bound(cuda, ref64, ref32_error):
+    """FP32 populations: the floor is their own rounding (measured 9.5e-7)."""
     lat = run("f32", cuda)
     err = rel_l2_u(lat.populations().cpu().numpy(), ref64)
-    assert err <= 1e-5, err
-    assert err <= 1.5 * ref32_error, (err, ref32_error)
+    assert err <= 1.2e-6, err
+    assert err <= 0.25 * ref32_error, (err, ref32_error)
 
 
 def test_f32dev_error_bound(cuda, ref64):
-    """FP32 deviation storage and deviation-form collision: the same 72 bytes
-    per cell as FP32, every rounding on numbers ~1e-2.  After 1000 steps of
-    this transient flow the velocity still carries the FP32 relative rounding
-    of u itself (measured 3.9e-6 against FP32's 5.5e-6), so the bound is
-    "no worse than FP32, and below 5e-6"; its gain shows where the absolute
-    floor matters (steady states, a 10x lower velocity-change floor)."""
+    """FP32 deviation storage, pair-form collision (momentum changes only by
+    the final roundings): measured 9.1e-8, the rounding of the stored
+    deviations (an FP64-arithmetic emulation gives 7.7e-8); the directly
+    evaluated equilibrium it replaced gave 3.9e-6."""
     e32 = rel_l2_u(run("f32", cuda).populations().cpu().numpy(), ref64)
     edev = rel_l2_u(run("f32dev", cuda).populations(torch.float64).cpu().numpy(), ref64)
-    assert edev <= 5e-6, edev
-    assert edev <= e32, (edev, e32)
+    assert edev <= 2e-7, edev
+    assert edev <= 0.25 * e32, (edev, e32)
+
+
+def test_fp32_meets_1e6_velocity_tolerance_256(cuda):
+    """The stated step count: a 256^2 cavity (omega 1.7, u0 0.1, Re ~ 870)
+    stays within 1e-6 relative L2 of the FP64 oracle's velocity up to 20,000
+    steps in FP32-deviation storage (bound 2.5e-7, measured <= 1.07e-7 at
+    every checkpoint); FP32 population storage stays within 1.8e-6 (its own
+    rounding floor, measured <= 1.66e-6)."""
+    n = 256
+    f64 = oracle.equilibrium(np.ones((n, n)), np.zeros((n, n)), np.zeros((n, n)))
+    lats = {s: run(s, cuda, steps=0, nx=n, ny=n) for s in ("f32dev", "f32")}
+    done = 0
+    for mark in (1000, 5000, 20000):
+        port.cavity_run(f64, OMEGA, U0, mark - done, nthreads=0)
+        errs = {}
+        for s, lat in lats.items():
+            lat.step(mark - done)
+            errs[s] = rel_l2_u(lat.populations(torch.float64).cpu().numpy(), f64)
+        done = mark
+        assert errs["f32dev"] <= 2.5e-7, (mark, errs)
+        assert errs["f32"] <= 1.8e-6, (mark, errs)
 
 
 @pytest.mark.parametrize("storage,tol,mtol", [("f16dev", 2e-3, 0.05), ("bf16dev", 1.5e-2, 0.05)])
