@@ -26,6 +26,10 @@ Lines printed (rank 0, one JSON line):
   operator_path  MLUPS of the reference's loop body through the drop-in
              operators (stream_and_bounce_back with its scratch copy, then
              collide), next to the fused step
+  warm_start cavity time to steady state (max |du| < 1e-7 per 1000 steps),
+             cold from rest against warm from the committed surrogate's
+             prediction, for fixed held-out cases at 256^2 and 1024^2: steps,
+             wall seconds and their ratios
 
 ``--impl reference`` times the CPU implementation of the reference step (the
 C port of the oracle; the reference's own C++ extension needs Eigen, which is
@@ -78,6 +82,8 @@ def parse(argv=None):
                    help="skip the 16-bit storage comparison, the operator-path timing and the warm-start study")
     p.add_argument("--store-n", type=int, default=16384, help="lattice side of the 16-bit storage comparison")
     p.add_argument("--store-steps", type=int, default=60, help="timed steps per storage in that comparison")
+    p.add_argument("--warm-cases", type=int, default=8, help="held-out cavities timed cold and warm at 256^2")
+    p.add_argument("--warm-cases-large", type=int, default=2, help="held-out cavities timed at 1024^2")
     return p.parse_args(argv)
 
 
@@ -458,6 +464,7 @@ def run_ours(args):
     if not args.no_extras and args.boundary == "cavity":
         extras["operator_path"] = operator_path(args, dev)
         extras["fp16_store"] = storage_comparison(args, dev, d.local_rank)
+        extras["warm_start"] = warm_start(args, dev)
     cpu = None
     if not args.no_cpu_baseline:
         c_mlups, cores, sample = cpu_port_sample(args.nx, args.ny, args.omega, args.u0, args.storage, args.boundary,
@@ -541,6 +548,50 @@ def storage_comparison(args, dev, gpu_index):
             "rows": rows, "ratio_vs_f32": {k: round(v["mlups"] / f32, 3) for k, v in rows.items() if k != "f32"},
             "error_vs_fp64": {"case": "cavity 1024^2, omega 1.7, u_lid 0.1, 1000 steps, against the FP64 "
                                       "kernel (itself within 1e-12 of the FP64 oracle)", "by_storage": err}}
+
+
+WEIGHTS = os.path.join(ROOT, "latticeboltzmann_gb300", "weights", "fno_cavity256_bf16.npz")
+
+
+def warm_start(args, dev):
+    """Time to steady state of the lid-driven cavity started from rest (cold)
+    and from the surrogate's prediction in its Chapman-Enskog state (warm; the
+    wall time includes the network's inference and the start kernel), for a
+    fixed set of the trained network's held-out (Re, u_lid) pairs: evenly
+    spaced in Re at 256^2, and the lowest-Re ones evaluated at 1024^2.
+    Steady: max |u(t+1000) - u(t)| < 1e-7 (the reference's cold start is
+    cavity_opt1.py:333-335).  Each cavity runs alone, in FP32-deviation
+    storage (FP64 only if its change stalls above the tolerance)."""
+    import numpy as np
+    import torch
+    from latticeboltzmann_gb300 import surrogate as S
+    from latticeboltzmann_gb300.fno import FNO2d
+    if not os.path.exists(WEIGHTS):
+        return {"unavailable": "no trained weights at %s" % os.path.relpath(WEIGHTS, ROOT)}
+    net = FNO2d.load(WEIGHTS, device=dev)
+    meta = net.meta or {}
+    re, u = np.asarray(meta.get("held_out_re", [])), np.asarray(meta.get("held_out_u", []))
+    if re.size == 0:
+        return {"unavailable": "the weights file names no held-out cases"}
+    order = np.argsort(re)
+    pick = order[np.linspace(0, len(order) - 1, min(args.warm_cases, len(order))).astype(int)]
+    out = {"weights": os.path.relpath(WEIGHTS, ROOT), "tol": 1e-7,
+           "network": {k: meta.get(k) for k in ("epochs", "train_s", "val_rel_l2_u", "val_rel_l2_rho", "samples")}}
+    for n, sel in ((256, pick), (1024, order[:args.warm_cases_large])):
+        if len(sel) == 0:
+            continue
+        rows = S.single_case_timing(net, re[sel], u[sel], n, dev, max_steps=600_000 if n == 256 else 1_500_000)
+        cold = sum(r["cold_s"] for r in rows)
+        warm = sum(r["warm_s"] for r in rows)
+        out["n%d" % n] = {"cases": [{k: (round(v, 4) if isinstance(v, float) else v) for k, v in r.items()}
+                                    for r in rows],
+                          "cold_s": round(cold, 3), "warm_s": round(warm, 3),
+                          "wall_ratio": round(cold / warm, 3) if warm > 0 else None,
+                          "steps_ratio": round(sum(r["cold_steps"] for r in rows) /
+                                               max(1, sum(r["warm_steps"] for r in rows)), 3)}
+    del net
+    torch.cuda.empty_cache()
+    return out
 
 
 def operator_path(args, dev):

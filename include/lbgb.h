@@ -213,7 +213,8 @@ typedef struct {
  * first column, unused}: one warp's work is rows_per_task rows of a
  * 32*vec-cell row segment.  Flat tasks (flat = 1) are {instance, unused,
  * first cell, unused}: lane j takes cells first + 32 r + j of the flattened
- * grid for r < rows_per_task (every lane busy, however short the rows).
+ * grid for r < rows_per_task (every lane busy, however short the rows);
+ * rows_per_task is then 1, 2, 4 or 8 (LBGB_EINVAL otherwise).
  * total_elems bounds every access (entries that do not fit are skipped).
  * threads: multiple of 32 up to 256; blocks: persistent grid size.
  * Replaces the reference's loop over independent runs of
@@ -345,6 +346,11 @@ LBGB_API int lbgb_fno_mix_back(const float *dYm, const float *P, const void *Rr,
                                float *dRr, float *dRi, int C, int O, int B, int q, int mk, void *stream);
 LBGB_API int lbgb_fno_mse(const float *y, const float *t, float *d, double *partials, int nparts,
                           long long n, void *stream);
+/* lbgb_fno_mse with a weight per plane of `plane` consecutive elements (the
+ * (channel, sample) planes of a (C, B, H, W) output): partials of
+ * sum w_p (y - t)^2, d = 2 w_p (y - t) / n. */
+LBGB_API int lbgb_fno_mse_weighted(const float *y, const float *t, const float *w, long long plane, float *d,
+                                   double *partials, int nparts, long long n, void *stream);
 LBGB_API int lbgb_fno_adam(float *w, const float *g, float *m, float *v, void *wb, long long n, float lr,
                            float b1, float b2, float eps, int step, float weight_decay, void *stream);
 LBGB_API int lbgb_fno_sum_splits(const float *parts, float *out, int S, long long n, float beta,

@@ -79,6 +79,7 @@ SIGNATURES = {
     "lbgb_fno_mix": (_I, [_P, _P, _P, _P, _I, _I, _I, _I, _I, _P]),
     "lbgb_fno_mix_back": (_I, [_P, _P, _P, _P, _P, _P, _P, _I, _I, _I, _I, _I, _P]),
     "lbgb_fno_mse": (_I, [_P, _P, _P, _P, _I, ctypes.c_longlong, _P]),
+    "lbgb_fno_mse_weighted": (_I, [_P, _P, _P, ctypes.c_longlong, _P, _P, _I, ctypes.c_longlong, _P]),
     "lbgb_fno_adam": (_I, [_P, _P, _P, _P, _P, ctypes.c_longlong, ctypes.c_float, ctypes.c_float, ctypes.c_float,
                            ctypes.c_float, _I, ctypes.c_float, _P]),
     "lbgb_fno_sum_splits": (_I, [_P, _P, _I, ctypes.c_longlong, ctypes.c_float, _P]),

@@ -99,11 +99,16 @@ __device__ __forceinline__ void pull_cell(const typename C::raw *__restrict__ sr
     }
 }
 
-template <int DT, int BC>
+// R rounds per task: lane j owns cells c0 + 32 r + j, r < R.  The cell
+// indices of all R rounds are computed first and all 9 R loads issued before
+// the first collision, so each thread keeps 9 R loads in flight (a loop that
+// finishes one round before loading the next leaves the kernel waiting on
+// load latency).
+template <int DT, int BC, int R>
 __global__ void __launch_bounds__(256)
 k_batch_step_flat(const typename Codec<DT>::raw *__restrict__ src, typename Codec<DT>::raw *__restrict__ dst,
                   long long total_elems, const BatchInstanceDev *__restrict__ inst, int n_inst,
-                  const int4 *__restrict__ tasks, long long n_tasks, int rounds) {
+                  const int4 *__restrict__ tasks, long long n_tasks) {
     using C = Codec<DT>;
     using real = typename C::real;
     using raw = typename C::raw;
@@ -123,19 +128,31 @@ k_batch_step_flat(const typename Codec<DT>::raw *__restrict__ src, typename Code
         // by 32 cells per round (no 64-bit division per cell)
         long long c = (long long)tk.z + lane;
         int k = (int)(c / in.ny), l = (int)(c - (long long)k * in.ny);
-        for (int r = 0; r < rounds && c < n; ++r) {
-            real v[9];
-            pull_cell<C, BC>(s, in.nx, in.ny, k, l, (real)in.u0, v);
-            raw out[9];
-            collide_encode<DT>(v, (real)in.omega, out);
+        long long cr[R];
+        int kr[R], lr[R];
 #pragma unroll
-            for (int i = 0; i < 9; ++i) d[i * n + c] = out[i];
+        for (int r = 0; r < R; ++r) {
+            cr[r] = c;
+            kr[r] = k;
+            lr[r] = l;
             c += 32;
             l += 32;
             while (l >= in.ny) {
                 l -= in.ny;
                 ++k;
             }
+        }
+        real v[R][9];
+#pragma unroll
+        for (int r = 0; r < R; ++r)
+            if (cr[r] < n) pull_cell<C, BC>(s, in.nx, in.ny, kr[r], lr[r], (real)in.u0, v[r]);
+#pragma unroll
+        for (int r = 0; r < R; ++r) {
+            if (cr[r] >= n) continue;
+            raw out[9];
+            collide_encode<DT>(v[r], (real)in.omega, out);
+#pragma unroll
+            for (int i = 0; i < 9; ++i) d[i * n + cr[r]] = out[i];
         }
     }
 }
@@ -263,9 +280,19 @@ static int launch_batch(const void *src, void *dst, long long total, const void 
     using raw = typename Codec<DT>::raw;
     constexpr int VW = 16 / sizeof(raw);
     if (flat) {
-        k_batch_step_flat<DT, BC><<<blocks, threads, 0, s>>>(
-            static_cast<const raw *>(src), static_cast<raw *>(dst), total,
-            static_cast<const BatchInstanceDev *>(inst), n_inst, static_cast<const int4 *>(tasks), n_tasks, rows);
+        // rounds per task: 1, 2, 4 or 8 (the task queue steps 32 * rows cells)
+        auto go = [&](auto kernel) {
+            kernel<<<blocks, threads, 0, s>>>(static_cast<const raw *>(src), static_cast<raw *>(dst), total,
+                                              static_cast<const BatchInstanceDev *>(inst), n_inst,
+                                              static_cast<const int4 *>(tasks), n_tasks);
+        };
+        switch (rows) {
+        case 1: go(k_batch_step_flat<DT, BC, 1>); break;
+        case 2: go(k_batch_step_flat<DT, BC, 2>); break;
+        case 4: go(k_batch_step_flat<DT, BC, 4>); break;
+        case 8: go(k_batch_step_flat<DT, BC, 8>); break;
+        default: set_error("lbgb_batch_step: flat tasks take 1, 2, 4 or 8 rounds (got %d)", rows); return LBGB_EINVAL;
+        }
         return check_launch("k_batch_step_flat");
     }
     k_batch_step<DT, BC, VW><<<blocks, threads, 0, s>>>(

@@ -259,6 +259,30 @@ __global__ void __launch_bounds__(256) k_mse(const float *__restrict__ y, const 
     if (threadIdx.x == 0) part[blockIdx.x] = sm[0];
 }
 
+// Weighted squared error: element i lies in plane i / plane of (cout, B) planes
+// of H*W elements each, and plane p carries the weight w[p].  Loss partials
+// sum w_p e^2, d = 2 w_p e / n.
+__global__ void __launch_bounds__(256) k_mse_weighted(const float *__restrict__ y, const float *__restrict__ t,
+                                                      const float *__restrict__ w, long long plane,
+                                                      float *__restrict__ d, double *__restrict__ part, long long n) {
+    double acc = 0.0;
+    const float s = 2.f / (float)n;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        const float e = y[i] - t[i];
+        const float wp = w[i / plane];
+        acc += (double)wp * e * e;
+        d[i] = s * wp * e;
+    }
+    __shared__ double sm[256];
+    sm[threadIdx.x] = acc;
+    __syncthreads();
+    for (int k = blockDim.x / 2; k > 0; k >>= 1) {
+        if (threadIdx.x < k) sm[threadIdx.x] += sm[threadIdx.x + k];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) part[blockIdx.x] = sm[0];
+}
+
 // Adam on FP32 master weights, refreshing their BF16 copies
 __global__ void k_adam(float *__restrict__ w, const float *__restrict__ g, float *__restrict__ m, float *__restrict__ v,
                        __nv_bfloat16 *__restrict__ wb, long long n, float lr, float b1, float b2, float eps, float c1,
@@ -407,6 +431,20 @@ extern "C" int lbgb_fno_mse(const float *y, const float *t, float *d, double *pa
     }
     k_mse<<<nparts, 256, 0, (cudaStream_t)stream>>>(y, t, d, partials, n);
     return check_launch("k_mse");
+}
+
+extern "C" int lbgb_fno_mse_weighted(const float *y, const float *t, const float *w, long long plane, float *d,
+                                     double *partials, int nparts, long long n, void *stream) {
+    if (nparts <= 0 || nparts > 8192) {
+        set_error("lbgb_fno_mse_weighted: 1 <= nparts <= 8192");
+        return LBGB_EINVAL;
+    }
+    if (plane <= 0 || n % plane != 0 || !w) {
+        set_error("lbgb_fno_mse_weighted: n must be a positive multiple of the plane size and w given");
+        return LBGB_EINVAL;
+    }
+    k_mse_weighted<<<nparts, 256, 0, (cudaStream_t)stream>>>(y, t, w, plane, d, partials, n);
+    return check_launch("k_mse_weighted");
 }
 
 extern "C" int lbgb_fno_adam(float *w, const float *g, float *m, float *v, void *wb, long long n, float lr, float b1,

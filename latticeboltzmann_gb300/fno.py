@@ -160,18 +160,36 @@ class FNO2d:
                                cin=self.cin, cout=self.cout, pad=self.pad),
                 "params": self.params(), "adam_steps": self.adam_steps}
 
-    def save(self, path):
-        """Weights (FP32), configuration and output scales in one .npz file."""
+    def save(self, path, bf16=False, meta=None):
+        """Weights, configuration and output scales in one .npz file.
+
+        bf16=True stores the matrices as the BF16 values the GEMMs compute
+        with and the biases (used in FP32) as they are: half the size, and
+        inference from the file equals the trained network's; FP32 masters
+        otherwise.  ``meta``: a JSON-serialisable dict stored beside them
+        (e.g. the held-out cases of the training run)."""
         sd = self.state_dict()
+        extra = {"meta": json.dumps(meta)} if meta is not None else {}
+        if bf16:
+            bits = lambda v: torch.from_numpy(v.astype(np.float32)).to(torch.bfloat16).view(torch.int16).numpy()
+            params = {("b_" + k if v.ndim >= 2 else "p_" + k): (bits(v) if v.ndim >= 2 else v.astype(np.float32))
+                      for k, v in sd["params"].items()}
+        else:
+            params = {"p_" + k: v.astype(np.float32) for k, v in sd["params"].items()}
         np.savez(path, config=json.dumps(sd["config"]), out_scale=np.asarray(self.out_scale, dtype=np.float64),
-                 **{"p_" + k: v.astype(np.float32) for k, v in sd["params"].items()})
+                 **extra, **params)
 
     @classmethod
     def load(cls, path, device=None, engine=ENGINE_TENSOR_CORES):
         z = np.load(path)
         net = cls(device=device, engine=engine, **json.loads(str(z["config"])))
         net.out_scale = np.asarray(z["out_scale"], dtype=np.float64)
-        return net.load_params({k[2:]: z[k] for k in z.files if k.startswith("p_")})
+        params = {k[2:]: z[k] for k in z.files if k.startswith("p_")}
+        for k in z.files:
+            if k.startswith("b_"):
+                params[k[2:]] = torch.from_numpy(z[k]).view(torch.bfloat16).float().numpy()
+        net.meta = json.loads(str(z["meta"])) if "meta" in z.files else None
+        return net.load_params(params)
 
     # ------------------------------------------------------------ plumbing
     def _gemm(self, m, n, k, A, a, B, b, C, c, batch=1, beta=0.0, bf16_out=False):
@@ -296,10 +314,12 @@ class FNO2d:
                   self.cout, N, 0, s)
         return out.view(self.cout, B, H, W)
 
-    def loss_and_backward(self, a, target):
+    def loss_and_backward(self, a, target, weight=None):
         """Mean squared error of forward(a) against target (cout, B, H, W) and
         its gradient with respect to every parameter into ``self.grad``.
-        Returns the loss as a device scalar (float64)."""
+        ``weight``: optional contiguous float32 (cout, B) device tensor, a
+        weight per (channel, sample) plane.  Returns the loss as a device
+        scalar (float64)."""
         out = self.forward(a, train=True)
         B, H, W = self._shape
         N = B * H * W
@@ -308,7 +328,15 @@ class FNO2d:
             raise ValueError("target must be a contiguous float32 tensor of shape %s" % (tuple(out.shape),))
         s = self._s()
         nparts = 1024
-        _lib.call("lbgb_fno_mse", _ptr(out), _ptr(target), _ptr(ws["d"]), _ptr(ws["mse"]), nparts, out.numel(), s)
+        if weight is None:
+            _lib.call("lbgb_fno_mse", _ptr(out), _ptr(target), _ptr(ws["d"]), _ptr(ws["mse"]), nparts, out.numel(),
+                      s)
+        else:
+            if (tuple(weight.shape) != (self.cout, B) or weight.dtype != torch.float32 or not weight.is_contiguous()
+                    or weight.device != out.device):
+                raise ValueError("weight must be a contiguous float32 (%d, %d) device tensor" % (self.cout, B))
+            _lib.call("lbgb_fno_mse_weighted", _ptr(out), _ptr(target), _ptr(weight), H * W, _ptr(ws["d"]),
+                      _ptr(ws["mse"]), nparts, out.numel(), s)
         loss = ws["mse"].sum() / out.numel()
         self.backward(ws["d"])
         return loss

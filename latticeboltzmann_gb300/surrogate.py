@@ -71,9 +71,36 @@ def generate(n_samples, n=256, seed=0, device=None, log=None, max_steps=600_000,
     return {"re": re, "u": u, "fields": fields, "steps": steps, "wall": wall, "info": info}
 
 
-def train(net, data, idx, epochs=100, batch=16, lr=1e-3, lr_min=1e-5, log=None, seed=0, val_idx=None):
+def sample_weights(t_all, idx, rho_weight=1.0, max_ratio=100.0):
+    """Loss weight of every (channel, sample) plane of the normalised targets
+    t_all (3, S, n, n): the inverse of the plane's mean square, so that each
+    sample's fields are fit to the same relative accuracy (the density
+    channel (rho - 1) / u0^2 is ~100x smaller at Re 1000 than at Re 10, and
+    with one weight for all samples the high-Re pressure -- the slowest part
+    of those runs to settle -- would hardly count), capped at max_ratio times
+    the smallest weight of the channel, scaled to mean 1 over ``idx`` and
+    multiplied by (rho_weight, 1, 1)."""
+    ms = t_all.pow(2).mean(dim=(2, 3)).double()  # (3, S)
+    w = 1.0 / ms.clamp_min(1e-30)
+    sel = torch.as_tensor(np.asarray(idx), device=w.device)
+    for c in range(w.shape[0]):
+        lo = w[c].index_select(0, sel).min()
+        w[c] = torch.minimum(w[c], lo * max_ratio)
+        w[c] = w[c] / w[c].index_select(0, sel).mean()
+    w[0] *= rho_weight
+    return w.float()
+
+
+def train(net, data, idx, epochs=100, batch=16, lr=1e-3, lr_min=1e-5, log=None, seed=0, val_idx=None,
+          seconds=None, weighting="relative", rho_weight=2.0):
     """Adam on the samples ``idx`` of ``data`` (cosine schedule from lr to lr_min).
-    Returns the history of (epoch, mean train loss, validation loss)."""
+
+    weighting: "relative" (each (channel, sample) plane weighted to the same
+    relative accuracy, the density channel by rho_weight; sample_weights) or
+    "uniform" (one mean squared error over all planes).  seconds: a wall-time
+    budget; after the first epoch the epoch count is set to what fits it (at
+    most ``epochs``) and the schedule spans those.  Returns the history of
+    (epoch, mean train loss, validation rel-L2 of u, of rho - 1)."""
     device = net.device
     fields = data["fields"]
     n = fields.shape[-1]
@@ -82,37 +109,53 @@ def train(net, data, idx, epochs=100, batch=16, lr=1e-3, lr_min=1e-5, log=None, 
     net.out_scale = scale.cpu().numpy()
     t_all = targets / scale[:, None, None, None]
     a_all = net.inputs(data["re"], data["u"], n, n)
+    w_all = sample_weights(t_all, idx, rho_weight) if weighting == "relative" else None
     rng = np.random.default_rng(seed)
     steps_per_epoch = max(1, len(idx) // batch)
     total = epochs * steps_per_epoch
     hist = []
     k = 0
-    for ep in range(epochs):
+    t_start = time.perf_counter()
+    ep = 0
+    while ep < epochs:
         perm = rng.permutation(idx)
         acc = torch.zeros((), dtype=torch.float64, device=device)
         for s in range(steps_per_epoch):
             sel = torch.as_tensor(np.sort(perm[s * batch:(s + 1) * batch]), device=device)
             a = a_all.index_select(1, sel).contiguous()
             t = t_all.index_select(1, sel).contiguous()
-            acc += net.loss_and_backward(a, t)
-            cur = lr_min + 0.5 * (lr - lr_min) * (1 + math.cos(math.pi * k / total))
+            w = None if w_all is None else w_all.index_select(1, sel).contiguous()
+            acc += net.loss_and_backward(a, t, weight=w)
+            cur = lr_min + 0.5 * (lr - lr_min) * (1 + math.cos(math.pi * min(k, total) / total))
             net.adam(cur)
             k += 1
+        if seconds is not None and ep == 0:
+            torch.cuda.synchronize(device)
+            per_epoch = time.perf_counter() - t_start
+            epochs = max(1, min(epochs, int(seconds / per_epoch)))
+            total = epochs * steps_per_epoch
+            if log is not None:
+                log("training: %.2f s per epoch, %d epochs in the %.0f s budget" % (per_epoch, epochs, seconds))
         # once per epoch: a GEMM whose bounded wait gave up left weights or
         # gradients incomplete; stop instead of training on them
         _lib.gemm_status()
-        if log is not None and (ep % 10 == 0 or ep == epochs - 1):
-            vl = evaluate(net, data, val_idx) if val_idx is not None and len(val_idx) else float("nan")
+        if log is not None and (ep % 25 == 0 or ep == epochs - 1):
+            if val_idx is not None and len(val_idx):
+                vl, vr = evaluate(net, data, val_idx, with_rho=True)
+            else:
+                vl = vr = float("nan")
             tl = float(acc) / steps_per_epoch
-            hist.append((ep, tl, vl))
-            log("epoch %d train %.3e val rel-L2 %.3e lr %.2e" % (ep, tl, vl, cur))
+            hist.append((ep, tl, vl, vr))
+            log("epoch %d train %.3e val rel-L2 u %.3e rho-1 %.3e lr %.2e" % (ep, tl, vl, vr, cur))
+        ep += 1
     return hist
 
 
-def evaluate(net, data, idx, batch=16):
-    """Mean relative L2 error of the predicted velocity over the samples idx."""
+def evaluate(net, data, idx, batch=16, with_rho=False):
+    """Mean relative L2 error of the predicted velocity over the samples idx
+    (and, with_rho, of the predicted rho - 1)."""
     n = data["fields"].shape[-1]
-    errs = []
+    errs, rerrs = [], []
     for s in range(0, len(idx), batch):
         sel = np.asarray(idx[s:s + batch])
         rho, ux, uy = net.predict(data["re"][sel], data["u"][sel], n, n)
@@ -120,7 +163,12 @@ def evaluate(net, data, idx, batch=16):
         num = ((ux - f[:, 1]) ** 2 + (uy - f[:, 2]) ** 2).sum(dim=(1, 2)).sqrt()
         den = (f[:, 1] ** 2 + f[:, 2] ** 2).sum(dim=(1, 2)).sqrt()
         errs.append((num / den).cpu())
+        rnum = ((rho - f[:, 0]) ** 2).sum(dim=(1, 2)).sqrt()
+        rden = ((f[:, 0] - 1) ** 2).sum(dim=(1, 2)).sqrt().clamp_min(1e-30)
+        rerrs.append((rnum / rden).cpu())
     _lib.gemm_status()
+    if with_rho:
+        return float(torch.cat(errs).mean()), float(torch.cat(rerrs).mean())
     return float(torch.cat(errs).mean())
 
 
@@ -219,6 +267,11 @@ def main(argv=None):
     ap.add_argument("--n", type=int, default=256)
     ap.add_argument("--held-out", type=int, default=64)
     ap.add_argument("--epochs", type=int, default=150)
+    ap.add_argument("--train-seconds", type=float, default=None,
+                    help="wall-time budget of the training (the epoch count is fitted to it, at most --epochs)")
+    ap.add_argument("--weighting", choices=["relative", "uniform"], default="relative",
+                    help="loss weights per (channel, sample): same relative accuracy for every sample, or one MSE")
+    ap.add_argument("--rho-weight", type=float, default=2.0, help="extra weight of the density channel")
     ap.add_argument("--batch", type=int, default=16)
     ap.add_argument("--lr", type=float, default=1e-3)
     ap.add_argument("--max-steps", type=int, default=600_000)
@@ -257,11 +310,19 @@ def main(argv=None):
     val, tr = perm[:args.held_out], perm[args.held_out:]
     net = FNO2d(device=dev, seed=args.seed)
     t1 = time.perf_counter()
-    hist = train(net, data, tr, epochs=args.epochs, batch=args.batch, lr=args.lr, log=log, val_idx=val)
+    hist = train(net, data, tr, epochs=args.epochs, batch=args.batch, lr=args.lr, log=log, val_idx=val,
+                 seconds=args.train_seconds, weighting=args.weighting, rho_weight=args.rho_weight)
     torch.cuda.synchronize()
     t_train = time.perf_counter() - t1
     net.save(os.path.join(args.out, "fno.npz"))
-    log("training: %.1f s, val rel-L2 %.3e" % (t_train, evaluate(net, data, val)))
+    vu, vr = evaluate(net, data, val, with_rho=True)
+    net.save(os.path.join(args.out, "fno_bf16.npz"), bf16=True, meta={
+        "n": args.n, "samples": args.samples, "seed": args.seed, "steady": int(len(ok)),
+        "held_out_re": data["re"][val].tolist(), "held_out_u": data["u"][val].tolist(),
+        "held_out_cold_steps": data["steps"][val].tolist(), "epochs": int(hist[-1][0]) + 1 if hist else 0,
+        "train_s": t_train, "weighting": args.weighting, "rho_weight": args.rho_weight,
+        "val_rel_l2_u": vu, "val_rel_l2_rho": vr})
+    log("training: %.1f s, val rel-L2 u %.3e rho-1 %.3e" % (t_train, vu, vr))
     res = {"samples": args.samples, "n": args.n, "steady": int(len(ok)), "data_wall_s": data["wall"],
            "data_steps": data["steps"].tolist(), "data_re": data["re"].tolist(), "data_u": data["u"].tolist(),
            "held_out": val.tolist(), "train_s": t_train, "history": hist}

@@ -122,3 +122,38 @@ def test_surrogate_pipeline_small(cuda, tmp_path):
     path = tmp_path / "net.npz"
     net.save(path)
     assert np.allclose(F.FNO2d.load(path, device=cuda).out_scale, net.out_scale)
+
+
+def test_weighted_mse_kernel(cuda):
+    """lbgb_fno_mse_weighted: partials sum to sum w_p (y - t)^2 and
+    d = 2 w_p (y - t) / n, one weight per (channel, sample) plane."""
+    from latticeboltzmann_gb300 import _lib
+    rng = np.random.default_rng(5)
+    C, B, H, W = 3, 4, 6, 10
+    y, t = rng.standard_normal((2, C, B, H, W)).astype(np.float32)
+    w = rng.random((C, B)).astype(np.float32) + 0.1
+    Y, Tt, Wt = (torch.from_numpy(x).to(cuda) for x in (y, t, w))
+    d = torch.empty_like(Y)
+    part = torch.zeros(64, dtype=torch.float64, device=cuda)
+    _lib.call("lbgb_fno_mse_weighted", Y.data_ptr(), Tt.data_ptr(), Wt.data_ptr(), H * W, d.data_ptr(),
+              part.data_ptr(), 64, y.size, torch.cuda.current_stream().cuda_stream)
+    e = y.astype(np.float64) - t
+    ref_loss = (w[:, :, None, None] * e * e).sum()
+    assert abs(float(part.sum()) - ref_loss) < 1e-9 * abs(ref_loss)
+    np.testing.assert_allclose(d.cpu().numpy(), 2 * w[:, :, None, None] * e / y.size, rtol=1e-5, atol=1e-9)
+    with pytest.raises(ValueError):
+        _lib.call("lbgb_fno_mse_weighted", Y.data_ptr(), Tt.data_ptr(), Wt.data_ptr(), 7, d.data_ptr(),
+                  part.data_ptr(), 64, y.size, torch.cuda.current_stream().cuda_stream)
+
+
+def test_bf16_weights_file_gives_the_same_inference(cuda, tmp_path):
+    """save(bf16=True) keeps the matrices as the BF16 values the GEMMs use and
+    the biases in FP32: the loaded network predicts bit for bit the same."""
+    net = F.FNO2d(device=cuda, seed=4)
+    net.out_scale = np.array([0.5, 2.0, 3.0])
+    path = tmp_path / "w.npz"
+    net.save(path, bf16=True, meta={"held_out_re": [12.5]})
+    net2 = F.FNO2d.load(path, device=cuda)
+    assert net2.meta == {"held_out_re": [12.5]}
+    for x, y in zip(net.predict([40.0], [0.07], 24, 32), net2.predict([40.0], [0.07], 24, 32)):
+        assert torch.equal(x, y)
