@@ -307,9 +307,15 @@ LBGB_API int lbgb_chapman_enskog(const void *rho, const void *ux, const void *uy
  * independent problems.  A (m x k) and B (k x n) are BF16; C is FP32, or BF16
  * when c_bf16 != 0 (rounded once, after the FP32 accumulation).  Element
  * (i, j) of X is X[i * x_rs + j * x_cs] and problem z starts at z * x_bs, so
- * any transposed or strided view works.  engine: 0/2 tensor cores
- * (tcgen05.mma, accumulator in tensor memory), 1 CUDA-core reference.  Used
- * by the Fourier-neural-operator surrogate; no counterpart in the reference. */
+ * any transposed or strided view works.  engine: 0 tensor cores, choosing
+ * the TMA pipeline (cp.async.bulk.tensor operand loads, warp-specialised
+ * producer / MMA / epilogue, double-buffered tensor-memory accumulator,
+ * persistent CTAs) when A and B are both K-major (x_cs = 1 for A, x_rs = 1
+ * for B) and their rows are 16-byte aligned, else the
+ * staged kernel; 2 the staged tcgen05 kernel only (operands copied into
+ * shared memory by the threads); 3 the TMA pipeline only (LBGB_EINVAL for
+ * other layouts); 1 CUDA-core reference.  Used by the Fourier-neural-operator
+ * surrogate; no counterpart in the reference. */
 LBGB_API int lbgb_gemm_bf16(int m, int n, int k, const void *A, long long a_rs, long long a_cs,
                             long long a_bs, const void *B, long long b_rs, long long b_cs,
                             long long b_bs, void *C, long long c_rs, long long c_cs, long long c_bs,

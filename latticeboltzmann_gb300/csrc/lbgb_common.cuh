@@ -83,6 +83,7 @@ constexpr float F16_UNSCALE = 1.0f / 16384.0f;
 // converted operands, in one instruction instead of a conversion and an FMA.
 constexpr unsigned short F16_UNSCALE_BITS = 0x0400;    // half 2^-14
 constexpr unsigned short F16_MINUS_ONE_BITS = 0xbc00;  // half -1
+constexpr unsigned short F16_ONE_BITS = 0x3c00;        // half 1
 template <bool BF>
 __device__ __forceinline__ float fma16(unsigned short a, unsigned short b, float c) {
     float d;
@@ -232,6 +233,27 @@ struct Packet {
             return Codec<DT>::dec_h(x);
         else
             return x;
+    }
+    // the stored 16-bit values of a packet as FP32 without unscaling (FP16:
+    // the deviation times 2^14, exactly; bfloat16: the deviation)
+    static __device__ __forceinline__ void dec_units(const vec &x, real (&o)[N]) {
+        uint32_t wd[WORDS];
+        memcpy(wd, &x, BYTES);
+#pragma unroll
+        for (int q = 0; q < WORDS; ++q) {
+            if constexpr (DT == LBGB_F16DEV) {
+                fma16x2<false>(wd[q], F16_ONE_BITS, 0.f, 0.f, o[2 * q], o[2 * q + 1]);
+            } else {
+                o[2 * q] = __uint_as_float(wd[q] << 16);
+                o[2 * q + 1] = __uint_as_float(wd[q] & 0xffff0000u);
+            }
+        }
+    }
+    static __device__ __forceinline__ real dec1_units(raw x) {
+        if constexpr (DT == LBGB_F16DEV)
+            return __half2float(__ushort_as_half(x));
+        else
+            return Codec<DT>::dec_h(x);
     }
     // packs N FP16 values that are already scaled by 2^14, two per conversion
     static __device__ __forceinline__ vec enc_scaled(const real (&hs)[N]) {
@@ -511,16 +533,21 @@ __device__ __forceinline__ void bgk_collide_native(R (&f)[9], R omega) {
 // at 9e-8 after 1000 and 2000 steps, the storage floor.  Same equilibrium as
 // w_i rho (1 + 3 c.u + 4.5 (c.u)^2 - 1.5 u^2) (c/d2q9.h:59-81) in exact
 // arithmetic.  REST = false leaves h_0 to the caller, which writes it from
-// the rounded stored values.  Returns D.
-template <bool REST = true>
+// the rounded stored values.  LOG2K: the values are h 2^LOG2K (FP16 storage
+// keeps its deviations scaled by 2^14; a kernel that collides in those units
+// skips a scaling per value on decode and encode).  Every operation commutes
+// exactly with the power-of-two scale, so the results are bit for bit the
+// unscaled ones times 2^LOG2K.  Returns D (in the same units).
+template <bool REST = true, int LOG2K = 0>
 __device__ __forceinline__ float collide_dev(float (&h)[9], float omega) {
+    constexpr float UNIT = 1.f / (float)(1u << LOG2K);
     const float a13 = h[1] - h[3], b13 = h[1] + h[3];
     const float a24 = h[2] - h[4], b24 = h[2] + h[4];
     const float a57 = h[5] - h[7], b57 = h[5] + h[7];
     const float a68 = h[6] - h[8], b68 = h[6] + h[8];
     const float d = (((h[0] + b13) + b24) + b57) + b68;
     const float jx = (a13 + a57) - a68, jy = (a24 + a57) + a68;
-    const float inv = recip_approx(1.f + d);
+    const float inv = recip_approx(fmaf(d, UNIT, 1.f)) * UNIT;
     const float ux = jx * inv, uy = jy * inv;
     const float base = fmaf(-1.5f, fmaf(jx, ux, jy * uy), d);
     const float sx = jx + jy, sy = jy - jx;
@@ -561,9 +588,12 @@ __device__ __forceinline__ R lid_term(R rho_lid, R u0) {
 // deviations and rho_lid = 1 + s: c + c s with c = (6 w) u0 rounded once, so
 // that the low bits of s are not lost in a rounding of 1 + s (which would
 // repeat itself at every lid node and step).
+// With the deviations in units of 2^-LOG2K (see collide_dev) the term is
+// c s + c 2^LOG2K, the same value in those units.
+template <int LOG2K = 0>
 __device__ __forceinline__ float lid_term_dev(float s, float u0) {
     const float c = (6.f * (1.f / 36.f)) * u0;
-    return fmaf(c, s, c);
+    return fmaf(c, s, c * (float)(1u << LOG2K));
 }
 
 // Equilibrium of one node (same formulation as above).

@@ -16,6 +16,7 @@
 //
 // SIMT path (k_gemm_simt): the same contract with FP32 FMAs; the reference the
 // tensor-core path is tested against.
+#include <cuda.h>
 #include <stdio.h>
 
 #include "lbgb_common.cuh"
@@ -27,13 +28,15 @@ __device__ int g_gemm_status;
 __device__ __forceinline__ uint32_t smem_u32(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
 
 // shared-memory matrix descriptor (tcgen05): start address, leading and stride
-// byte offsets (16-byte units), descriptor version bit 46, no swizzle
-__device__ __forceinline__ uint64_t umma_desc(uint32_t saddr, uint32_t lbo, uint32_t sbo) {
+// byte offsets (16-byte units), descriptor version bit 46, layout type in
+// bits 61-63 (0: no swizzle, 2: 128-byte swizzle)
+__device__ __forceinline__ uint64_t umma_desc(uint32_t saddr, uint32_t lbo, uint32_t sbo, uint32_t layout = 0) {
     uint64_t d = 0;
     d |= (uint64_t)((saddr & 0x3ffffu) >> 4);
     d |= (uint64_t)((lbo >> 4) & 0x3fffu) << 16;
     d |= (uint64_t)((sbo >> 4) & 0x3fffu) << 32;
     d |= (uint64_t)1 << 46;
+    d |= (uint64_t)(layout & 7u) << 61;
     return d;
 }
 
@@ -425,11 +428,373 @@ static int tc_dyn_smem() {
     return d;
 }
 
+// ---------------------------------------------------------------- TMA pipeline
+// Persistent, warp-specialised GEMM for products whose A and B are both
+// K-major (k contiguous: A(r, k) = A[r * a_rs + k], B(k, n) = B[n * b_cs + k]),
+// rows 16-byte aligned -- the forward W and H transforms, the inverse W
+// transform and the split-K weight gradients of the surrogate.
+//
+//  * warp 0, one thread: TMA producer.  Per 64-deep K block it issues one
+//    cp.async.bulk.tensor load of A (128 rows x 64 k) and one of B (NT rows
+//    x 64 k): 128-byte rows with the 128-byte swizzle, which is the
+//    tcgen05 K-major SWIZZLE_128B layout (8-row atoms of 1024 bytes; the
+//    MMAs step through K by advancing the descriptor 32 bytes).
+//    Out-of-range rows and k read as zeros.  A ring of STAGES stages,
+//    full/empty mbarriers.
+//  * warp 1, one thread: issues tcgen05.mma (M = 128, N = NT, K = 16) into
+//    one of two TMEM accumulators and commits each stage back to the
+//    producer and each finished tile to the epilogue.
+//  * warps 2-9: epilogue.  Warp w reads TMEM lanes 32 (w % 4) .. + 31 (the
+//    lane quarter it may access) and half of the tile's columns, applies
+//    alpha/beta and stores; then frees the accumulator, so the MMAs of the
+//    next tile run while this one drains.
+// Every wait is bounded: a timeout sets the status word and ends that role's
+// loop; the other roles' bounded waits then run out in turn, the producer
+// waits for its copies in flight and the MMA thread for its last commit
+// before the tensor memory is released.
+constexpr int TP_KB = 64;
+constexpr int TP_THREADS = 320;
+
+template <int NT>
+struct TmaShape {
+    static constexpr int A_BYTES = TC_M * TP_KB * 2;
+    static constexpr int B_BYTES = NT * TP_KB * 2;
+    static constexpr int STAGE = A_BYTES + B_BYTES;
+    // two CTAs per SM: ~82-97 KB of dynamic shared memory each
+    static constexpr int STAGES = NT == 128 ? 2 : (NT == 64 ? 3 : 4);
+    static constexpr int EPI = 8 * 32 * 17 * 4;
+    static constexpr int SMEM = STAGES * STAGE + EPI;
+};
+
+__device__ __forceinline__ void mbar_arrive_g(uint64_t *bar) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx_g(uint64_t *bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
+}
+// one box of a 2-D (x = k, y = row) or 3-D (z = problem) tensor map
+__device__ __forceinline__ void tma_load_box(void *dst, const CUtensorMap *map, bool three_d, int x, int y, int z,
+                                             uint64_t *bar) {
+    if (three_d)
+        asm volatile(
+            "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], "
+            "[%5];" ::"r"(smem_u32(dst)),
+            "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(z), "r"(smem_u32(bar))
+            : "memory");
+    else
+        asm volatile(
+            "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];" ::"r"(
+                smem_u32(dst)),
+            "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(smem_u32(bar))
+            : "memory");
+}
+__device__ __forceinline__ void tc_ld16(uint32_t taddr, uint32_t (&v)[16]) {
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, "
+        "%14, %15}, [%16];"
+        : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7]), "=r"(v[8]),
+          "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]), "=r"(v[15])
+        : "r"(taddr));
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+}
+
+template <int NT, typename OUT>
+__global__ void __launch_bounds__(TP_THREADS, 2)
+k_gemm_tma(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB, int a3d, int b3d, int M,
+           int N, int K, int batch, OUT *__restrict__ C, long long c_rs, long long c_cs, long long c_bs, float alpha,
+           float beta) {
+    using S = TmaShape<NT>;
+    constexpr int STAGES = S::STAGES;
+    extern __shared__ __align__(1024) unsigned char dsm[];
+    float *estage = reinterpret_cast<float *>(dsm + STAGES * S::STAGE);
+    __shared__ __align__(8) uint64_t full[STAGES], empty[STAGES], tfull[2], tempty[2];
+    __shared__ uint32_t tmem_slot;
+
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int tiles_m = (M + TC_M - 1) / TC_M, tiles_n = (N + NT - 1) / NT;
+    const long long tiles = (long long)tiles_m * tiles_n * batch;
+    const int kblocks = (K + TP_KB - 1) / TP_KB;
+
+    if (warp == 1) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&tmem_slot)),
+                     "r"((uint32_t)(2 * NT))
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < STAGES; ++s) {
+            mbar_init_g(&full[s], 1);
+            mbar_init_g(&empty[s], 1);
+        }
+        for (int b = 0; b < 2; ++b) {
+            mbar_init_g(&tfull[b], 1);
+            mbar_init_g(&tempty[b], 8 * 32);
+        }
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    const uint32_t tmem = tmem_slot;
+
+    if (warp == 0) {
+        if (lane == 0) {
+            long long it = 0;
+            bool ok = true;
+            for (long long t = blockIdx.x; t < tiles && ok; t += gridDim.x) {
+                const int z = (int)(t / ((long long)tiles_m * tiles_n));
+                const int rem = (int)(t - (long long)z * tiles_m * tiles_n);
+                const int nt = rem / tiles_m, mt = rem - nt * tiles_m;
+                for (int kb = 0; kb < kblocks; ++kb, ++it) {
+                    const int s = (int)(it % STAGES);
+                    const uint32_t ph = (uint32_t)(it / STAGES) & 1u;
+                    if (!mbar_wait_g(&empty[s], ph ^ 1u, TC_WAIT)) {
+                        atomicCAS(&g_gemm_status, 0, 2);
+                        ok = false;
+                        break;
+                    }
+                    mbar_expect_tx_g(&full[s], (uint32_t)S::STAGE);
+                    unsigned char *sa = dsm + (size_t)s * S::STAGE, *sb = sa + S::A_BYTES;
+                    tma_load_box(sa, &tmA, a3d != 0, kb * TP_KB, mt * TC_M, z, &full[s]);
+                    tma_load_box(sb, &tmB, b3d != 0, kb * TP_KB, nt * NT, z, &full[s]);
+                }
+            }
+            // the copies of the last stages land before the CTA can exit
+            for (long long j = it > STAGES ? it - STAGES : 0; j < it; ++j)
+                mbar_wait_g(&full[j % STAGES], (uint32_t)(j / STAGES) & 1u, TC_WAIT);
+        }
+    } else if (warp == 1) {
+        if (lane == 0) {
+            constexpr uint32_t idesc = umma_idesc_bf16(TC_M, NT);
+            long long it = 0;
+            int tc = 0;
+            bool ok = true;
+            uint64_t *last = nullptr;  // the barrier of the last commit, and its phase
+            uint32_t last_ph = 0;
+            for (long long t = blockIdx.x; t < tiles && ok; t += gridDim.x, ++tc) {
+                const int buf = tc & 1;
+                const uint32_t aph = (uint32_t)(tc >> 1) & 1u;
+                if (!mbar_wait_g(&tempty[buf], aph ^ 1u, TC_WAIT)) {
+                    atomicCAS(&g_gemm_status, 0, 3);
+                    break;
+                }
+                asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+                const uint32_t d = tmem + (uint32_t)(buf * NT);
+                for (int kb = 0; kb < kblocks; ++kb, ++it) {
+                    const int s = (int)(it % STAGES);
+                    const uint32_t ph = (uint32_t)(it / STAGES) & 1u;
+                    if (!mbar_wait_g(&full[s], ph, TC_WAIT)) {
+                        atomicCAS(&g_gemm_status, 0, 4);
+                        ok = false;
+                        break;
+                    }
+                    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+                    const uint32_t sa = smem_u32(dsm + (size_t)s * S::STAGE), sb = sa + S::A_BYTES;
+#pragma unroll
+                    for (int kk = 0; kk < TP_KB / 16; ++kk) {
+                        // K = 16 = 32 bytes of each 128-byte swizzled row; 8-row atoms 1024 bytes apart
+                        const uint64_t da = umma_desc(sa + kk * 32, 16, 1024, 2);
+                        const uint64_t db = umma_desc(sb + kk * 32, 16, 1024, 2);
+                        const uint32_t acc = (kb > 0 || kk > 0) ? 1u : 0u;
+                        asm volatile(
+                            "{\n\t.reg .pred p;\n\t"
+                            "setp.ne.u32 p, %4, 0;\n\t"
+                            "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(d),
+                            "l"(da), "l"(db), "r"(idesc), "r"(acc)
+                            : "memory");
+                    }
+                    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                                     smem_u32(&empty[s]))
+                                 : "memory");
+                    last = &empty[s];
+                    last_ph = ph;
+                }
+                if (!ok) break;
+                asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                                 smem_u32(&tfull[buf]))
+                             : "memory");
+                last = &tfull[buf];  // completes phase tc >> 1 of tfull[buf]
+                last_ph = aph;
+            }
+            // MMAs still in flight must finish before the tensor memory is freed
+            if (last) mbar_wait_g(last, last_ph, TC_WAIT);
+        }
+    } else {
+        const int ew = warp - 2, q = warp & 3, half = ew >> 2;
+        float *ostage = estage + ew * (32 * 17);
+        int tc = 0;
+        for (long long t = blockIdx.x; t < tiles; t += gridDim.x, ++tc) {
+            const int buf = tc & 1;
+            const uint32_t ph = (uint32_t)(tc >> 1) & 1u;
+            const bool w = mbar_wait_g(&tfull[buf], ph, TC_WAIT);
+            if (!w) atomicCAS(&g_gemm_status, 0, 5);
+            if (__any_sync(0xffffffffu, !w)) break;
+            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+            const int z = (int)(t / ((long long)tiles_m * tiles_n));
+            const int rem = (int)(t - (long long)z * tiles_m * tiles_n);
+            const int nt = rem / tiles_m, mt = rem - nt * tiles_m;
+            const int m0 = mt * TC_M + q * 32, n0 = nt * NT;
+            OUT *Cz = C + (long long)z * c_bs;
+#pragma unroll 1
+            for (int c0 = half * (NT / 2); c0 < (half + 1) * (NT / 2); c0 += 16) {
+                uint32_t v[16];
+                tc_ld16(tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(buf * NT + c0), v);
+                if (c_cs == 1 && c_rs != 1) {
+                    // row-major C: stage the warp's 32 x 16 block and write two
+                    // rows per instruction, 16 consecutive columns each
+#pragma unroll
+                    for (int j = 0; j < 16; ++j) ostage[lane * 17 + j] = __uint_as_float(v[j]);
+                    __syncwarp();
+                    const int j = lane & 15, col = n0 + c0 + j;
+                    float old[16];
+#pragma unroll
+                    for (int i = 0; i < 16; ++i) {
+                        const int row = m0 + 2 * i + (lane >> 4);
+                        old[i] = (beta != 0.f && row < M && col < N) ? load_out(Cz + (long long)row * c_rs + col) : 0.f;
+                    }
+#pragma unroll
+                    for (int i = 0; i < 16; ++i) {
+                        const int r = 2 * i + (lane >> 4), row = m0 + r;
+                        if (row < M && col < N)
+                            store_out(Cz + (long long)row * c_rs + col, alpha * ostage[r * 17 + j] + beta * old[i]);
+                    }
+                    __syncwarp();
+                } else {
+                    const int row = m0 + lane;
+                    if (row < M) {
+                        float old[16];
+#pragma unroll
+                        for (int j = 0; j < 16; ++j) {
+                            const int col = n0 + c0 + j;
+                            old[j] = (beta != 0.f && col < N) ? load_out(Cz + (long long)row * c_rs + (long long)col * c_cs)
+                                                              : 0.f;
+                        }
+#pragma unroll
+                        for (int j = 0; j < 16; ++j) {
+                            const int col = n0 + c0 + j;
+                            if (col < N)
+                                store_out(Cz + (long long)row * c_rs + (long long)col * c_cs,
+                                          alpha * __uint_as_float(v[j]) + beta * old[j]);
+                        }
+                    }
+                }
+            }
+            asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+            mbar_arrive_g(&tempty[buf]);
+        }
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    if (warp == 1)
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"((uint32_t)(2 * NT))
+                     : "memory");
+}
+
+// cuTensorMapEncodeTiled from the driver, looked up once through the runtime
+// (the library links only the CUDA runtime)
+typedef CUresult (*EncodeTiledFn)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *, const cuuint64_t *,
+                                  const cuuint64_t *, const cuuint32_t *, const cuuint32_t *, CUtensorMapInterleave,
+                                  CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+static EncodeTiledFn encode_tiled() {
+    static std::atomic<EncodeTiledFn> fn{nullptr};
+    static std::atomic<bool> tried{false};
+    EncodeTiledFn f = fn.load(std::memory_order_acquire);
+    if (f || tried.load(std::memory_order_acquire)) return f;
+    std::lock_guard<std::mutex> lock(setup_mutex());
+    if (!tried.load(std::memory_order_relaxed)) {
+        void *p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn.store(reinterpret_cast<EncodeTiledFn>(p), std::memory_order_release);
+        tried.store(true, std::memory_order_release);
+    }
+    return fn.load(std::memory_order_acquire);
+}
+
+// Tensor map of a K-major BF16 operand: rows x k, element (r, k) at
+// X[r * rs + k], problem z at X + z * bs (3-D map when batch > 1 and bs != 0,
+// else 2-D); box: 64 k (128 bytes, 128-byte swizzle) x box_rows rows.  False
+// if TMA cannot address it.
+static bool kmajor_map(CUtensorMap *map, const __nv_bfloat16 *X, long long rows, long long k, long long rs, int batch,
+                       long long bs, int box_rows, int *three_d) {
+    EncodeTiledFn enc = encode_tiled();
+    if (!enc || !aligned(X, 16) || rs % 8 || rs <= 0 || bs % 8 || bs < 0 || k <= 0 || rows <= 0) return false;
+    const bool use3 = batch > 1 && bs != 0;
+    cuuint64_t dims[3] = {(cuuint64_t)k, (cuuint64_t)rows, (cuuint64_t)batch};
+    cuuint64_t strides[2] = {(cuuint64_t)rs * 2, (cuuint64_t)bs * 2};
+    cuuint32_t box[3] = {(cuuint32_t)TP_KB, (cuuint32_t)box_rows, 1};
+    cuuint32_t estr[3] = {1, 1, 1};
+    const CUresult r = enc(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, use3 ? 3 : 2, const_cast<__nv_bfloat16 *>(X), dims,
+                           strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+                           CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    *three_d = use3 ? 1 : 0;
+    return r == CUDA_SUCCESS;
+}
+
+// Launches the TMA pipeline if A and B are K-major and TMA can address them;
+// returns 1 (nothing launched) when it cannot, so the caller falls back.
+template <int NT, typename OUT>
+static int launch_gemm_tma_nt(int m, int n, int k, const __nv_bfloat16 *a, long long a_rs, long long a_bs,
+                              const __nv_bfloat16 *b, long long b_cs, long long b_bs, OUT *C, long long c_rs,
+                              long long c_cs, long long c_bs, int batch, float alpha, float beta, cudaStream_t s) {
+    using S = TmaShape<NT>;
+    CUtensorMap ma, mb;
+    int a3 = 0, b3 = 0;
+    if (!kmajor_map(&ma, a, m, k, a_rs, batch, a_bs, TC_M, &a3) || !kmajor_map(&mb, b, n, k, b_cs, batch, b_bs, NT, &b3))
+        return 1;
+    static std::atomic<bool> attr[MAX_DEVICES];
+    const int dev = current_device();
+    if (!attr[dev].load(std::memory_order_acquire)) {
+        std::lock_guard<std::mutex> lock(setup_mutex());
+        const cudaError_t e =
+            cudaFuncSetAttribute(k_gemm_tma<NT, OUT>, cudaFuncAttributeMaxDynamicSharedMemorySize, S::SMEM);
+        if (e != cudaSuccess) {
+            set_error("k_gemm_tma: cannot reserve %d bytes of shared memory: %s", S::SMEM, cudaGetErrorString(e));
+            return LBGB_ECUDA;
+        }
+        attr[dev].store(true, std::memory_order_release);
+    }
+    int sms = 0;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    const long long tiles = (long long)((m + TC_M - 1) / TC_M) * ((n + NT - 1) / NT) * batch;
+    const long long slots = 2ll * (sms > 0 ? sms : 1);
+    const int grid = (int)(tiles < slots ? tiles : slots);
+    k_gemm_tma<NT, OUT><<<grid, TP_THREADS, S::SMEM, s>>>(ma, mb, a3, b3, m, n, k, batch, C, c_rs, c_cs, c_bs, alpha,
+                                                          beta);
+    return check_launch("k_gemm_tma");
+}
+
+template <typename OUT>
+static int launch_gemm_tma(int m, int n, int k, const __nv_bfloat16 *a, long long a_rs, long long a_cs, long long a_bs,
+                           const __nv_bfloat16 *b, long long b_rs, long long b_cs, long long b_bs, OUT *C,
+                           long long c_rs, long long c_cs, long long c_bs, int batch, float alpha, float beta,
+                           cudaStream_t s) {
+    if (a_cs != 1 || b_rs != 1 || k <= 0) return 1;
+    if (n <= 32) return launch_gemm_tma_nt<32>(m, n, k, a, a_rs, a_bs, b, b_cs, b_bs, C, c_rs, c_cs, c_bs, batch, alpha,
+                                               beta, s);
+    if (n <= 64) return launch_gemm_tma_nt<64>(m, n, k, a, a_rs, a_bs, b, b_cs, b_bs, C, c_rs, c_cs, c_bs, batch, alpha,
+                                               beta, s);
+    return launch_gemm_tma_nt<128>(m, n, k, a, a_rs, a_bs, b, b_cs, b_bs, C, c_rs, c_cs, c_bs, batch, alpha, beta, s);
+}
+
 template <typename OUT>
 static int launch_gemm(int m, int n, int k, const __nv_bfloat16 *a, long long a_rs, long long a_cs, long long a_bs,
                        const __nv_bfloat16 *b, long long b_rs, long long b_cs, long long b_bs, OUT *C, long long c_rs,
                        long long c_cs, long long c_bs, int batch, float alpha, float beta, int engine,
                        cudaStream_t s) {
+    if (engine == 0 || engine == 3) {
+        // both operands K-major: the TMA pipeline (engine 3 insists on it)
+        const int rc = k > 0 ? launch_gemm_tma(m, n, k, a, a_rs, a_cs, a_bs, b, b_rs, b_cs, b_bs, C, c_rs, c_cs, c_bs,
+                                               batch, alpha, beta, s)
+                             : 1;
+        if (rc <= 0) return rc;
+        if (engine == 3) {
+            set_error("lbgb_gemm_bf16: engine 3 needs K-major A and B with 16-byte aligned rows");
+            return LBGB_EINVAL;
+        }
+    }
     if (engine == 1 || k == 0) {  // K = 0: C = beta C, no tensor-core work
         dim3 grid((m + 63) / 64, (n + 63) / 64, batch);
         k_gemm_simt<OUT><<<grid, 256, 0, s>>>(m, n, k, a, a_rs, a_cs, a_bs, b, b_rs, b_cs, b_bs, C, c_rs, c_cs, c_bs,
@@ -481,7 +846,7 @@ extern "C" int lbgb_gemm_bf16(int m, int n, int k, const void *A, long long a_rs
         set_error("lbgb_gemm_bf16: null operand");
         return LBGB_EINVAL;
     }
-    if (engine != 0 && engine != 1 && engine != 2) {
+    if (engine < 0 || engine > 3) {
         set_error("lbgb_gemm_bf16: unknown engine %d", engine);
         return LBGB_EINVAL;
     }

@@ -113,6 +113,16 @@ k_step_pipe(const typename Codec<DT>::raw *__restrict__ src, typename Codec<DT>:
     using G = PipeGeom<raw, NCW_, NC_>;
     using P = Packet<DT, NC_>;
     constexpr int NC = G::NC, HALO = G::HALO, L = G::L, SLOT = G::SLOT, NCW = G::NCW;
+    // FP16 collisions run in the stored units (deviations times 2^14): no
+    // scaling per value on decode or encode, bit for bit the same results
+    constexpr bool UNITS = DT == LBGB_F16DEV && COLLIDE;
+    constexpr int LOG2K = UNITS ? 14 : 0;
+    auto decv = [&](raw x, int ch) -> real {
+        if constexpr (UNITS)
+            return P::dec1_units(x);
+        else
+            return C::dec(x, ch);
+    };
 
     extern __shared__ __align__(128) unsigned char smem[];
     raw *slots = reinterpret_cast<raw *>(smem);
@@ -193,7 +203,10 @@ k_step_pipe(const typename Codec<DT>::raw *__restrict__ src, typename Codec<DT>:
 #pragma unroll
             for (int i = 0; i < 9; ++i) {
                 const raw *sl = stage + i * SLOT + HALO + t * NC;
-                P::dec(*reinterpret_cast<const typename P::vec *>(sl), wgt<real>(i), v[i]);
+                if constexpr (UNITS)
+                    P::dec_units(*reinterpret_cast<const typename P::vec *>(sl), v[i]);
+                else
+                    P::dec(*reinterpret_cast<const typename P::vec *>(sl), wgt<real>(i), v[i]);
                 const bool wall = (cx(i) > 0 && wl) || (cx(i) < 0 && wr);
                 if (wall || cy(i) == 0) continue;
                 int row = k - cx(i);
@@ -201,18 +214,18 @@ k_step_pipe(const typename Codec<DT>::raw *__restrict__ src, typename Codec<DT>:
                 if (cy(i) > 0) {
                     real prev = 0;
                     if (c > 0)
-                        prev = P::dec1(sl[-1], wgt<real>(i));
+                        prev = decv(sl[-1], i);
                     else if (BC == LBGB_PERIODIC)
-                        prev = C::dec(ld1(src + (size_t)i * cs + (size_t)row * ny + (ny - 1)), i);
+                        prev = decv(ld1(src + (size_t)i * cs + (size_t)row * ny + (ny - 1)), i);
 #pragma unroll
                     for (int j = NC - 1; j > 0; --j) v[i][j] = v[i][j - 1];
                     v[i][0] = prev;
                 } else {
                     real next = 0;
                     if (c + NC < ny)
-                        next = P::dec1(sl[NC], wgt<real>(i));
+                        next = decv(sl[NC], i);
                     else if (BC == LBGB_PERIODIC)
-                        next = C::dec(ld1(src + (size_t)i * cs + (size_t)row * ny), i);
+                        next = decv(ld1(src + (size_t)i * cs + (size_t)row * ny), i);
 #pragma unroll
                     for (int j = 0; j < NC - 1; ++j) v[i][j] = v[i][j + 1];
                     v[i][NC - 1] = next;
@@ -223,7 +236,7 @@ k_step_pipe(const typename Codec<DT>::raw *__restrict__ src, typename Codec<DT>:
         if (!act) continue;
 
         if (BC != LBGB_PERIODIC) {
-            auto g = [&](int ch, int row, int l) { return C::dec(ld1(src + (size_t)ch * cs + (size_t)row * ny + l), ch); };
+            auto g = [&](int ch, int row, int l) { return decv(ld1(src + (size_t)ch * cs + (size_t)row * ny + l), ch); };
             if (c == 0) {
                 v[CN][0] = g(CS, k, 0);
                 v[CNE][0] = g(CSW, k, 0);
@@ -232,7 +245,7 @@ k_step_pipe(const typename Codec<DT>::raw *__restrict__ src, typename Codec<DT>:
             if (c + NC == ny) {
                 const int T = ny - 1;
                 if (BC == LBGB_CAVITY_LADD) {
-                    const real lid = real(6) * real(1.0 / 36.0) * u0;
+                    const real lid = real(6) * real(1.0 / 36.0) * u0 * real(1u << LOG2K);
                     v[CS][NC - 1] = g(CN, k, T);
                     v[CSE][NC - 1] = g(CNW, k, T) + lid;
                     v[CSW][NC - 1] = g(CNE, k, T) - lid;
@@ -242,7 +255,11 @@ k_step_pipe(const typename Codec<DT>::raw *__restrict__ src, typename Codec<DT>:
                     const real gN = g(CN, k, T), gNW = g(CNW, k, T), gNE = g(CNE, k, T);
                     const real rho_lid = gNW + gN + gNE + g(CNW, ke, T - 1) + g(CN, k, T - 1) + g(CNE, kw, T - 1) +
                                          g(CW, ke, T) + g(C0, k, T) + g(CE, kw, T);
-                    const real lid = lid_from_sum<C>(rho_lid, u0);
+                    real lid;
+                    if constexpr (UNITS)
+                        lid = lid_term_dev<LOG2K>(rho_lid, u0);
+                    else
+                        lid = lid_from_sum<C>(rho_lid, u0);
                     v[CS][NC - 1] = gN;
                     v[CSE][NC - 1] = (k == 0) ? gNW : gNW + lid;
                     v[CSW][NC - 1] = (k == nx - 1) ? gNE : gNE - lid;
@@ -268,9 +285,9 @@ k_step_pipe(const typename Codec<DT>::raw *__restrict__ src, typename Codec<DT>:
                     real h[9];
 #pragma unroll
                     for (int i = 0; i < 9; ++i) h[i] = v[i][j];
-                    hs[0][j] = collide_dev<false>(h, omega) * F16_SCALE;
+                    hs[0][j] = collide_dev<false, LOG2K>(h, omega);
 #pragma unroll
-                    for (int i = 1; i < 9; ++i) hs[i][j] = h[i] * F16_SCALE;
+                    for (int i = 1; i < 9; ++i) hs[i][j] = h[i];
                 }
                 typename P::vec pk[9];
 #pragma unroll
@@ -299,9 +316,9 @@ k_step_pipe(const typename Codec<DT>::raw *__restrict__ src, typename Codec<DT>:
                 real h[9];
 #pragma unroll
                 for (int i = 0; i < 9; ++i) h[i] = v[i][j];
-                dm[j] = collide_dev<!keep_mass>(h, omega);
+                dm[j] = collide_dev<!keep_mass, LOG2K>(h, omega);
 #pragma unroll
-                for (int i = 0; i < 9; ++i) hpost[i][j] = sr ? sr_dev<DT>(h[i]) : h[i];
+                for (int i = 0; i < 9; ++i) hpost[i][j] = (sr && !UNITS) ? sr_dev<DT>(h[i]) : h[i];
             }
             uint32_t base[NC / 2];
             if constexpr (sr) {
@@ -323,13 +340,19 @@ k_step_pipe(const typename Codec<DT>::raw *__restrict__ src, typename Codec<DT>:
                     uint32_t wd[NC / 2];
                     memcpy(wd, &pk, sizeof(wd));
 #pragma unroll
-                    for (int q = 0; q < NC / 2; ++q) sub_stored2<DT>(dm[2 * q], dm[2 * q + 1], wd[q]);
+                    for (int q = 0; q < NC / 2; ++q) {
+                        if constexpr (UNITS)
+                            fma16x2<false>(wd[q], F16_MINUS_ONE_BITS, dm[2 * q], dm[2 * q + 1], dm[2 * q],
+                                           dm[2 * q + 1]);
+                        else
+                            sub_stored2<DT>(dm[2 * q], dm[2 * q + 1], wd[q]);
+                    }
                 }
                 st_cs(reinterpret_cast<typename P::vec *>(out_row + (size_t)i * cs), pk);
             }
             if constexpr (keep_mass) {
 #pragma unroll
-                for (int j = 0; j < NC; ++j) hpost[0][j] = sr ? sr_rest<DT>(dm[j]) : dm[j];
+                for (int j = 0; j < NC; ++j) hpost[0][j] = (sr && !UNITS) ? sr_rest<DT>(dm[j]) : dm[j];
             }
             typename P::vec pk0;
             if constexpr (sr)

@@ -39,7 +39,9 @@ import torch
 
 from . import _lib
 
-ENGINE_TENSOR_CORES, ENGINE_CUDA_CORES = 0, 1
+# GEMM engines: tensor cores (the TMA pipeline where both operands are
+# K-major, else the staged kernel), CUDA cores, the staged tensor-core kernel
+ENGINE_TENSOR_CORES, ENGINE_CUDA_CORES, ENGINE_STAGED = 0, 1, 2
 RE_RANGE = (10.0, 1000.0)
 U_RANGE = (0.05, 0.1)
 
@@ -220,8 +222,11 @@ class FNO2d:
             if Hp < 2 * self.modes or Wp // 2 + 1 < self.modes:
                 raise ValueError("grid %dx%d too small for %d modes" % (H, W, self.modes))
             fw, G, iw = dft_matrices(H, W, self.modes, Hp, Wp)
+            # G and iw also transposed: the backward products that read them
+            # along their other axis then have both operands K-major (the
+            # GEMM's TMA pipeline)
             self._mats[key] = tuple(torch.as_tensor(x, dtype=torch.bfloat16, device=self.device).contiguous()
-                                    for x in (fw, G, iw))
+                                    for x in (fw, G, iw, G.T, iw.T))
         return self._mats[key]
 
     def _workspace(self, B, H, W, train):
@@ -268,7 +273,7 @@ class FNO2d:
         N = B * H * W
         ws = self._workspace(B, H, W, train)
         self._shape = (B, H, W)
-        fw, G, iw = self.matrices(H, W)
+        fw, G, iw, _, _ = self.matrices(H, W)
         C, m = self.width, self.modes
         q2, m2 = 4 * m, 2 * m
         s = self._s()
@@ -346,7 +351,7 @@ class FNO2d:
         B, H, W = self._shape
         N = B * H * W
         ws = self._ws[(B, H, W, True)]
-        fw, G, iw = self.matrices(H, W)
+        fw, G, iw, Gt, iwt = self.matrices(H, W)
         C, m, hid = self.width, self.modes, self.hidden
         q2, m2 = 4 * m, 2 * m
         s = self._s()
@@ -374,14 +379,14 @@ class FNO2d:
             self._wgrad(C, C, N, _ptr(dzb), _ptr(v), _ptr(g, o["W%d" % l]), C, 1, ws)
             _lib.call("lbgb_fno_row_sum", _ptr(dv), _ptr(g, o["b%d" % l]), _ptr(ws["rowsum"]), C, N, s)
             # spectral branch, transposed step by step
-            self._gemm(C * B * H, m2, W, _ptr(dzb), (W, 1, 0), _ptr(iw), (m2, 1, 0), _ptr(ws["Z"]), (m2, 1, 0),
+            self._gemm(C * B * H, m2, W, _ptr(dzb), (W, 1, 0), _ptr(iwt), (1, W, 0), _ptr(ws["Z"]), (m2, 1, 0),
                        bf16_out=True)
             self._gemm(q2, m2, H, _ptr(G), (H, 1, 0), _ptr(ws["Z"]), (m2, 1, H * m2), _ptr(ws["dYm"]),
                        (m2, 1, q2 * m2), batch=C * B)
             _lib.call("lbgb_fno_mix_back", _ptr(ws["dYm"]), _ptr(ws["Pm"][l]), _ptr(pb, o["Rr%d" % l]),
                       _ptr(pb, o["Ri%d" % l]), _ptr(ws["dP"]), _ptr(g, o["Rr%d" % l]), _ptr(g, o["Ri%d" % l]),
                       C, C, B, 2 * m, m, s)
-            self._gemm(C * B * m2, H, q2, _ptr(ws["dP"]), (q2, 1, 0), _ptr(G), (H, 1, 0), _ptr(ws["X1p"]),
+            self._gemm(C * B * m2, H, q2, _ptr(ws["dP"]), (q2, 1, 0), _ptr(Gt), (1, q2, 0), _ptr(ws["X1p"]),
                        (H, 1, 0), bf16_out=True)
             # pointwise branch: dv = W^T dz, then the spectral branch's input gradient on top
             self._gemm(N, C, C, _ptr(dzb), (1, N, 0), _ptr(pb, o["W%d" % l]), (C, 1, 0), _ptr(dv), (1, N, 0))
@@ -441,12 +446,14 @@ def main(argv=None):
     ap.add_argument("--n", type=int, default=256)
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
-    ap.add_argument("--engine", choices=["tensor", "cuda"], default="tensor")
+    ap.add_argument("--engine", choices=["tensor", "staged", "cuda"], default="tensor",
+                    help="tensor: TMA pipeline where both operands are K-major, else the staged kernel; "
+                         "staged: the staged tcgen05 kernel for every product; cuda: CUDA cores")
     ap.add_argument("--max-splits", type=int, default=1024, help="split-K count cap of the weight gradients")
     args = ap.parse_args(argv)
     dev = torch.device("cuda", torch.cuda.current_device())
-    net = FNO2d(device=dev, engine=ENGINE_TENSOR_CORES if args.engine == "tensor" else ENGINE_CUDA_CORES,
-                max_splits=args.max_splits)
+    engine = {"tensor": ENGINE_TENSOR_CORES, "staged": ENGINE_STAGED, "cuda": ENGINE_CUDA_CORES}[args.engine]
+    net = FNO2d(device=dev, engine=engine, max_splits=args.max_splits)
     rng = np.random.default_rng(0)
     re = np.exp(rng.uniform(math.log(RE_RANGE[0]), math.log(RE_RANGE[1]), args.batch))
     a = net.inputs(re, rng.uniform(*U_RANGE, args.batch), args.n, args.n)

@@ -23,7 +23,7 @@ def gemm(A, B, C, alpha=1.0, beta=0.0, engine=0, batch=1, a_bs=0, b_bs=0, c_bs=0
                                    (512, 24, 24), (300, 64, 33), (2048, 32, 8), (256, 200, 16),
                                    (32, 32, 1600), (40, 4, 1000), (160, 32, 704)])
 @pytest.mark.parametrize("layout", ["nn", "nt", "tn", "tt"])
-@pytest.mark.parametrize("engine", [1, 2])
+@pytest.mark.parametrize("engine", [0, 1, 2])
 def test_gemm_matches_float64(cuda, m, n, k, layout, engine):
     g = torch.Generator(device="cpu").manual_seed(m * 7 + n + k)
     a = torch.randn(m, k, generator=g).to(torch.bfloat16)
@@ -84,3 +84,66 @@ def test_gemm_empty_inner_dimension(cuda, engine):
               1.0, 0.5, 0, engine, torch.cuda.current_stream().cuda_stream)
     _lib.call("lbgb_gemm_status", 1)
     assert torch.all(C == 1.5)
+
+
+def _call(m, n, k, A, a, B, b, C, c, batch, alpha, beta, engine):
+    _lib.call("lbgb_gemm_bf16", m, n, k, A.data_ptr(), a[0], a[1], a[2], B.data_ptr(), b[0], b[1], b[2], C.data_ptr(),
+              c[0], c[1], c[2], batch, alpha, beta, int(C.dtype == torch.bfloat16), engine,
+              torch.cuda.current_stream().cuda_stream)
+
+
+@pytest.mark.parametrize("m,n,k,batch,shared_b", [(128, 32, 64, 1, False), (1000, 24, 256, 1, False),
+                                                  (130, 130, 72, 1, False), (4096, 128, 24, 1, False),
+                                                  (300, 64, 40, 3, False), (256, 48, 256, 4, True),
+                                                  (33, 7, 8, 1, False), (640, 256, 24, 2, True),
+                                                  (129, 96, 1032, 2, False)])
+@pytest.mark.parametrize("out", ["f32_rows", "f32_cols", "bf16_rows"])
+def test_tma_pipeline_k_major(cuda, m, n, k, batch, shared_b, out):
+    """The TMA + warp-specialised tcgen05 kernel (engine 3: A and B both
+    K-major): ragged M, N and K tails, batched problems with their own or a
+    shared B, FP32 output in either layout and BF16 output, alpha and beta,
+    against a float64 product of the same BF16 operands."""
+    g = torch.Generator(device="cpu").manual_seed(m + 3 * n + 7 * k + batch)
+    a = torch.randn(batch, m, k, generator=g).to(torch.bfloat16)
+    bt = torch.randn(1 if shared_b else batch, n, k, generator=g).to(torch.bfloat16)  # B(k, n) = bt[n, k]
+    ref = torch.einsum("zmk,znk->zmn", a.double(), bt.double().expand(batch, n, k))
+    A, Bt = a.to(cuda), bt.to(cuda)
+    dt = torch.bfloat16 if out == "bf16_rows" else torch.float32
+    if out == "f32_cols":
+        Cs = torch.full((batch, n, m), 2.0, device=cuda)
+        C, c = Cs, (1, m, m * n)
+    else:
+        C = torch.full((batch, m, n), 2.0, device=cuda, dtype=dt)
+        c = (n, 1, m * n)
+    _call(m, n, k, A, (k, 1, m * k), Bt, (1, k, 0 if shared_b else n * k), C, c, batch, 0.5, 0.25, 3)
+    _lib.call("lbgb_gemm_status", 1)
+    got = C.double().cpu()
+    if out == "f32_cols":
+        got = got.transpose(1, 2)
+    want = 0.5 * ref + 0.25 * 2.0
+    tol = (1e-2 if dt == torch.bfloat16 else 1e-4) * max(1.0, want.abs().max().item())
+    assert (got - want).abs().max().item() <= tol
+
+
+def test_tma_pipeline_split_k_strides(cuda):
+    """The weight-gradient pattern: one long K split into batched chunks whose
+    batch stride (the chunk) is smaller than the row stride (all of K)."""
+    M, N, K, S = 32, 32, 8192, 8
+    ks = K // S
+    g = torch.Generator(device="cpu").manual_seed(11)
+    a = torch.randn(M, K, generator=g).to(torch.bfloat16)
+    bt = torch.randn(N, K, generator=g).to(torch.bfloat16)
+    parts = torch.zeros(S, M, N, device=cuda)
+    _call(M, N, ks, a.to(cuda), (K, 1, ks), bt.to(cuda), (1, K, ks), parts, (N, 1, M * N), S, 1.0, 0.0, 0)
+    _lib.call("lbgb_gemm_status", 1)
+    ref = torch.stack([a[:, i * ks:(i + 1) * ks].double() @ bt[:, i * ks:(i + 1) * ks].double().t()
+                       for i in range(S)])
+    assert (parts.double().cpu() - ref).abs().max().item() <= 1e-4 * ref.abs().max().item()
+
+
+def test_tma_engine_rejects_other_layouts(cuda):
+    A = torch.zeros(64, 16, dtype=torch.bfloat16, device=cuda)
+    B = torch.zeros(16, 32, dtype=torch.bfloat16, device=cuda)
+    C = torch.zeros(64, 32, device=cuda)
+    with pytest.raises(ValueError):  # B is N-major here
+        _call(64, 32, 16, A, (16, 1, 0), B, (32, 1, 0), C, (32, 1, 0), 1, 1.0, 0.0, 3)
