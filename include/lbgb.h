@@ -310,8 +310,8 @@ LBGB_API int lbgb_chapman_enskog(const void *rho, const void *ux, const void *uy
  * any transposed or strided view works.  engine: 0 tensor cores, choosing
  * the TMA pipeline (cp.async.bulk.tensor operand loads, warp-specialised
  * producer / MMA / epilogue, double-buffered tensor-memory accumulator,
- * persistent CTAs) when A and B are both K-major (x_cs = 1 for A, x_rs = 1
- * for B) and their rows are 16-byte aligned, else the
+ * persistent CTAs) when B is K-major (b_rs = 1), A is K-major (a_cs = 1) or
+ * M-major (a_rs = 1), and their rows are 16-byte aligned, else the
  * staged kernel; 2 the staged tcgen05 kernel only (operands copied into
  * shared memory by the threads); 3 the TMA pipeline only (LBGB_EINVAL for
  * other layouts); 1 CUDA-core reference.  Used by the Fourier-neural-operator

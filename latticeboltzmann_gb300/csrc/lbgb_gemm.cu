@@ -429,10 +429,12 @@ static int tc_dyn_smem() {
 }
 
 // ---------------------------------------------------------------- TMA pipeline
-// Persistent, warp-specialised GEMM for products whose A and B are both
-// K-major (k contiguous: A(r, k) = A[r * a_rs + k], B(k, n) = B[n * b_cs + k]),
-// rows 16-byte aligned -- the forward W and H transforms, the inverse W
-// transform and the split-K weight gradients of the surrogate.
+// Persistent, warp-specialised GEMM for products whose B is K-major
+// (B(k, n) = B[n * b_cs + k]) and whose A is K-major (A(r, k) = A[r * a_rs + k])
+// or M-major (A(r, k) = A[k * a_cs + r]), rows 16-byte aligned -- the
+// forward W and H transforms, the inverse W transform, the split-K weight
+// gradients and the forward pointwise layers and projections of the
+// surrogate.
 //
 //  * warp 0, one thread: TMA producer.  Per 64-deep K block it issues one
 //    cp.async.bulk.tensor load of A (128 rows x 64 k) and one of B (NT rows
@@ -498,7 +500,13 @@ __device__ __forceinline__ void tc_ld16(uint32_t taddr, uint32_t (&v)[16]) {
     asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 }
 
-template <int NT, typename OUT>
+// AMN: A is M-major (m contiguous, A(m, k) = A[k * a_cs + m]; the
+// channel-major activations of the pointwise layers).  Its tile is then two
+// 64-element-wide boxes per K block (m0 and m0 + 64), each 64 k rows of 128
+// bytes with the 128-byte swizzle: the MN-major SWIZZLE_128B layout, 8-row
+// K groups 1024 bytes apart, the two 64-element M chunks 8192 bytes apart;
+// an MMA of K = 16 starts 2048 bytes further.
+template <int NT, typename OUT, bool AMN = false>
 __global__ void __launch_bounds__(TP_THREADS, 2)
 k_gemm_tma(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB, int a3d, int b3d, int M,
            int N, int K, int batch, OUT *__restrict__ C, long long c_rs, long long c_cs, long long c_bs, float alpha,
@@ -555,7 +563,12 @@ k_gemm_tma(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUte
                     }
                     mbar_expect_tx_g(&full[s], (uint32_t)S::STAGE);
                     unsigned char *sa = dsm + (size_t)s * S::STAGE, *sb = sa + S::A_BYTES;
-                    tma_load_box(sa, &tmA, a3d != 0, kb * TP_KB, mt * TC_M, z, &full[s]);
+                    if constexpr (AMN) {
+                        tma_load_box(sa, &tmA, a3d != 0, mt * TC_M, kb * TP_KB, z, &full[s]);
+                        tma_load_box(sa + S::A_BYTES / 2, &tmA, a3d != 0, mt * TC_M + 64, kb * TP_KB, z, &full[s]);
+                    } else {
+                        tma_load_box(sa, &tmA, a3d != 0, kb * TP_KB, mt * TC_M, z, &full[s]);
+                    }
                     tma_load_box(sb, &tmB, b3d != 0, kb * TP_KB, nt * NT, z, &full[s]);
                 }
             }
@@ -565,7 +578,7 @@ k_gemm_tma(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUte
         }
     } else if (warp == 1) {
         if (lane == 0) {
-            constexpr uint32_t idesc = umma_idesc_bf16(TC_M, NT);
+            constexpr uint32_t idesc = umma_idesc_bf16(TC_M, NT) | (AMN ? (1u << 15) : 0u);  // bit 15: A MN-major
             long long it = 0;
             int tc = 0;
             bool ok = true;
@@ -593,7 +606,8 @@ k_gemm_tma(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUte
 #pragma unroll
                     for (int kk = 0; kk < TP_KB / 16; ++kk) {
                         // K = 16 = 32 bytes of each 128-byte swizzled row; 8-row atoms 1024 bytes apart
-                        const uint64_t da = umma_desc(sa + kk * 32, 16, 1024, 2);
+                        const uint64_t da = AMN ? umma_desc(sa + kk * 2048, S::A_BYTES / 2, 1024, 2)
+                                                : umma_desc(sa + kk * 32, 16, 1024, 2);
                         const uint64_t db = umma_desc(sb + kk * 32, 16, 1024, 2);
                         const uint32_t acc = (kb > 0 || kk > 0) ? 1u : 0u;
                         asm volatile(
@@ -733,36 +747,63 @@ static bool kmajor_map(CUtensorMap *map, const __nv_bfloat16 *X, long long rows,
     return r == CUDA_SUCCESS;
 }
 
-// Launches the TMA pipeline if A and B are K-major and TMA can address them;
-// returns 1 (nothing launched) when it cannot, so the caller falls back.
+// Tensor map of an M-major BF16 operand: element (m, k) at X[k * ks + m],
+// problem z at X + z * bs; box: 64 m (128 bytes, 128-byte swizzle) x 64 k.
+static bool mmajor_map(CUtensorMap *map, const __nv_bfloat16 *X, long long m, long long k, long long ks, int batch,
+                       long long bs, int *three_d) {
+    EncodeTiledFn enc = encode_tiled();
+    if (!enc || !aligned(X, 16) || ks % 8 || ks <= 0 || bs % 8 || bs < 0 || k <= 0 || m <= 0) return false;
+    const bool use3 = batch > 1 && bs != 0;
+    cuuint64_t dims[3] = {(cuuint64_t)m, (cuuint64_t)k, (cuuint64_t)batch};
+    cuuint64_t strides[2] = {(cuuint64_t)ks * 2, (cuuint64_t)bs * 2};
+    cuuint32_t box[3] = {64, (cuuint32_t)TP_KB, 1};
+    cuuint32_t estr[3] = {1, 1, 1};
+    const CUresult r = enc(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, use3 ? 3 : 2, const_cast<__nv_bfloat16 *>(X), dims,
+                           strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+                           CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    *three_d = use3 ? 1 : 0;
+    return r == CUDA_SUCCESS;
+}
+
+// Launches the TMA pipeline if B is K-major, A K-major or M-major, and TMA
+// can address them; returns 1 (nothing launched) when it cannot, so the
+// caller falls back.
 template <int NT, typename OUT>
-static int launch_gemm_tma_nt(int m, int n, int k, const __nv_bfloat16 *a, long long a_rs, long long a_bs,
-                              const __nv_bfloat16 *b, long long b_cs, long long b_bs, OUT *C, long long c_rs,
-                              long long c_cs, long long c_bs, int batch, float alpha, float beta, cudaStream_t s) {
+static int launch_gemm_tma_nt(int m, int n, int k, const __nv_bfloat16 *a, long long a_rs, long long a_cs,
+                              long long a_bs, const __nv_bfloat16 *b, long long b_cs, long long b_bs, OUT *C,
+                              long long c_rs, long long c_cs, long long c_bs, int batch, float alpha, float beta,
+                              cudaStream_t s) {
     using S = TmaShape<NT>;
     CUtensorMap ma, mb;
     int a3 = 0, b3 = 0;
-    if (!kmajor_map(&ma, a, m, k, a_rs, batch, a_bs, TC_M, &a3) || !kmajor_map(&mb, b, n, k, b_cs, batch, b_bs, NT, &b3))
+    const bool amn = a_cs != 1;  // the caller passes a_cs == 1 (K-major) or a_rs == 1 (M-major)
+    if (!(amn ? mmajor_map(&ma, a, m, k, a_cs, batch, a_bs, &a3) : kmajor_map(&ma, a, m, k, a_rs, batch, a_bs, TC_M, &a3)) ||
+        !kmajor_map(&mb, b, n, k, b_cs, batch, b_bs, NT, &b3))
         return 1;
-    static std::atomic<bool> attr[MAX_DEVICES];
+    static std::atomic<bool> attr[MAX_DEVICES][2];
     const int dev = current_device();
-    if (!attr[dev].load(std::memory_order_acquire)) {
+    if (!attr[dev][amn].load(std::memory_order_acquire)) {
         std::lock_guard<std::mutex> lock(setup_mutex());
         const cudaError_t e =
-            cudaFuncSetAttribute(k_gemm_tma<NT, OUT>, cudaFuncAttributeMaxDynamicSharedMemorySize, S::SMEM);
+            amn ? cudaFuncSetAttribute(k_gemm_tma<NT, OUT, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, S::SMEM)
+                : cudaFuncSetAttribute(k_gemm_tma<NT, OUT, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, S::SMEM);
         if (e != cudaSuccess) {
             set_error("k_gemm_tma: cannot reserve %d bytes of shared memory: %s", S::SMEM, cudaGetErrorString(e));
             return LBGB_ECUDA;
         }
-        attr[dev].store(true, std::memory_order_release);
+        attr[dev][amn].store(true, std::memory_order_release);
     }
     int sms = 0;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     const long long tiles = (long long)((m + TC_M - 1) / TC_M) * ((n + NT - 1) / NT) * batch;
     const long long slots = 2ll * (sms > 0 ? sms : 1);
     const int grid = (int)(tiles < slots ? tiles : slots);
-    k_gemm_tma<NT, OUT><<<grid, TP_THREADS, S::SMEM, s>>>(ma, mb, a3, b3, m, n, k, batch, C, c_rs, c_cs, c_bs, alpha,
-                                                          beta);
+    if (amn)
+        k_gemm_tma<NT, OUT, true><<<grid, TP_THREADS, S::SMEM, s>>>(ma, mb, a3, b3, m, n, k, batch, C, c_rs, c_cs, c_bs,
+                                                                    alpha, beta);
+    else
+        k_gemm_tma<NT, OUT, false><<<grid, TP_THREADS, S::SMEM, s>>>(ma, mb, a3, b3, m, n, k, batch, C, c_rs, c_cs,
+                                                                     c_bs, alpha, beta);
     return check_launch("k_gemm_tma");
 }
 
@@ -771,12 +812,20 @@ static int launch_gemm_tma(int m, int n, int k, const __nv_bfloat16 *a, long lon
                            const __nv_bfloat16 *b, long long b_rs, long long b_cs, long long b_bs, OUT *C,
                            long long c_rs, long long c_cs, long long c_bs, int batch, float alpha, float beta,
                            cudaStream_t s) {
-    if (a_cs != 1 || b_rs != 1 || k <= 0) return 1;
-    if (n <= 32) return launch_gemm_tma_nt<32>(m, n, k, a, a_rs, a_bs, b, b_cs, b_bs, C, c_rs, c_cs, c_bs, batch, alpha,
-                                               beta, s);
-    if (n <= 64) return launch_gemm_tma_nt<64>(m, n, k, a, a_rs, a_bs, b, b_cs, b_bs, C, c_rs, c_cs, c_bs, batch, alpha,
-                                               beta, s);
-    return launch_gemm_tma_nt<128>(m, n, k, a, a_rs, a_bs, b, b_cs, b_bs, C, c_rs, c_cs, c_bs, batch, alpha, beta, s);
+    if ((a_cs != 1 && a_rs != 1) || b_rs != 1 || k <= 0) return 1;
+    // M-major A with more than 64 output columns stays on the staged kernel:
+    // there the output (the 128-channel projection: 512 MB per pass) is what
+    // takes the time, and 8192 staged CTAs drain it faster than the
+    // persistent kernel's two CTAs per SM (measured 119 against 192 us)
+    if (a_cs != 1 && n > 64) return 1;
+    if (n <= 32)
+        return launch_gemm_tma_nt<32>(m, n, k, a, a_rs, a_cs, a_bs, b, b_cs, b_bs, C, c_rs, c_cs, c_bs, batch, alpha,
+                                      beta, s);
+    if (n <= 64)
+        return launch_gemm_tma_nt<64>(m, n, k, a, a_rs, a_cs, a_bs, b, b_cs, b_bs, C, c_rs, c_cs, c_bs, batch, alpha,
+                                      beta, s);
+    return launch_gemm_tma_nt<128>(m, n, k, a, a_rs, a_cs, a_bs, b, b_cs, b_bs, C, c_rs, c_cs, c_bs, batch, alpha,
+                                   beta, s);
 }
 
 template <typename OUT>
@@ -791,7 +840,7 @@ static int launch_gemm(int m, int n, int k, const __nv_bfloat16 *a, long long a_
                              : 1;
         if (rc <= 0) return rc;
         if (engine == 3) {
-            set_error("lbgb_gemm_bf16: engine 3 needs K-major A and B with 16-byte aligned rows");
+            set_error("lbgb_gemm_bf16: engine 3 needs a K-major B, a K- or M-major A and 16-byte aligned rows");
             return LBGB_EINVAL;
         }
     }

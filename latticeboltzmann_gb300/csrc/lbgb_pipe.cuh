@@ -61,6 +61,10 @@ __device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity, long l
         if (mbar_try_wait(bar, parity)) return true;
     return false;
 }
+// Requests the line of p into L1 without waiting for it.
+__device__ __forceinline__ void prefetch_l1(const void *p) {
+    asm volatile("prefetch.global.L1 [%0];" ::"l"(p));
+}
 // Bulk asynchronous copy global -> shared, completion counted on `bar`.
 __device__ __forceinline__ void bulk_copy_g2s(void *dst, const void *src, uint32_t bytes, uint64_t *bar) {
     asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
@@ -183,16 +187,76 @@ k_step_pipe(const typename Codec<DT>::raw *__restrict__ src, typename Codec<DT>:
 
     // ---------------------------------------------------------------- consumers
     const int t = threadIdx.x;  // 0 .. NCW*32-1
+    // tile -> (row, tile within the row), advanced without a division per tile
+    const int dq = gridDim.x / tiles_per_row, dr = gridDim.x - dq * tiles_per_row;
+    int kr = blockIdx.x / tiles_per_row, lt = blockIdx.x - kr * tiles_per_row;
+    // The threads at a row's first and last column read a few values from
+    // global memory after the stage wait (wrap-around, walls, the lid
+    // density).  Their addresses are prefetched into L1 one tile ahead, so
+    // that those warps do not wait a DRAM round trip while holding a stage.
+    // (16-bit storage: not done -- those kernels are issue-bound, and the
+    // per-tile instructions cost more than the stalls they save: -4 %)
+    auto prefetch_edges = [&](int tl, int krow, int ltile) {
+        if constexpr (sizeof(raw) == 2) return;
+        if (tl >= total_tiles) return;
+        const int kk = k_first + krow;
+        const int cc = ltile * L + t * NC;
+        const bool first = cc == 0, last = cc + NC == ny;
+        if (!first && !last) return;
+        auto pf = [&](int ch, int row, int l) { prefetch_l1(src + (size_t)ch * cs + (size_t)row * ny + l); };
+        if (BC == LBGB_PERIODIC) {
+            const int km = kk == 0 ? nx - 1 : kk - 1, kp = kk == nx - 1 ? 0 : kk + 1;
+            if (first) {
+                pf(CN, kk, ny - 1);
+                pf(CNE, km, ny - 1);
+                pf(CNW, kp, ny - 1);
+            }
+            if (last) {
+                pf(CS, kk, 0);
+                pf(CSW, kp, 0);
+                pf(CSE, km, 0);
+            }
+        } else {
+            if (first) {
+                pf(CS, kk, 0);
+                pf(CSW, kk, 0);
+                pf(CSE, kk, 0);
+            }
+            if (last) {
+                const int T = ny - 1;
+                pf(CN, kk, T);
+                pf(CNW, kk, T);
+                pf(CNE, kk, T);
+                if (BC == LBGB_CAVITY) {
+                    const int kw = kk == 0 ? nx - 1 : kk - 1, ke = kk == nx - 1 ? 0 : kk + 1;
+                    pf(CNW, ke, T - 1);
+                    pf(CN, kk, T - 1);
+                    pf(CNE, kw, T - 1);
+                    pf(CW, ke, T);
+                    pf(C0, kk, T);
+                    pf(CE, kw, T);
+                }
+            }
+        }
+    };
+    prefetch_edges(blockIdx.x, kr, lt);
     int it = 0;
     for (int tile = blockIdx.x; tile < total_tiles; tile += gridDim.x, ++it) {
+        const int k = k_first + kr;
+        const int l0 = lt * L;
+        lt += dr;
+        kr += dq;
+        if (lt >= tiles_per_row) {
+            lt -= tiles_per_row;
+            ++kr;
+        }
+        prefetch_edges(tile + gridDim.x, kr, lt);
         const int s = it % stages;
         const uint32_t ph = (uint32_t)(it / stages) & 1u;
         if (!mbar_wait(&full[s], ph, wait_limit)) {
             pipe_report(2);
             break;
         }
-        const int k = k_first + tile / tiles_per_row;
-        const int l0 = (tile - (k - k_first) * tiles_per_row) * L;
         const int c = l0 + t * NC;  // first cell of this thread
         const bool act = c < ny;
         const raw *stage = slots + (size_t)s * 9 * SLOT;

@@ -272,6 +272,7 @@ def main(argv=None):
     ap.add_argument("--weighting", choices=["relative", "uniform"], default="relative",
                     help="loss weights per (channel, sample): same relative accuracy for every sample, or one MSE")
     ap.add_argument("--rho-weight", type=float, default=2.0, help="extra weight of the density channel")
+    ap.add_argument("--init", default=None, help="start the training from these weights (.npz) instead of at random")
     ap.add_argument("--batch", type=int, default=16)
     ap.add_argument("--lr", type=float, default=1e-3)
     ap.add_argument("--max-steps", type=int, default=600_000)
@@ -308,7 +309,7 @@ def main(argv=None):
     rng = np.random.default_rng(args.seed + 1)
     perm = rng.permutation(ok)
     val, tr = perm[:args.held_out], perm[args.held_out:]
-    net = FNO2d(device=dev, seed=args.seed)
+    net = FNO2d.load(args.init, device=dev) if args.init else FNO2d(device=dev, seed=args.seed)
     t1 = time.perf_counter()
     hist = train(net, data, tr, epochs=args.epochs, batch=args.batch, lr=args.lr, log=log, val_idx=val,
                  seconds=args.train_seconds, weighting=args.weighting, rho_weight=args.rho_weight)
@@ -321,7 +322,9 @@ def main(argv=None):
         "held_out_re": data["re"][val].tolist(), "held_out_u": data["u"][val].tolist(),
         "held_out_cold_steps": data["steps"][val].tolist(), "epochs": int(hist[-1][0]) + 1 if hist else 0,
         "train_s": t_train, "weighting": args.weighting, "rho_weight": args.rho_weight,
-        "val_rel_l2_u": vu, "val_rel_l2_rho": vr})
+        "val_rel_l2_u": vu, "val_rel_l2_rho": vr,
+        "init_epochs": int((getattr(net, "meta", None) or {}).get("epochs", 0)) if args.init else 0,
+        "init_train_s": float((getattr(net, "meta", None) or {}).get("train_s", 0.0)) if args.init else 0.0})
     log("training: %.1f s, val rel-L2 u %.3e rho-1 %.3e" % (t_train, vu, vr))
     res = {"samples": args.samples, "n": args.n, "steady": int(len(ok)), "data_wall_s": data["wall"],
            "data_steps": data["steps"].tolist(), "data_re": data["re"].tolist(), "data_u": data["u"].tolist(),

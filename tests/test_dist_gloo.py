@@ -50,6 +50,51 @@ def test_replica_aggregation_two_ranks():
         assert abs(mlups - expected) < 1e-12
 
 
+def _lattice_worker(rank, world, port, results):
+    """Each rank steps its own replica (the oracle's C port stands in for the
+    GPU step on a CPU-only host), times it, and the ranks aggregate."""
+    os.environ.update({"MASTER_ADDR": "127.0.0.1", "MASTER_PORT": str(port), "RANK": str(rank),
+                       "WORLD_SIZE": str(world), "LOCAL_RANK": str(rank)})
+    import time
+    import numpy as np
+    import bench
+    from oracle import d2q9
+    from oracle import port as c_port
+    d = bench.Dist(backend="gloo")
+    nx, ny, steps = 48 + 16 * rank, 40, 20  # uneven replicas
+    f = d2q9.equilibrium(np.ones((nx, ny)), np.zeros((nx, ny)), np.zeros((nx, ny)))
+    d.barrier()
+    t0 = time.perf_counter()
+    c_port.cavity_run(f, 1.7, 0.1, steps, nthreads=1)
+    secs = time.perf_counter() - t0
+    mlups, t = bench.aggregate_mlups(nx * ny, steps, secs, d)
+    ref = d2q9.equilibrium(np.ones((nx, ny)), np.zeros((nx, ny)), np.zeros((nx, ny)))
+    for _ in range(steps):
+        d2q9.cavity_step(ref, 1.7, 0.1)
+    results[rank] = (mlups, t, secs, nx * ny, float(np.abs(f - ref).max()))
+    d.close()
+
+
+@pytest.mark.timeout(120)
+def test_replicas_step_their_own_lattices_two_ranks():
+    ctx = mp.get_context("spawn")
+    manager = ctx.Manager()
+    results = manager.dict()
+    port = _free_port()
+    procs = [ctx.Process(target=_lattice_worker, args=(r, 2, port, results)) for r in range(2)]
+    for p in procs:
+        p.start()
+    for p in procs:
+        p.join(90)
+        assert p.exitcode == 0
+    slowest = max(results[r][2] for r in range(2))
+    total = sum(results[r][3] * 20 for r in range(2))
+    for r in range(2):
+        mlups, t, _, _, err = results[r]
+        assert t == slowest and abs(mlups - total / slowest / 1e6) < 1e-9 * mlups
+        assert err < 1e-12  # each replica's lattice is the oracle's
+
+
 def test_single_process_needs_no_process_group(monkeypatch):
     for k in ("WORLD_SIZE", "RANK", "LOCAL_RANK"):
         monkeypatch.delenv(k, raising=False)

@@ -98,11 +98,12 @@ def _call(m, n, k, A, a, B, b, C, c, batch, alpha, beta, engine):
                                                   (33, 7, 8, 1, False), (640, 256, 24, 2, True),
                                                   (129, 96, 1032, 2, False)])
 @pytest.mark.parametrize("out", ["f32_rows", "f32_cols", "bf16_rows"])
-def test_tma_pipeline_k_major(cuda, m, n, k, batch, shared_b, out):
-    """The TMA + warp-specialised tcgen05 kernel (engine 3: A and B both
-    K-major): ragged M, N and K tails, batched problems with their own or a
-    shared B, FP32 output in either layout and BF16 output, alpha and beta,
-    against a float64 product of the same BF16 operands."""
+@pytest.mark.parametrize("a_major", ["k", "m"])
+def test_tma_pipeline_k_major(cuda, m, n, k, batch, shared_b, out, a_major):
+    """The TMA + warp-specialised tcgen05 kernel (engine 3: B K-major, A
+    K-major or M-major): ragged M, N and K tails, batched problems with their
+    own or a shared B, FP32 output in either layout and BF16 output, alpha
+    and beta, against a float64 product of the same BF16 operands."""
     g = torch.Generator(device="cpu").manual_seed(m + 3 * n + 7 * k + batch)
     a = torch.randn(batch, m, k, generator=g).to(torch.bfloat16)
     bt = torch.randn(1 if shared_b else batch, n, k, generator=g).to(torch.bfloat16)  # B(k, n) = bt[n, k]
@@ -115,7 +116,13 @@ def test_tma_pipeline_k_major(cuda, m, n, k, batch, shared_b, out):
     else:
         C = torch.full((batch, m, n), 2.0, device=cuda, dtype=dt)
         c = (n, 1, m * n)
-    _call(m, n, k, A, (k, 1, m * k), Bt, (1, k, 0 if shared_b else n * k), C, c, batch, 0.5, 0.25, 3)
+    if a_major == "k":
+        _call(m, n, k, A, (k, 1, m * k), Bt, (1, k, 0 if shared_b else n * k), C, c, batch, 0.5, 0.25, 3)
+    else:
+        if m % 8:
+            pytest.skip("M-major rows need m a multiple of 8 (16-byte aligned)")
+        At = a.transpose(1, 2).contiguous().to(cuda)  # (batch, k, m): A(m, k) = At[k, m]
+        _call(m, n, k, At, (1, m, m * k), Bt, (1, k, 0 if shared_b else n * k), C, c, batch, 0.5, 0.25, 3)
     _lib.call("lbgb_gemm_status", 1)
     got = C.double().cpu()
     if out == "f32_cols":
