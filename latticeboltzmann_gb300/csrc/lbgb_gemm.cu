@@ -811,13 +811,13 @@ template <typename OUT>
 static int launch_gemm_tma(int m, int n, int k, const __nv_bfloat16 *a, long long a_rs, long long a_cs, long long a_bs,
                            const __nv_bfloat16 *b, long long b_rs, long long b_cs, long long b_bs, OUT *C,
                            long long c_rs, long long c_cs, long long c_bs, int batch, float alpha, float beta,
-                           cudaStream_t s) {
+                           bool forced, cudaStream_t s) {
     if ((a_cs != 1 && a_rs != 1) || b_rs != 1 || k <= 0) return 1;
-    // M-major A with more than 64 output columns stays on the staged kernel:
-    // there the output (the 128-channel projection: 512 MB per pass) is what
-    // takes the time, and 8192 staged CTAs drain it faster than the
-    // persistent kernel's two CTAs per SM (measured 119 against 192 us)
-    if (a_cs != 1 && n > 64) return 1;
+    // automatic choice: M-major A with more than 64 output columns stays on
+    // the staged kernel -- there the output (the 128-channel projection:
+    // 512 MB per pass) is what takes the time, and 8192 staged CTAs drain it
+    // faster than the persistent kernel's two CTAs per SM (119 against 192 us)
+    if (!forced && a_cs != 1 && n > 64) return 1;
     if (n <= 32)
         return launch_gemm_tma_nt<32>(m, n, k, a, a_rs, a_cs, a_bs, b, b_cs, b_bs, C, c_rs, c_cs, c_bs, batch, alpha,
                                       beta, s);
@@ -836,7 +836,7 @@ static int launch_gemm(int m, int n, int k, const __nv_bfloat16 *a, long long a_
     if (engine == 0 || engine == 3) {
         // both operands K-major: the TMA pipeline (engine 3 insists on it)
         const int rc = k > 0 ? launch_gemm_tma(m, n, k, a, a_rs, a_cs, a_bs, b, b_rs, b_cs, b_bs, C, c_rs, c_cs, c_bs,
-                                               batch, alpha, beta, s)
+                                               batch, alpha, beta, engine == 3, s)
                              : 1;
         if (rc <= 0) return rc;
         if (engine == 3) {

@@ -71,7 +71,7 @@ def generate(n_samples, n=256, seed=0, device=None, log=None, max_steps=600_000,
     return {"re": re, "u": u, "fields": fields, "steps": steps, "wall": wall, "info": info}
 
 
-def sample_weights(t_all, idx, rho_weight=1.0, max_ratio=100.0):
+def sample_weights(t_all, idx, rho_weight=1.0, max_ratio=100.0, re=None, re_exp=0.0):
     """Loss weight of every (channel, sample) plane of the normalised targets
     t_all (3, S, n, n): the inverse of the plane's mean square, so that each
     sample's fields are fit to the same relative accuracy (the density
@@ -79,7 +79,10 @@ def sample_weights(t_all, idx, rho_weight=1.0, max_ratio=100.0):
     with one weight for all samples the high-Re pressure -- the slowest part
     of those runs to settle -- would hardly count), capped at max_ratio times
     the smallest weight of the channel, scaled to mean 1 over ``idx`` and
-    multiplied by (rho_weight, 1, 1)."""
+    multiplied by (rho_weight, 1, 1).  re_exp > 0: each sample's weights are
+    further multiplied by (Re / min Re)^re_exp, scaled to mean 1 over idx --
+    the steps to steady grow like Re^0.6, so high-Re accuracy buys the most
+    wall time."""
     ms = t_all.pow(2).mean(dim=(2, 3)).double()  # (3, S)
     w = 1.0 / ms.clamp_min(1e-30)
     sel = torch.as_tensor(np.asarray(idx), device=w.device)
@@ -88,18 +91,23 @@ def sample_weights(t_all, idx, rho_weight=1.0, max_ratio=100.0):
         w[c] = torch.minimum(w[c], lo * max_ratio)
         w[c] = w[c] / w[c].index_select(0, sel).mean()
     w[0] *= rho_weight
+    if re is not None and re_exp:
+        r = torch.as_tensor(np.asarray(re, dtype=np.float64), device=w.device)
+        g = (r / r.index_select(0, sel).min()) ** re_exp
+        w *= (g / g.index_select(0, sel).mean())[None, :]
     return w.float()
 
 
 def train(net, data, idx, epochs=100, batch=16, lr=1e-3, lr_min=1e-5, log=None, seed=0, val_idx=None,
-          seconds=None, weighting="relative", rho_weight=2.0):
+          seconds=None, weighting="relative", rho_weight=2.0, re_exp=0.0):
     """Adam on the samples ``idx`` of ``data`` (cosine schedule from lr to lr_min).
 
     weighting: "relative" (each (channel, sample) plane weighted to the same
     relative accuracy, the density channel by rho_weight; sample_weights) or
     "uniform" (one mean squared error over all planes).  seconds: a wall-time
-    budget; after the first epoch the epoch count is set to what fits it (at
-    most ``epochs``) and the schedule spans those.  Returns the history of
+    budget; after the third epoch the epoch count is set to what fits it (at
+    most ``epochs``; the time of epochs 1-2 is the estimate, epoch 0 includes
+    one-time set-up) and the schedule spans those.  Returns the history of
     (epoch, mean train loss, validation rel-L2 of u, of rho - 1)."""
     device = net.device
     fields = data["fields"]
@@ -109,13 +117,14 @@ def train(net, data, idx, epochs=100, batch=16, lr=1e-3, lr_min=1e-5, log=None, 
     net.out_scale = scale.cpu().numpy()
     t_all = targets / scale[:, None, None, None]
     a_all = net.inputs(data["re"], data["u"], n, n)
-    w_all = sample_weights(t_all, idx, rho_weight) if weighting == "relative" else None
+    w_all = sample_weights(t_all, idx, rho_weight, re=data["re"], re_exp=re_exp) if weighting == "relative" else None
     rng = np.random.default_rng(seed)
     steps_per_epoch = max(1, len(idx) // batch)
     total = epochs * steps_per_epoch
     hist = []
     k = 0
     t_start = time.perf_counter()
+    t_ep1 = None
     ep = 0
     while ep < epochs:
         perm = rng.permutation(idx)
@@ -131,8 +140,11 @@ def train(net, data, idx, epochs=100, batch=16, lr=1e-3, lr_min=1e-5, log=None, 
             k += 1
         if seconds is not None and ep == 0:
             torch.cuda.synchronize(device)
-            per_epoch = time.perf_counter() - t_start
-            epochs = max(1, min(epochs, int(seconds / per_epoch)))
+            t_ep1 = time.perf_counter()
+        if seconds is not None and ep == 2:
+            torch.cuda.synchronize(device)
+            per_epoch = (time.perf_counter() - t_ep1) / 2
+            epochs = max(3, min(epochs, int((seconds - (t_ep1 - t_start)) / per_epoch)))
             total = epochs * steps_per_epoch
             if log is not None:
                 log("training: %.2f s per epoch, %d epochs in the %.0f s budget" % (per_epoch, epochs, seconds))
@@ -273,6 +285,8 @@ def main(argv=None):
                     help="loss weights per (channel, sample): same relative accuracy for every sample, or one MSE")
     ap.add_argument("--rho-weight", type=float, default=2.0, help="extra weight of the density channel")
     ap.add_argument("--init", default=None, help="start the training from these weights (.npz) instead of at random")
+    ap.add_argument("--re-exp", type=float, default=0.0,
+                    help="sample loss weights times (Re / Re_min)^re_exp (0: off)")
     ap.add_argument("--batch", type=int, default=16)
     ap.add_argument("--lr", type=float, default=1e-3)
     ap.add_argument("--max-steps", type=int, default=600_000)
@@ -312,7 +326,8 @@ def main(argv=None):
     net = FNO2d.load(args.init, device=dev) if args.init else FNO2d(device=dev, seed=args.seed)
     t1 = time.perf_counter()
     hist = train(net, data, tr, epochs=args.epochs, batch=args.batch, lr=args.lr, log=log, val_idx=val,
-                 seconds=args.train_seconds, weighting=args.weighting, rho_weight=args.rho_weight)
+                 seconds=args.train_seconds, weighting=args.weighting, rho_weight=args.rho_weight,
+                 re_exp=args.re_exp)
     torch.cuda.synchronize()
     t_train = time.perf_counter() - t1
     net.save(os.path.join(args.out, "fno.npz"))
@@ -321,7 +336,7 @@ def main(argv=None):
         "n": args.n, "samples": args.samples, "seed": args.seed, "steady": int(len(ok)),
         "held_out_re": data["re"][val].tolist(), "held_out_u": data["u"][val].tolist(),
         "held_out_cold_steps": data["steps"][val].tolist(), "epochs": int(hist[-1][0]) + 1 if hist else 0,
-        "train_s": t_train, "weighting": args.weighting, "rho_weight": args.rho_weight,
+        "train_s": t_train, "weighting": args.weighting, "rho_weight": args.rho_weight, "re_exp": args.re_exp,
         "val_rel_l2_u": vu, "val_rel_l2_rho": vr,
         "init_epochs": int((getattr(net, "meta", None) or {}).get("epochs", 0)) if args.init else 0,
         "init_train_s": float((getattr(net, "meta", None) or {}).get("train_s", 0.0)) if args.init else 0.0})
