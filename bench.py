@@ -24,8 +24,8 @@ Lines printed (rank 0, one JSON line):
              fraction and clock record per storage, ratio to FP32, and each
              mode's error against an FP64 run (1024^2, 1000 steps)
   operator_path  MLUPS of the reference's loop body through the drop-in
-             operators (stream_and_bounce_back with its scratch copy, then
-             collide), next to the fused step
+             operators (stream_and_bounce_back in place, then collide),
+             next to the fused step
   warm_start cavity time to steady state (max |du| < 1e-7 per 1000 steps),
              cold from rest against warm from the committed surrogate's
              prediction, for fixed held-out cases at 256^2 and 1024^2: steps,
@@ -596,10 +596,11 @@ def warm_start(args, dev):
 
 def operator_path(args, dev):
     """MLUPS of the reference's loop body through the drop-in operators
-    (cavity_opt2.py:276-277): Streaming.stream_and_bounce_back (out of place
-    into scratch, copied back) then Collision.collide, on the benchmark
-    lattice in FP32.  216 bytes per cell per step (stream 72, copy 72,
-    collide 72) against the fused step's 72."""
+    (cavity_opt2.py:276-277): Streaming.stream_and_bounce_back (in place:
+    edge records, then tiles streamed through shared memory) then
+    Collision.collide, on the benchmark lattice in FP32.  144 algorithmic
+    bytes per cell per step (stream 72, collide 72; the edge records add
+    ~7 more) against the fused step's 72."""
     import torch
     import latticeboltzmann_gb300 as PyLB
     from latticeboltzmann_gb300 import _lib
@@ -631,9 +632,9 @@ def operator_path(args, dev):
     del f
     torch.cuda.empty_cache()
     return {"mlups": round(nx * ny * steps / secs / 1e6, 1), "ms_per_step": round(secs / steps * 1e3, 4),
-            "bytes_per_cell": 216, "frac": round(216 * nx * ny * steps / secs / 1e9 / peak, 4), "steps": steps,
+            "bytes_per_cell": 144, "frac": round(144 * nx * ny * steps / secs / 1e9 / peak, 4), "steps": steps,
             "launches_per_step": 3,
-            "path": "PyLB.Streaming.stream_and_bounce_back (kernel into scratch + copy back) + PyLB.collide, "
+            "path": "PyLB.Streaming.stream_and_bounce_back (in place: k_ip_save + k_ip_stream) + PyLB.collide, "
                     "float32 (%dx%d)" % (nx, ny)}
 
 

@@ -23,6 +23,16 @@
  * LBGB_F32DEV stores h_i as float and collides in deviation form (every
  * rounding is of numbers ~1e-2 instead of ~0.4: about 30x finer than
  * LBGB_F32 at the same 72 bytes per cell and step).
+ *
+ * The fused solvers (lbgb_step*, lbgb_batch_*) collide every storage but
+ * LBGB_F64 in the deviation "pair form": opposite channels enter as
+ * a = h_i - h_j and b = h_i + h_j, the momentum is read from the a's, the
+ * relaxation of the odd (momentum-carrying) part is written so that the
+ * post-collision momentum equals the pre-collision one exactly in exact
+ * arithmetic, and the rest population is written last as the node's mass
+ * minus the moving channels.  With FP32-rounded lattice weights the direct
+ * formula gains a systematic momentum factor (1 + delta) every step; the
+ * pair form does not.
  */
 #ifndef LBGB_H
 #define LBGB_H
@@ -84,11 +94,12 @@ LBGB_API int lbgb_collide(void *f, int64_t n, int64_t chan_stride, int dtype,
                  double omega, void *stream);
 
 /* lbgb_collide with options.  flags = 0: as lbgb_collide.
- * LBGB_COLLIDE_KEEP_MASS: the fused solver's collision instead, whose FP32
- * store writes the rest population last as f_0 + sum_{i>0} (f_i - f_i'), so
- * that each node keeps its mass up to the rounding of that one value (the
- * native float path drifts by ~1e-2 in 500 steps of a 48 x 40 box with
- * resting walls, this one by ~5e-6).  Other bits: LBGB_EINVAL.
+ * LBGB_COLLIDE_KEEP_MASS: the fused solver's collision instead (the pair
+ * form above, on h = f - w for LBGB_F32), whose store writes the rest
+ * population last as f_0 + sum_{i>0} (f_i - f_i'), so that each node keeps
+ * its mass up to the rounding of that one value (the native float path
+ * drifts by ~1e-2 in 500 steps of a 48 x 40 box with resting walls, this
+ * one by ~5e-6).  Other bits: LBGB_EINVAL.
  * Same reference interface as lbgb_collide (c/d2q9.h:121-131); the flag has
  * no counterpart there. */
 #define LBGB_COLLIDE_KEEP_MASS 1
@@ -109,6 +120,24 @@ LBGB_API int lbgb_stream_periodic(const void *src, void *dst, int nx, int ny, in
  *    cavity_opt0.py:155-223 and cavity_opt2.py:109-177). */
 LBGB_API int lbgb_stream_bounce_back(const void *src, void *dst, int nx, int ny,
                             double u0, int dtype, void *stream);
+
+/* The same two streams in place on f (the reference's operators assign the
+ * streamed planes back into their argument).  Two launches: the edge values
+ * of every 16-row x 512-byte tile that a neighbouring tile pulls are saved
+ * into work, then each tile is streamed through shared memory and written
+ * back over itself.  Results equal the out-of-place calls bit for bit; about
+ * 79 bytes per FP32 cell instead of 144 for out-of-place + copy back.
+ * work: a 16-byte aligned device buffer of at least
+ * lbgb_stream_inplace_workspace_bytes(nx, ny, dtype) bytes (0 for an invalid
+ * grid or storage code): 6 / 16 + 6 element size / 512 elements per cell,
+ * 4.7 % of an FP32 lattice (5.2 % FP64); it must not be in use by another call in flight.
+ * Replaces: PyLB.Streaming.stream (PyLB/Streaming.py:33-46) and
+ *   stream_and_bounce_back(f_ikl, u0) (cavity_opt1.py:177-245), in place. */
+LBGB_API size_t lbgb_stream_inplace_workspace_bytes(int nx, int ny, int dtype);
+LBGB_API int lbgb_stream_periodic_inplace(void *f, int nx, int ny, int dtype, void *work,
+                                 size_t work_bytes, void *stream);
+LBGB_API int lbgb_stream_bounce_back_inplace(void *f, int nx, int ny, double u0, int dtype,
+                                    void *work, size_t work_bytes, void *stream);
 
 /* One fused time step: pull streaming (boundary = LBGB_PERIODIC or
  * LBGB_CAVITY with lid velocity u0) followed by BGK collision, src -> dst.

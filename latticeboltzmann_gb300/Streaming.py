@@ -6,11 +6,15 @@ simulators/parallel_lid_drive_cavity/cavity_opt1.py:177-245); it is offered
 here as part of the module, with the same semantics, plus ``bounce_back``
 (resting walls) and ``moving_wall`` (an alias taking the lid velocity).
 
-All calls act in place on a C-contiguous CUDA tensor of shape ``(9, nx, ny)``.
-The kernels stream out of place (pull scheme), so each call goes through a
-scratch tensor from torch's caching allocator and copies back; a time loop
-that owns its buffers should use ``latticeboltzmann_gb300.Lattice`` (fused
-stream + collide, ping-pong buffers, no copy).
+All calls act in place on a C-contiguous CUDA tensor of shape ``(9, nx, ny)``
+through the library's in-place streams: the values that neighbouring tiles
+pull across tile edges are saved into a small workspace (about 5 % of the
+lattice, from torch's caching allocator), then every tile is streamed in
+shared memory and written back over itself -- one read and one write of the
+lattice plus the edges, with results equal to the out-of-place kernels' bit
+for bit.  A time loop that owns its buffers should use
+``latticeboltzmann_gb300.Lattice`` (fused stream + collide, 72 bytes per FP32
+cell and step).
 """
 
 import numpy as np
@@ -26,6 +30,14 @@ c_ic = np.array([[0, 1, 0, -1, 0, 1, -1, -1, 1],
                  [0, 0, 1, 0, -1, 1, 1, -1, -1]]).T
 
 
+def _workspace(f_ikl, nx, ny, code):
+    """Edge-record workspace of one in-place stream, from torch's caching
+    allocator on the tensor's device (stream-ordered: reused only after the
+    call that held it)."""
+    nbytes = int(_lib.load().lbgb_stream_inplace_workspace_bytes(nx, ny, code))
+    return torch.empty(max(nbytes, 16), dtype=torch.uint8, device=f_ikl.device), nbytes
+
+
 def stream(f_ikl):
     """Propagate every channel by one cell with periodic wrap, in place.
 
@@ -35,9 +47,9 @@ def stream(f_ikl):
     code = storage_code(f_ikl, "stream")
     if f_ikl.numel() == 0:
         return None
-    tmp = torch.empty_like(f_ikl)
-    _lib.call("lbgb_stream_periodic", f_ikl.data_ptr(), tmp.data_ptr(), nx, ny, code, stream_handle(f_ikl))
-    f_ikl.copy_(tmp)
+    ws, nbytes = _workspace(f_ikl, nx, ny, code)
+    _lib.call("lbgb_stream_periodic_inplace", f_ikl.data_ptr(), nx, ny, code, ws.data_ptr(), nbytes,
+              stream_handle(f_ikl))
     return None
 
 
@@ -54,10 +66,9 @@ def stream_and_bounce_back(f_ikl, u0=0.1):
     code = storage_code(f_ikl, "stream_and_bounce_back")
     if nx < 2 or ny < 2:
         raise ValueError("stream_and_bounce_back: the cavity needs nx >= 2 and ny >= 2, got %d x %d" % (nx, ny))
-    tmp = torch.empty_like(f_ikl)
-    _lib.call("lbgb_stream_bounce_back", f_ikl.data_ptr(), tmp.data_ptr(), nx, ny, float(u0), code,
-              stream_handle(f_ikl))
-    f_ikl.copy_(tmp)
+    ws, nbytes = _workspace(f_ikl, nx, ny, code)
+    _lib.call("lbgb_stream_bounce_back_inplace", f_ikl.data_ptr(), nx, ny, float(u0), code, ws.data_ptr(),
+              nbytes, stream_handle(f_ikl))
     return None
 
 

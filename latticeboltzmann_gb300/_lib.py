@@ -50,6 +50,9 @@ SIGNATURES = {
     "lbgb_collide_ex": (_I, [_P, _I64, _I64, _I, _D, _I, _P]),
     "lbgb_stream_periodic": (_I, [_P, _P, _I, _I, _I, _P]),
     "lbgb_stream_bounce_back": (_I, [_P, _P, _I, _I, _D, _I, _P]),
+    "lbgb_stream_inplace_workspace_bytes": (_SZ, [_I, _I, _I]),
+    "lbgb_stream_periodic_inplace": (_I, [_P, _I, _I, _I, _P, _SZ, _P]),
+    "lbgb_stream_bounce_back_inplace": (_I, [_P, _I, _I, _D, _I, _P, _SZ, _P]),
     "lbgb_step_fused": (_I, [_P, _P, _I, _I, _I, _D, _D, _I, _P]),
     "lbgb_copy_rows": (_I, [_P, _P, _I, _I, _I, _I, _I, _P]),
     "lbgb_step_fused_rows": (_I, [_P, _P, _I, _I, _I, _I, _I, ctypes.c_double, ctypes.c_double, _I, _P]),

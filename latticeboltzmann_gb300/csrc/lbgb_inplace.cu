@@ -1,0 +1,323 @@
+// In-place streaming for the drop-in operators (PyLB.Streaming.stream and the
+// cavity scripts' stream_and_bounce_back act on their argument in place).
+//
+// A pull stream reads every node's eight neighbours, so it cannot overwrite
+// its source in one pass over independent blocks: a block would read values
+// that a neighbouring block has already replaced.  Here the lattice is cut
+// into tiles of IP_TX rows x 512 bytes of a row; one block owns one tile, reads
+// the whole tile (all nine channels) into shared memory, waits for its own
+// threads, and writes the streamed tile back over the same cells.  The only
+// values a tile needs from outside itself are the rows and columns next to
+// it, and only the three channels that cross each edge; a first kernel saves
+// exactly those edge values of every tile into a small workspace before any
+// tile is overwritten, and the second kernel takes its halo from there.
+//
+// Bytes per cell: 72 (FP32: 36 read, 36 written) plus the edge records, about
+// 9 % at the default tile; the stream-into-scratch-and-copy-back it replaces
+// moved 144.  Results equal the out-of-place kernels' bit for bit (same
+// decode, same lid arithmetic, same encode).
+#include <limits.h>
+
+#include "lbgb_common.cuh"
+
+namespace lbgb {
+namespace {
+
+constexpr int IP_TX = 16;         // tile rows (x)
+constexpr int IP_THREADS = 256;
+
+template <class raw>
+struct IpGeom {
+    static constexpr int VW = 16 / (int)sizeof(raw);   // elements per 16-byte vector
+    static constexpr int TY = 512 / (int)sizeof(raw);  // tile columns (y): 512 bytes of a row
+    static constexpr int PITCH = TY + 2 * VW;          // shared row: halo column, interior at VW, halo column
+    static constexpr int ROWS = IP_TX + 2;             // halo row, IP_TX interior rows, halo row
+    static constexpr size_t SMEM = 9ull * ROWS * PITCH * sizeof(raw);
+    static constexpr int VPR = TY / VW;                // vectors per full tile row (32)
+    static constexpr int MAXV = 9 * IP_TX * VPR / IP_THREADS;  // vectors per thread of a full tile (18)
+    static_assert(9 * IP_TX * VPR % IP_THREADS == 0, "full tiles split evenly over the threads");
+    static_assert(IP_THREADS % TY == 0, "whole rows per pass of the store loop");
+};
+
+// The channels that a neighbouring tile pulls across each edge of a tile:
+// side 0 first row (pulled from k+1: cx < 0), side 1 last row (cx > 0),
+// side 2 first column (pulled from l+1: cy < 0), side 3 last column (cy > 0).
+__host__ __device__ constexpr int edge_ch(int side, int j) {
+    return side == 0 ? (j == 0 ? CW : j == 1 ? CNW : CSW)
+         : side == 1 ? (j == 0 ? CE : j == 1 ? CNE : CSE)
+         : side == 2 ? (j == 0 ? CS : j == 1 ? CSW : CSE)
+                     : (j == 0 ? CN : j == 1 ? CNE : CNW);
+}
+
+// Workspace: row records [ntx][2][3][ny] (first / last row of each x tile),
+// then, from a 16-byte boundary, column records [nty][2][3][nx].
+struct IpLayout {
+    long long ntx, nty, col_off, total;  // counts and offsets in elements
+};
+
+template <class raw>
+__host__ __device__ inline IpLayout ip_layout(int nx, int ny) {
+    using G = IpGeom<raw>;
+    IpLayout L;
+    L.ntx = (nx + IP_TX - 1) / IP_TX;
+    L.nty = (ny + G::TY - 1) / G::TY;
+    const long long rows = 6 * L.ntx * (long long)ny;
+    L.col_off = (rows + G::VW - 1) / G::VW * G::VW;
+    L.total = L.col_off + 6 * L.nty * (long long)nx;
+    return L;
+}
+
+// One block per edge record: copies channel edge_ch(side, j) of one row or
+// column of f into the workspace.
+template <class raw>
+__global__ void __launch_bounds__(IP_THREADS) k_ip_save(const raw *f, raw *__restrict__ ws, int nx, int ny) {
+    using G = IpGeom<raw>;
+    const IpLayout L = ip_layout<raw>(nx, ny);
+    const size_t cs = (size_t)nx * ny;
+    const long long rec = blockIdx.x;
+    if (rec < 6 * L.ntx) {
+        const int t = (int)(rec / 6), side = (int)(rec / 3 % 2), j = (int)(rec % 3);
+        const int row = side == 0 ? t * IP_TX : min((t + 1) * IP_TX, nx) - 1;
+        const raw *src = f + (size_t)edge_ch(side, j) * cs + (size_t)row * ny;
+        raw *dst = ws + rec * ny;
+        for (int l = threadIdx.x; l < ny; l += IP_THREADS) dst[l] = src[l];
+    } else {
+        const long long r2 = rec - 6 * L.ntx;
+        const int u = (int)(r2 / 6), side = (int)(r2 / 3 % 2), j = (int)(r2 % 3);
+        const int col = side == 0 ? u * G::TY : min((u + 1) * G::TY, ny) - 1;
+        const raw *src = f + (size_t)edge_ch(2 + side, j) * cs + col;
+        raw *dst = ws + L.col_off + r2 * nx;
+        for (int k = threadIdx.x; k < nx; k += IP_THREADS) dst[k] = src[(size_t)k * ny];
+    }
+}
+
+// One block per tile: the tile and its saved halo into shared memory, then
+// the pulled (and, for the cavity, reflected) values back over the tile.
+template <int DT, int BC>
+__global__ void __launch_bounds__(IP_THREADS, 2)
+k_ip_stream(typename Codec<DT>::raw *f, const typename Codec<DT>::raw *__restrict__ ws, int nx, int ny,
+            typename Codec<DT>::real u0, int vec) {
+    using C = Codec<DT>;
+    using raw = typename C::raw;
+    using real = typename C::real;
+    using G = IpGeom<raw>;
+    extern __shared__ __align__(16) unsigned char ip_smem[];
+    raw *s = reinterpret_cast<raw *>(ip_smem);
+    auto S = [](int ch, int rr, int cc) { return (ch * G::ROWS + rr) * G::PITCH + cc; };
+
+    const IpLayout L = ip_layout<raw>(nx, ny);
+    const int tx = (int)(blockIdx.x / L.nty), ty = (int)(blockIdx.x % L.nty);
+    const int a = tx * IP_TX, c = ty * G::TY;
+    const int txn = min(IP_TX, nx - a), tyn = min(G::TY, ny - c);
+    const size_t cs = (size_t)nx * ny;
+    const int tid = threadIdx.x;
+
+    // ---- the tile, all nine channels
+    if (vec) {
+        // rows hold whole 16-byte vectors (ny % VW == 0, f 16-byte aligned),
+        // so does every tile row: c and tyn are multiples of VW
+        const int vpr = tyn / G::VW, per_ch = txn * vpr, nvec = 9 * per_ch;
+        uint4 buf[G::MAXV];
+#pragma unroll
+        for (int q = 0; q < G::MAXV; ++q) {
+            const int i = tid + q * IP_THREADS;
+            if (i < nvec) {
+                const int ch = i / per_ch, rem = i - ch * per_ch, r = rem / vpr, v = rem - r * vpr;
+                buf[q] = *reinterpret_cast<const uint4 *>(f + ch * cs + (size_t)(a + r) * ny + c + v * G::VW);
+            }
+        }
+#pragma unroll
+        for (int q = 0; q < G::MAXV; ++q) {
+            const int i = tid + q * IP_THREADS;
+            if (i < nvec) {
+                const int ch = i / per_ch, rem = i - ch * per_ch, r = rem / vpr, v = rem - r * vpr;
+                *reinterpret_cast<uint4 *>(s + S(ch, r + 1, G::VW + v * G::VW)) = buf[q];
+            }
+        }
+    } else {
+        const int per_ch = txn * tyn, n = 9 * per_ch;
+        for (int i = tid; i < n; i += IP_THREADS) {
+            const int ch = i / per_ch, rem = i - ch * per_ch, r = rem / tyn, col = rem - r * tyn;
+            s[S(ch, r + 1, G::VW + col)] = f[ch * cs + (size_t)(a + r) * ny + c + col];
+        }
+    }
+
+    // ---- halo rows a-1 and a+txn (periodic in x), columns c-1 .. c+tyn (periodic in y)
+    {
+        const int tlo = (tx == 0 ? (int)L.ntx : tx) - 1, thi = (tx + 1 == L.ntx) ? 0 : tx + 1;
+        const int w = tyn + 2, n = 6 * w;
+        for (int i = tid; i < n; i += IP_THREADS) {
+            const int hi = i / (3 * w), rem = i - hi * 3 * w, j = rem / w, col = rem - j * w - 1;
+            int l = c + col;
+            if (l < 0) l += ny;
+            if (l >= ny) l -= ny;
+            const long long rec = hi ? ((long long)thi * 2 + 0) * 3 + j : ((long long)tlo * 2 + 1) * 3 + j;
+            s[S(edge_ch(hi ? 0 : 1, j), hi ? txn + 1 : 0, G::VW + col)] = ws[rec * ny + l];
+        }
+    }
+    // ---- halo columns c-1 and c+tyn, rows a .. a+txn-1
+    {
+        const int ulo = (ty == 0 ? (int)L.nty : ty) - 1, uhi = (ty + 1 == L.nty) ? 0 : ty + 1;
+        const int n = 6 * txn;
+        for (int i = tid; i < n; i += IP_THREADS) {
+            const int hi = i / (3 * txn), rem = i - hi * 3 * txn, j = rem / txn, r = rem - j * txn;
+            const long long rec = hi ? ((long long)uhi * 2 + 0) * 3 + j : ((long long)ulo * 2 + 1) * 3 + j;
+            s[S(edge_ch(hi ? 2 : 3, j), r + 1, hi ? G::VW + tyn : G::VW - 1)] = ws[L.col_off + rec * nx + a + r];
+        }
+    }
+    __syncthreads();
+
+    // ---- stream: every value of the tile from shared memory, back over f
+    constexpr int RPP = IP_THREADS / G::TY;  // rows per pass
+    const int col = tid % G::TY;
+    if (col >= tyn) return;
+    const int l = c + col, cc = G::VW + col;
+    for (int r = tid / G::TY; r < txn; r += RPP) {
+        const int k = a + r, rr = r + 1;
+        auto at = [&](int ch, int dr, int dc) { return C::dec(s[S(ch, rr + dr, cc + dc)], ch); };
+        real v[9];
+        v[0] = at(C0, 0, 0);
+#pragma unroll
+        for (int ch = 1; ch < 9; ++ch) {
+            const bool wall = BC != LBGB_PERIODIC && ((cx(ch) > 0 && k == 0) || (cx(ch) < 0 && k == nx - 1));
+            // side-wall bounce-back from the same node, decoded as channel ch
+            v[ch] = wall ? C::dec(s[S(opp(ch), rr, cc)], ch) : at(ch, -cx(ch), -cy(ch));
+        }
+        if (BC != LBGB_PERIODIC) {
+            if (l == 0) {
+                // bottom wall: N, NE, NW bounce back from the same node
+                v[CN] = C::dec(s[S(CS, rr, cc)], CN);
+                v[CNE] = C::dec(s[S(CSW, rr, cc)], CNE);
+                v[CNW] = C::dec(s[S(CSE, rr, cc)], CNW);
+            }
+            if (l == ny - 1) {
+                // lid: S bounces back, SE/SW get the Ladd term with the lid
+                // density read across the periodic seam, side walls win at
+                // the corners (the out-of-place kernel's sum order)
+                const real gN = at(CN, 0, 0), gNW = at(CNW, 0, 0), gNE = at(CNE, 0, 0);
+                const real rho_lid = gNW + gN + gNE + at(CNW, 1, -1) + at(CN, 0, -1) + at(CNE, -1, -1) +
+                                     at(CW, 1, 0) + at(C0, 0, 0) + at(CE, -1, 0);
+                const real lid = lid_from_sum<C>(rho_lid, u0);
+                v[CS] = gN;
+                v[CSE] = (k == 0) ? gNW : gNW + lid;
+                v[CSW] = (k == nx - 1) ? gNE : gNE - lid;
+            }
+        }
+        raw *dst = f + (size_t)k * ny + l;
+#pragma unroll
+        for (int ch = 0; ch < 9; ++ch) dst[ch * cs] = C::enc(v[ch], ch);
+    }
+}
+
+template <int DT>
+int launch_ip(void *f, int nx, int ny, int boundary, double u0, void *ws, size_t ws_bytes, cudaStream_t s,
+              const char *what) {
+    using raw = typename Codec<DT>::raw;
+    using G = IpGeom<raw>;
+    const IpLayout L = ip_layout<raw>(nx, ny);
+    const size_t need = (size_t)L.total * sizeof(raw);
+    if (!ws || ws_bytes < need) {
+        set_error("%s: workspace of %zu bytes given, %zu needed (lbgb_stream_inplace_workspace_bytes)", what,
+                  ws_bytes, need);
+        return LBGB_EINVAL;
+    }
+    if (!aligned(ws, 16)) {
+        set_error("%s: the workspace must be 16-byte aligned", what);
+        return LBGB_EINVAL;
+    }
+    const long long tiles = L.ntx * L.nty, recs = 6 * (L.ntx + L.nty);
+    if (tiles > INT_MAX || recs > INT_MAX) {
+        set_error("%s: lattice %d x %d has too many tiles", what, nx, ny);
+        return LBGB_EINVAL;
+    }
+    const int vec = (ny % G::VW == 0) && aligned(f, 16);
+    raw *fp = static_cast<raw *>(f);
+    k_ip_save<raw><<<(unsigned)recs, IP_THREADS, 0, s>>>(fp, static_cast<raw *>(ws), nx, ny);
+    int rc = check_launch("k_ip_save");
+    if (rc) return rc;
+    static std::atomic<bool> attr_set[MAX_DEVICES][2];
+    const int dev = current_device();
+    const int variant = boundary == LBGB_PERIODIC ? 0 : 1;
+    auto go = [&](auto kernel) -> int {
+        if (!attr_set[dev][variant].load(std::memory_order_acquire)) {
+            std::lock_guard<std::mutex> lock(setup_mutex());
+            cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)G::SMEM);
+            if (e != cudaSuccess) {
+                set_error("k_ip_stream: cannot reserve %zu bytes of shared memory: %s", G::SMEM,
+                          cudaGetErrorString(e));
+                return LBGB_ECUDA;
+            }
+            attr_set[dev][variant].store(true, std::memory_order_release);
+        }
+        kernel<<<(unsigned)tiles, IP_THREADS, G::SMEM, s>>>(fp, static_cast<const raw *>(ws), nx, ny,
+                                                            (typename Codec<DT>::real)u0, vec);
+        return check_launch("k_ip_stream");
+    };
+    return variant == 0 ? go(k_ip_stream<DT, LBGB_PERIODIC>) : go(k_ip_stream<DT, LBGB_CAVITY>);
+}
+
+int ip_check(void *f, int nx, int ny, int dtype, int boundary, const char *what) {
+    if (raw_size(dtype) == 0) {
+        set_error("%s: unsupported storage code %d", what, dtype);
+        return LBGB_EDTYPE;
+    }
+    if (nx <= 0 || ny <= 0) {
+        set_error("%s: grid %d x %d must be positive", what, nx, ny);
+        return LBGB_EINVAL;
+    }
+    if (boundary != LBGB_PERIODIC && (nx < 2 || ny < 2)) {
+        set_error("%s: the cavity needs nx >= 2 and ny >= 2 (got %d x %d)", what, nx, ny);
+        return LBGB_EINVAL;
+    }
+    if (!f) {
+        set_error("%s: null population pointer", what);
+        return LBGB_EINVAL;
+    }
+    if (!aligned(f, raw_size(dtype))) {
+        set_error("%s: population pointer must be aligned to the element size", what);
+        return LBGB_EINVAL;
+    }
+    return LBGB_OK;
+}
+
+int ip_dispatch(void *f, int nx, int ny, int dtype, int boundary, double u0, void *ws, size_t ws_bytes,
+                void *stream, const char *what) {
+    int rc = ip_check(f, nx, ny, dtype, boundary, what);
+    if (rc) return rc;
+    cudaStream_t s = (cudaStream_t)stream;
+    switch (dtype) {
+    case LBGB_F32: return launch_ip<LBGB_F32>(f, nx, ny, boundary, u0, ws, ws_bytes, s, what);
+    case LBGB_F64: return launch_ip<LBGB_F64>(f, nx, ny, boundary, u0, ws, ws_bytes, s, what);
+    case LBGB_F16DEV: return launch_ip<LBGB_F16DEV>(f, nx, ny, boundary, u0, ws, ws_bytes, s, what);
+    case LBGB_BF16DEV: return launch_ip<LBGB_BF16DEV>(f, nx, ny, boundary, u0, ws, ws_bytes, s, what);
+    case LBGB_F32DEV: return launch_ip<LBGB_F32DEV>(f, nx, ny, boundary, u0, ws, ws_bytes, s, what);
+    default: set_error("%s: unsupported storage code %d", what, dtype); return LBGB_EDTYPE;
+    }
+}
+
+}  // namespace
+}  // namespace lbgb
+
+using namespace lbgb;
+
+extern "C" size_t lbgb_stream_inplace_workspace_bytes(int nx, int ny, int dtype) {
+    if (nx <= 0 || ny <= 0) return 0;
+    switch (raw_size(dtype)) {
+    case 2: return (size_t)ip_layout<unsigned short>(nx, ny).total * 2;
+    case 4: return (size_t)ip_layout<float>(nx, ny).total * 4;
+    case 8: return (size_t)ip_layout<double>(nx, ny).total * 8;
+    default: return 0;
+    }
+}
+
+extern "C" int lbgb_stream_periodic_inplace(void *f, int nx, int ny, int dtype, void *work, size_t work_bytes,
+                                            void *stream) {
+    return ip_dispatch(f, nx, ny, dtype, LBGB_PERIODIC, 0.0, work, work_bytes, stream,
+                       "lbgb_stream_periodic_inplace");
+}
+
+extern "C" int lbgb_stream_bounce_back_inplace(void *f, int nx, int ny, double u0, int dtype, void *work,
+                                               size_t work_bytes, void *stream) {
+    return ip_dispatch(f, nx, ny, dtype, LBGB_CAVITY, u0, work, work_bytes, stream,
+                       "lbgb_stream_bounce_back_inplace");
+}
