@@ -80,6 +80,8 @@ def parse(argv=None):
                         "advanced by one launch per step (autotuned)")
     p.add_argument("--no-extras", action="store_true",
                    help="skip the 16-bit storage comparison, the operator-path timing and the warm-start study")
+    p.add_argument("--extras", default="operator_path,fp16_store,warm_start",
+                   help="comma-separated extras to run (cavity workload): operator_path, fp16_store, warm_start")
     p.add_argument("--store-n", type=int, default=16384, help="lattice side of the 16-bit storage comparison")
     p.add_argument("--store-steps", type=int, default=60, help="timed steps per storage in that comparison")
     p.add_argument("--warm-cases", type=int, default=8, help="held-out cavities timed cold and warm at 256^2")
@@ -461,10 +463,17 @@ def run_ours(args):
                 "peak_source": peak_src,
                 "traffic_source": None if prof is None else prof.get("source")}
     extras = {}
-    if not args.no_extras and args.boundary == "cavity":
-        extras["operator_path"] = operator_path(args, dev)
-        extras["fp16_store"] = storage_comparison(args, dev, d.local_rank)
-        extras["warm_start"] = warm_start(args, dev)
+    want = set() if args.no_extras else {x.strip() for x in args.extras.split(",") if x.strip()}
+    unknown = want - {"operator_path", "fp16_store", "warm_start"}
+    if unknown:
+        raise SystemExit("bench.py: unknown extras %s" % sorted(unknown))
+    if args.boundary == "cavity":
+        if "operator_path" in want:
+            extras["operator_path"] = operator_path(args, dev)
+        if "fp16_store" in want:
+            extras["fp16_store"] = storage_comparison(args, dev, d.local_rank)
+        if "warm_start" in want:
+            extras["warm_start"] = warm_start(args, dev)
     cpu = None
     if not args.no_cpu_baseline:
         c_mlups, cores, sample = cpu_port_sample(args.nx, args.ny, args.omega, args.u0, args.storage, args.boundary,
@@ -616,23 +625,30 @@ def operator_path(args, dev):
         PyLB.Streaming.stream_and_bounce_back(f, args.u0)
         PyLB.collide(f.reshape(9, -1), args.omega)
 
-    for _ in range(max(3, args.warmup)):
-        step()
+    def timed(fn):
+        for _ in range(max(3, args.warmup)):
+            fn()
+        torch.cuda.synchronize(dev)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(steps):
+            fn()
+        e1.record(stream)
+        torch.cuda.synchronize(dev)
+        _lib.device_status()
+        return e0.elapsed_time(e1) / 1e3
+
     steps = max(5, min(args.steps, 20))
-    torch.cuda.synchronize(dev)
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    e0.record(stream)
-    for _ in range(steps):
-        step()
-    e1.record(stream)
-    torch.cuda.synchronize(dev)
-    _lib.device_status()
-    secs = e0.elapsed_time(e1) / 1e3
+    secs = timed(step)
+    s_secs = timed(lambda: PyLB.Streaming.stream_and_bounce_back(f, args.u0))
     peak, _ = hbm_peak()
     del f
     torch.cuda.empty_cache()
     return {"mlups": round(nx * ny * steps / secs / 1e6, 1), "ms_per_step": round(secs / steps * 1e3, 4),
             "bytes_per_cell": 144, "frac": round(144 * nx * ny * steps / secs / 1e9 / peak, 4), "steps": steps,
+            "stream_only": {"mlups": round(nx * ny * steps / s_secs / 1e6, 1),
+                            "ms": round(s_secs / steps * 1e3, 4), "bytes_per_cell": 72,
+                            "frac": round(72 * nx * ny * steps / s_secs / 1e9 / peak, 4)},
             "launches_per_step": 3,
             "path": "PyLB.Streaming.stream_and_bounce_back (in place: k_ip_save + k_ip_stream) + PyLB.collide, "
                     "float32 (%dx%d)" % (nx, ny)}

@@ -231,6 +231,32 @@ def single_case_timing(net, re, u, n, device=None, tol=1e-7, max_steps=600_000):
     return rows
 
 
+class Ensemble:
+    """Mean of several trained networks' predictions: independent fits make
+    partly independent errors, which the mean reduces."""
+
+    def __init__(self, nets):
+        self.nets = list(nets)
+        self.device = self.nets[0].device
+
+    def predict(self, re, u_lid, nx, ny):
+        acc = None
+        for net in self.nets:
+            p = net.predict(re, u_lid, nx, ny)  # views of the network's workspace
+            acc = [x.clone() for x in p] if acc is None else [a.add_(x) for a, x in zip(acc, p)]
+        k = 1.0 / len(self.nets)
+        return tuple(a.mul_(k) for a in acc)
+
+
+def load_networks(paths, device):
+    """One network (.npz), or the Ensemble of several (a list of paths, or
+    one string with comma-separated paths)."""
+    if isinstance(paths, str):
+        paths = [p for p in paths.split(",") if p]
+    nets = [FNO2d.load(p, device=device) for p in paths]
+    return nets[0] if len(nets) == 1 else Ensemble(nets)
+
+
 def study_only(args):
     """Warm-versus-cold study of a trained network on the held-out pairs of
     an earlier run (no data generation, no training)."""
@@ -243,11 +269,12 @@ def study_only(args):
         logf.write(m + "\n")
         logf.flush()
 
-    net = FNO2d.load(args.weights, device=dev)
+    net = load_networks(args.weights, dev)
     prev = json.load(open(args.held_out_from))
     val = np.asarray(prev["held_out"])
     re_all, u_all = np.asarray(prev["data_re"]), np.asarray(prev["data_u"])
-    res = {"weights": os.path.basename(args.weights), "storage": args.storage, "switch_tol": args.switch_tol}
+    res = {"weights": [os.path.basename(p) for p in args.weights.split(",")], "storage": args.storage,
+           "switch_tol": args.switch_tol}
     res["study"] = study(net, re_all[val], u_all[val], args.n, dev, max_steps=args.max_steps)
     s = res["study"]
     log("study %d: cold %.1f s, warm %.1f s (inference %.3f s); steps cold %d warm %d (sums)" % (
@@ -298,7 +325,9 @@ def main(argv=None):
     ap.add_argument("--storage", default="f32dev", help="storage of the steady runs before any FP64 refinement")
     ap.add_argument("--switch-tol", type=float, default=None,
                     help="run every instance to this change, then FP64 (default: FP64 only where a run stalls)")
-    ap.add_argument("--weights", default=None, help="study only: a trained network (.npz) instead of training")
+    ap.add_argument("--weights", default=None,
+                    help="study only: a trained network (.npz), or comma-separated networks whose predictions "
+                         "are averaged, instead of training")
     ap.add_argument("--held-out-from", default=None,
                     help="study only: results.json of the training run that holds the held-out (Re, u) pairs")
     args = ap.parse_args(argv)
