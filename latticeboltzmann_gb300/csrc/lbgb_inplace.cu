@@ -13,9 +13,10 @@
 // tile is overwritten, and the second kernel takes its halo from there.
 //
 // Bytes per cell: 72 (FP32: 36 read, 36 written) plus the edge records, about
-// 9 % at the default tile; the stream-into-scratch-and-copy-back it replaces
-// moved 144.  Results equal the out-of-place kernels' bit for bit (same
-// decode, same lid arithmetic, same encode).
+// 15 % at the default tile (a column record's scattered reads fetch whole
+// lines); the stream-into-scratch-and-copy-back it replaces moved 144.
+// Results equal the out-of-place kernels' bit for bit (same decode, same lid
+// arithmetic, same encode).
 #include <limits.h>
 
 #include "lbgb_common.cuh"
@@ -34,9 +35,6 @@ struct IpGeom {
     static constexpr int ROWS = IP_TX + 2;             // halo row, IP_TX interior rows, halo row
     static constexpr size_t SMEM = 9ull * ROWS * PITCH * sizeof(raw);
     static constexpr int VPR = TY / VW;                // vectors per full tile row (32)
-    static constexpr int MAXV = 9 * IP_TX * VPR / IP_THREADS;  // vectors per thread of a full tile (18)
-    static_assert(9 * IP_TX * VPR % IP_THREADS == 0, "full tiles split evenly over the threads");
-    static_assert(IP_THREADS % TY == 0, "whole rows per pass of the store loop");
 };
 
 // The channels that a neighbouring tile pulls across each edge of a tile:
@@ -91,104 +89,99 @@ __global__ void __launch_bounds__(IP_THREADS) k_ip_save(const raw *f, raw *__res
     }
 }
 
-// One block per tile: the tile and its saved halo into shared memory, then
-// the pulled (and, for the cavity, reflected) values back over the tile.
-template <int DT, int BC>
-__global__ void __launch_bounds__(IP_THREADS, 2)
-k_ip_stream(typename Codec<DT>::raw *f, const typename Codec<DT>::raw *__restrict__ ws, int nx, int ny,
-            typename Codec<DT>::real u0, int vec) {
+// A tile's rows [a, a + txn) and columns [c, c + tyn).
+struct IpTile {
+    int tx, ty, a, c, txn, tyn;
+};
+
+template <class raw>
+__device__ __forceinline__ IpTile ip_tile(long long t, const IpLayout &L, int nx, int ny) {
+    using G = IpGeom<raw>;
+    IpTile T;
+    T.tx = (int)(t / L.nty);
+    T.ty = (int)(t - (long long)T.tx * L.nty);
+    T.a = T.tx * IP_TX;
+    T.c = T.ty * G::TY;
+    T.txn = min(IP_TX, nx - T.a);
+    T.tyn = min(G::TY, ny - T.c);
+    return T;
+}
+
+// Element offset of (channel, shared row rr, shared column cc) in one stage:
+// rr = r + 1 for tile row r (0 and txn + 1 are the halo rows), cc = VW + col
+// (VW - 1 and VW + tyn are the halo columns).
+template <class raw>
+__device__ __forceinline__ int ip_S(int ch, int rr, int cc) {
+    using G = IpGeom<raw>;
+    return (ch * G::ROWS + rr) * G::PITCH + cc;
+}
+
+// Halo value i of tile T, 0 <= i < 6 (tyn + 2) + 6 txn: rows a - 1 and a + txn
+// over columns c - 1 .. c + tyn (periodic in both directions), then columns
+// c - 1 and c + tyn over the tile's rows.  Sets its shared-memory offset and
+// workspace index; false past the end.
+template <class raw>
+__device__ __forceinline__ bool ip_halo_item(int i, const IpTile &T, const IpLayout &L, int nx, int ny, int &soff,
+                                             long long &widx) {
+    using G = IpGeom<raw>;
+    const int w = T.tyn + 2, nrow = 6 * w;
+    if (i < nrow) {
+        const int hi = i / (3 * w), rem = i - hi * 3 * w, j = rem / w, col = rem - j * w - 1;
+        int l = T.c + col;
+        if (l < 0) l += ny;
+        if (l >= ny) l -= ny;
+        const int tlo = (T.tx == 0 ? (int)L.ntx : T.tx) - 1, thi = (T.tx + 1 == L.ntx) ? 0 : T.tx + 1;
+        const long long rec = hi ? ((long long)thi * 2 + 0) * 3 + j : ((long long)tlo * 2 + 1) * 3 + j;
+        soff = ip_S<raw>(edge_ch(hi ? 0 : 1, j), hi ? T.txn + 1 : 0, G::VW + col);
+        widx = rec * ny + l;
+        return true;
+    }
+    i -= nrow;
+    if (i < 6 * T.txn) {
+        const int hi = i / (3 * T.txn), rem = i - hi * 3 * T.txn, j = rem / T.txn, r = rem - j * T.txn;
+        const int ulo = (T.ty == 0 ? (int)L.nty : T.ty) - 1, uhi = (T.ty + 1 == L.nty) ? 0 : T.ty + 1;
+        const long long rec = hi ? ((long long)uhi * 2 + 0) * 3 + j : ((long long)ulo * 2 + 1) * 3 + j;
+        soff = ip_S<raw>(edge_ch(hi ? 2 : 3, j), r + 1, hi ? G::VW + T.tyn : G::VW - 1);
+        widx = L.col_off + rec * nx + T.a + r;
+        return true;
+    }
+    return false;
+}
+
+// Every value of tile T from the stage s (interior and halo filled), pulled,
+// reflected at the cavity walls and lid, written back over the tile in f.
+// NT threads, a multiple of the tile width: thread tid owns column tid % TY.
+template <int DT, int BC, int NT>
+__device__ __forceinline__ void ip_stream_tile(const typename Codec<DT>::raw *s, typename Codec<DT>::raw *f,
+                                               const IpTile &T, int nx, int ny, typename Codec<DT>::real u0,
+                                               int tid) {
     using C = Codec<DT>;
     using raw = typename C::raw;
     using real = typename C::real;
     using G = IpGeom<raw>;
-    extern __shared__ __align__(16) unsigned char ip_smem[];
-    raw *s = reinterpret_cast<raw *>(ip_smem);
-    auto S = [](int ch, int rr, int cc) { return (ch * G::ROWS + rr) * G::PITCH + cc; };
-
-    const IpLayout L = ip_layout<raw>(nx, ny);
-    const int tx = (int)(blockIdx.x / L.nty), ty = (int)(blockIdx.x % L.nty);
-    const int a = tx * IP_TX, c = ty * G::TY;
-    const int txn = min(IP_TX, nx - a), tyn = min(G::TY, ny - c);
+    static_assert(NT % G::TY == 0, "whole rows per pass");
+    constexpr int RPP = NT / G::TY;  // rows per pass
     const size_t cs = (size_t)nx * ny;
-    const int tid = threadIdx.x;
-
-    // ---- the tile, all nine channels
-    if (vec) {
-        // rows hold whole 16-byte vectors (ny % VW == 0, f 16-byte aligned),
-        // so does every tile row: c and tyn are multiples of VW
-        const int vpr = tyn / G::VW, per_ch = txn * vpr, nvec = 9 * per_ch;
-        uint4 buf[G::MAXV];
-#pragma unroll
-        for (int q = 0; q < G::MAXV; ++q) {
-            const int i = tid + q * IP_THREADS;
-            if (i < nvec) {
-                const int ch = i / per_ch, rem = i - ch * per_ch, r = rem / vpr, v = rem - r * vpr;
-                buf[q] = *reinterpret_cast<const uint4 *>(f + ch * cs + (size_t)(a + r) * ny + c + v * G::VW);
-            }
-        }
-#pragma unroll
-        for (int q = 0; q < G::MAXV; ++q) {
-            const int i = tid + q * IP_THREADS;
-            if (i < nvec) {
-                const int ch = i / per_ch, rem = i - ch * per_ch, r = rem / vpr, v = rem - r * vpr;
-                *reinterpret_cast<uint4 *>(s + S(ch, r + 1, G::VW + v * G::VW)) = buf[q];
-            }
-        }
-    } else {
-        const int per_ch = txn * tyn, n = 9 * per_ch;
-        for (int i = tid; i < n; i += IP_THREADS) {
-            const int ch = i / per_ch, rem = i - ch * per_ch, r = rem / tyn, col = rem - r * tyn;
-            s[S(ch, r + 1, G::VW + col)] = f[ch * cs + (size_t)(a + r) * ny + c + col];
-        }
-    }
-
-    // ---- halo rows a-1 and a+txn (periodic in x), columns c-1 .. c+tyn (periodic in y)
-    {
-        const int tlo = (tx == 0 ? (int)L.ntx : tx) - 1, thi = (tx + 1 == L.ntx) ? 0 : tx + 1;
-        const int w = tyn + 2, n = 6 * w;
-        for (int i = tid; i < n; i += IP_THREADS) {
-            const int hi = i / (3 * w), rem = i - hi * 3 * w, j = rem / w, col = rem - j * w - 1;
-            int l = c + col;
-            if (l < 0) l += ny;
-            if (l >= ny) l -= ny;
-            const long long rec = hi ? ((long long)thi * 2 + 0) * 3 + j : ((long long)tlo * 2 + 1) * 3 + j;
-            s[S(edge_ch(hi ? 0 : 1, j), hi ? txn + 1 : 0, G::VW + col)] = ws[rec * ny + l];
-        }
-    }
-    // ---- halo columns c-1 and c+tyn, rows a .. a+txn-1
-    {
-        const int ulo = (ty == 0 ? (int)L.nty : ty) - 1, uhi = (ty + 1 == L.nty) ? 0 : ty + 1;
-        const int n = 6 * txn;
-        for (int i = tid; i < n; i += IP_THREADS) {
-            const int hi = i / (3 * txn), rem = i - hi * 3 * txn, j = rem / txn, r = rem - j * txn;
-            const long long rec = hi ? ((long long)uhi * 2 + 0) * 3 + j : ((long long)ulo * 2 + 1) * 3 + j;
-            s[S(edge_ch(hi ? 2 : 3, j), r + 1, hi ? G::VW + tyn : G::VW - 1)] = ws[L.col_off + rec * nx + a + r];
-        }
-    }
-    __syncthreads();
-
-    // ---- stream: every value of the tile from shared memory, back over f
-    constexpr int RPP = IP_THREADS / G::TY;  // rows per pass
     const int col = tid % G::TY;
-    if (col >= tyn) return;
-    const int l = c + col, cc = G::VW + col;
-    for (int r = tid / G::TY; r < txn; r += RPP) {
-        const int k = a + r, rr = r + 1;
-        auto at = [&](int ch, int dr, int dc) { return C::dec(s[S(ch, rr + dr, cc + dc)], ch); };
+    if (col >= T.tyn) return;
+    const int l = T.c + col, cc = G::VW + col;
+    for (int r = tid / G::TY; r < T.txn; r += RPP) {
+        const int k = T.a + r, rr = r + 1;
+        auto at = [&](int ch, int dr, int dc) { return C::dec(s[ip_S<raw>(ch, rr + dr, cc + dc)], ch); };
         real v[9];
         v[0] = at(C0, 0, 0);
 #pragma unroll
         for (int ch = 1; ch < 9; ++ch) {
             const bool wall = BC != LBGB_PERIODIC && ((cx(ch) > 0 && k == 0) || (cx(ch) < 0 && k == nx - 1));
             // side-wall bounce-back from the same node, decoded as channel ch
-            v[ch] = wall ? C::dec(s[S(opp(ch), rr, cc)], ch) : at(ch, -cx(ch), -cy(ch));
+            v[ch] = wall ? C::dec(s[ip_S<raw>(opp(ch), rr, cc)], ch) : at(ch, -cx(ch), -cy(ch));
         }
         if (BC != LBGB_PERIODIC) {
             if (l == 0) {
                 // bottom wall: N, NE, NW bounce back from the same node
-                v[CN] = C::dec(s[S(CS, rr, cc)], CN);
-                v[CNE] = C::dec(s[S(CSW, rr, cc)], CNE);
-                v[CNW] = C::dec(s[S(CSE, rr, cc)], CNW);
+                v[CN] = C::dec(s[ip_S<raw>(CS, rr, cc)], CN);
+                v[CNE] = C::dec(s[ip_S<raw>(CSW, rr, cc)], CNE);
+                v[CNW] = C::dec(s[ip_S<raw>(CSE, rr, cc)], CNW);
             }
             if (l == ny - 1) {
                 // lid: S bounces back, SE/SW get the Ladd term with the lid
@@ -207,6 +200,135 @@ k_ip_stream(typename Codec<DT>::raw *f, const typename Codec<DT>::raw *__restric
 #pragma unroll
         for (int ch = 0; ch < 9; ++ch) dst[ch * cs] = C::enc(v[ch], ch);
     }
+}
+
+// Generic form, any alignment: one block per tile; the tile and its saved
+// halo into shared memory, then the streamed tile back over itself.
+template <int DT, int BC>
+__global__ void __launch_bounds__(IP_THREADS, 2)
+k_ip_stream(typename Codec<DT>::raw *f, const typename Codec<DT>::raw *__restrict__ ws, int nx, int ny,
+            typename Codec<DT>::real u0) {
+    using raw = typename Codec<DT>::raw;
+    using G = IpGeom<raw>;
+    extern __shared__ __align__(16) unsigned char ip_smem[];
+    raw *s = reinterpret_cast<raw *>(ip_smem);
+    const IpLayout L = ip_layout<raw>(nx, ny);
+    const IpTile T = ip_tile<raw>(blockIdx.x, L, nx, ny);
+    const size_t cs = (size_t)nx * ny;
+    const int tid = threadIdx.x;
+    const int per_ch = T.txn * T.tyn, n = 9 * per_ch;
+    for (int i = tid; i < n; i += IP_THREADS) {
+        const int ch = i / per_ch, rem = i - ch * per_ch, r = rem / T.tyn, col = rem - r * T.tyn;
+        s[ip_S<raw>(ch, r + 1, G::VW + col)] = f[ch * cs + (size_t)(T.a + r) * ny + T.c + col];
+    }
+    const int nh = 6 * (T.tyn + 2) + 6 * T.txn;
+    for (int i = tid; i < nh; i += IP_THREADS) {
+        int soff;
+        long long widx;
+        if (ip_halo_item<raw>(i, T, L, nx, ny, soff, widx)) s[soff] = ws[widx];
+    }
+    __syncthreads();
+    ip_stream_tile<DT, BC, IP_THREADS>(s, f, T, nx, ny, u0, tid);
+}
+
+__device__ __forceinline__ void cp_async16(void *smem_dst, const void *gmem_src) {
+    const unsigned d = (unsigned)__cvta_generic_to_shared(smem_dst);
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(d), "l"(__cvta_generic_to_global(gmem_src))
+                 : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_prev() { asm volatile("cp.async.wait_group 1;\n" ::: "memory"); }
+
+// Pipelined form for rows of whole 16-byte vectors (16-byte aligned f, ny a
+// multiple of the vector width): one persistent block per SM with two
+// stages.  While a tile is streamed out of one stage, the next tile's
+// interior is on its way into the other (16-byte cp.async, one group per
+// tile) and its halo values into registers, so the SM's loads and stores
+// overlap instead of alternating.
+constexpr int IPP_THREADS = 512;
+
+template <int DT, int BC>
+__global__ void __launch_bounds__(IPP_THREADS, 1)
+k_ip_stream_pipe(typename Codec<DT>::raw *f, const typename Codec<DT>::raw *__restrict__ ws, int nx, int ny,
+                 typename Codec<DT>::real u0) {
+    using raw = typename Codec<DT>::raw;
+    using G = IpGeom<raw>;
+    constexpr int STAGE = 9 * G::ROWS * G::PITCH;                                    // elements per stage
+    constexpr int QMAX = 9 * IP_TX * G::VPR / IPP_THREADS;                           // vectors per thread
+    constexpr int HMAX = (6 * (G::TY + 2) + 6 * IP_TX + IPP_THREADS - 1) / IPP_THREADS;  // halo values per thread
+    static_assert(9 * IP_TX * G::VPR % IPP_THREADS == 0, "full tiles split evenly over the threads");
+    extern __shared__ __align__(16) unsigned char ip_smem[];
+    raw *sm = reinterpret_cast<raw *>(ip_smem);
+    const IpLayout L = ip_layout<raw>(nx, ny);
+    const size_t cs = (size_t)nx * ny;
+    const int tid = threadIdx.x;
+    const long long ntiles = L.ntx * L.nty;
+    long long t = blockIdx.x;
+    if (t >= ntiles) return;
+
+    auto issue = [&](long long tt, raw *stage) {
+        const IpTile T = ip_tile<raw>(tt, L, nx, ny);
+        const int vpr = T.tyn / G::VW, per_ch = T.txn * vpr, nvec = 9 * per_ch;
+#pragma unroll
+        for (int q = 0; q < QMAX; ++q) {
+            const int i = tid + q * IPP_THREADS;
+            if (i < nvec) {
+                const int ch = i / per_ch, rem = i - ch * per_ch, r = rem / vpr, v = rem - r * vpr;
+                cp_async16(stage + ip_S<raw>(ch, r + 1, G::VW + v * G::VW),
+                           f + ch * cs + (size_t)(T.a + r) * ny + T.c + v * G::VW);
+            }
+        }
+    };
+    raw hv[HMAX];
+    int hs[HMAX];
+    auto fetch_halo = [&](long long tt) {
+        const IpTile T = ip_tile<raw>(tt, L, nx, ny);
+#pragma unroll
+        for (int q = 0; q < HMAX; ++q) {
+            int soff;
+            long long widx;
+            if (ip_halo_item<raw>(tid + q * IPP_THREADS, T, L, nx, ny, soff, widx)) {
+                hs[q] = soff;
+                hv[q] = ws[widx];
+            } else {
+                hs[q] = -1;
+            }
+        }
+    };
+
+    int st = 0;
+    issue(t, sm);
+    cp_async_commit();
+    fetch_halo(t);
+    for (; t < ntiles; t += gridDim.x) {
+        const long long nt = t + gridDim.x;
+        raw *cur = sm + st * STAGE;
+        // the other stage was last read by the previous tile, which every
+        // thread finished before the barrier that ended the last iteration
+        if (nt < ntiles) issue(nt, sm + (st ^ 1) * STAGE);
+        cp_async_commit();  // one group per iteration, empty at the end
+#pragma unroll
+        for (int q = 0; q < HMAX; ++q)
+            if (hs[q] >= 0) cur[hs[q]] = hv[q];
+        if (nt < ntiles) fetch_halo(nt);
+        cp_async_wait_prev();  // this thread's copies of the current tile have landed
+        __syncthreads();       // ... and everyone's, with the halo
+        ip_stream_tile<DT, BC, IPP_THREADS>(cur, f, ip_tile<raw>(t, L, nx, ny), nx, ny, u0, tid);
+        __syncthreads();
+        st ^= 1;
+    }
+}
+
+int ip_sm_count() {
+    static std::atomic<int> cache[MAX_DEVICES];
+    const int dev = current_device();
+    int v = cache[dev].load(std::memory_order_acquire);
+    if (v) return v;
+    int n = 0;
+    cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+    v = n > 0 ? n : 1;
+    cache[dev].store(v, std::memory_order_release);
+    return v;
 }
 
 template <int DT>
@@ -230,30 +352,37 @@ int launch_ip(void *f, int nx, int ny, int boundary, double u0, void *ws, size_t
         set_error("%s: lattice %d x %d has too many tiles", what, nx, ny);
         return LBGB_EINVAL;
     }
-    const int vec = (ny % G::VW == 0) && aligned(f, 16);
+    const bool vec = (ny % G::VW == 0) && aligned(f, 16);
     raw *fp = static_cast<raw *>(f);
     k_ip_save<raw><<<(unsigned)recs, IP_THREADS, 0, s>>>(fp, static_cast<raw *>(ws), nx, ny);
     int rc = check_launch("k_ip_save");
     if (rc) return rc;
-    static std::atomic<bool> attr_set[MAX_DEVICES][2];
+    // variants: periodic / cavity x generic / pipelined
+    static std::atomic<bool> attr_set[MAX_DEVICES][4];
     const int dev = current_device();
-    const int variant = boundary == LBGB_PERIODIC ? 0 : 1;
-    auto go = [&](auto kernel) -> int {
+    const int variant = (boundary == LBGB_PERIODIC ? 0 : 1) + (vec ? 2 : 0);
+    const size_t smem = vec ? 2 * G::SMEM : G::SMEM;
+    auto go = [&](auto kernel, unsigned grid, int threads, const char *name) -> int {
         if (!attr_set[dev][variant].load(std::memory_order_acquire)) {
             std::lock_guard<std::mutex> lock(setup_mutex());
-            cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)G::SMEM);
+            cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
             if (e != cudaSuccess) {
-                set_error("k_ip_stream: cannot reserve %zu bytes of shared memory: %s", G::SMEM,
-                          cudaGetErrorString(e));
+                set_error("%s: cannot reserve %zu bytes of shared memory: %s", name, smem, cudaGetErrorString(e));
                 return LBGB_ECUDA;
             }
             attr_set[dev][variant].store(true, std::memory_order_release);
         }
-        kernel<<<(unsigned)tiles, IP_THREADS, G::SMEM, s>>>(fp, static_cast<const raw *>(ws), nx, ny,
-                                                            (typename Codec<DT>::real)u0, vec);
-        return check_launch("k_ip_stream");
+        kernel<<<grid, threads, smem, s>>>(fp, static_cast<const raw *>(ws), nx, ny, (typename Codec<DT>::real)u0);
+        return check_launch(name);
     };
-    return variant == 0 ? go(k_ip_stream<DT, LBGB_PERIODIC>) : go(k_ip_stream<DT, LBGB_CAVITY>);
+    if (vec) {
+        const unsigned grid = (unsigned)(tiles < ip_sm_count() ? tiles : ip_sm_count());
+        return boundary == LBGB_PERIODIC
+                   ? go(k_ip_stream_pipe<DT, LBGB_PERIODIC>, grid, IPP_THREADS, "k_ip_stream_pipe")
+                   : go(k_ip_stream_pipe<DT, LBGB_CAVITY>, grid, IPP_THREADS, "k_ip_stream_pipe");
+    }
+    return boundary == LBGB_PERIODIC ? go(k_ip_stream<DT, LBGB_PERIODIC>, (unsigned)tiles, IP_THREADS, "k_ip_stream")
+                                     : go(k_ip_stream<DT, LBGB_CAVITY>, (unsigned)tiles, IP_THREADS, "k_ip_stream");
 }
 
 int ip_check(void *f, int nx, int ny, int dtype, int boundary, const char *what) {

@@ -147,8 +147,12 @@ __global__ void k_collide(typename Codec<DT>::raw *__restrict__ f, int64_t n, in
 #pragma unroll
             for (int i = 0; i < 9; ++i) stv<raw, V>(f + i * cs + c0, out[i]);
         } else {
+            // constant indices only (a loop bound of cnt would put out[][] in local memory)
+#pragma unroll
             for (int i = 0; i < 9; ++i)
-                for (int j = 0; j < cnt; ++j) f[i * cs + c0 + j] = out[i][j];
+#pragma unroll
+                for (int j = 0; j < V; ++j)
+                    if (j < cnt) f[i * cs + c0 + j] = out[i][j];
         }
     }
 }

@@ -6,7 +6,10 @@ overwritten and streams each tile through shared memory; the cases cover
 lattices smaller than one tile (16 rows x 512 bytes of a row), exactly one
 tile, ragged tiles in both directions, rows that do not hold whole 16-byte
 vectors and a population pointer that is not 16-byte aligned (scalar loads),
-in every storage, periodic and with the cavity's walls and lid.
+in every storage, periodic and with the cavity's walls and lid.  Lattices
+whose rows hold whole 16-byte vectors take the pipelined kernel (one
+persistent block per SM, two shared-memory stages); the two largest cases
+have more tiles than the GPU has SMs, so its blocks loop over several tiles.
 """
 
 import numpy as np
@@ -23,7 +26,7 @@ STORAGES = {"f32": (_lib.F32, torch.float32), "f64": (_lib.F64, torch.float64),
             "f32dev": (_lib.F32DEV, torch.float32)}
 INT_VIEW = {2: torch.int16, 4: torch.int32, 8: torch.int64}
 SIZES = [(1, 1), (2, 2), (3, 8), (2, 16), (17, 40), (16, 128), (16, 256), (33, 129), (50, 300), (64, 1032),
-         (47, 2050), (300, 70)]
+         (47, 2050), (300, 70), (700, 1024), (1000, 520)]
 
 
 def raw_state(storage, nx, ny, seed, cuda, offset=0):
