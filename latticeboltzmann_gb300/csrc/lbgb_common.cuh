@@ -450,13 +450,47 @@ template <> struct Ieee<float> {
     static __device__ __forceinline__ float sub(float a, float b) { return __fsub_rn(a, b); }
     static __device__ __forceinline__ float mul(float a, float b) { return __fmul_rn(a, b); }
     static __device__ __forceinline__ float div(float a, float b) { return __fdiv_rn(a, b); }
+    static __device__ __forceinline__ float fma(float a, float b, float c) { return __fmaf_rn(a, b, c); }
+    static __device__ __forceinline__ float rcp(float b) { return __frcp_rn(b); }
+    // operand ranges of the reciprocal division below (no intermediate
+    // overflows or leaves the normal range)
+    static constexpr float A_MIN = 0x1p-60f, A_MAX = 0x1p60f, B_MIN = 0x1p-30f, B_MAX = 0x1p30f;
 };
 template <> struct Ieee<double> {
     static __device__ __forceinline__ double add(double a, double b) { return __dadd_rn(a, b); }
     static __device__ __forceinline__ double sub(double a, double b) { return __dsub_rn(a, b); }
     static __device__ __forceinline__ double mul(double a, double b) { return __dmul_rn(a, b); }
     static __device__ __forceinline__ double div(double a, double b) { return __ddiv_rn(a, b); }
+    static __device__ __forceinline__ double fma(double a, double b, double c) { return __fma_rn(a, b, c); }
+    static __device__ __forceinline__ double rcp(double b) { return __drcp_rn(b); }
+    static constexpr double A_MIN = 0x1p-500, A_MAX = 0x1p500, B_MIN = 0x1p-250, B_MAX = 0x1p250;
 };
+
+// The correctly rounded quotient RN(a / b) from y = RN(1/b), by Markstein's
+// correction (P. Markstein, "Computation of elementary functions on the IBM
+// RISC System/6000 processor", IBM J. Res. Develop. 34, 1990; J.-M. Muller et
+// al., Handbook of Floating-Point Arithmetic, ch. on division by FMA):
+//   q0 = RN(a y), within 1.5 ulp of a/b;
+//   r0 = a - b q0 (exact: one FMA), q1 = RN(q0 + r0 y), within one ulp;
+//   r1 = a - b q1 (exact), q2 = RN(q1 + r1 y) = RN(a / b),
+// the last step by Markstein's theorem (y within half an ulp of 1/b, q1
+// within one ulp of a/b, no underflow or overflow).  Outside the operand
+// range where that holds, and for b out of range, the IEEE division itself;
+// a = +-0 gives a y, the correctly signed zero.  Same result as Ieee<R>::div
+// for every input, at a few FMAs instead of a division per quotient.
+template <class R>
+__device__ __forceinline__ R div_by_rcp(R a, R b, R y) {
+    using O = Ieee<R>;
+    const R aa = a < R(0) ? -a : a, ab = b < R(0) ? -b : b;
+    const bool b_ok = ab >= O::B_MIN && ab <= O::B_MAX;
+    if (b_ok && aa >= O::A_MIN && aa <= O::A_MAX) {
+        const R q0 = O::mul(a, y);
+        const R q1 = O::fma(O::fma(-b, q0, a), y, q0);
+        return O::fma(O::fma(-b, q1, a), y, q1);
+    }
+    if (b_ok && a == R(0)) return O::mul(a, y);
+    return O::div(a, b);
+}
 
 // The BGK collision of the reference's native kernel, operation by operation
 // (d2q9_colliden, c/d2q9.h:121-131, with d2q9_equilibrium1, c/d2q9.h:59-81):
@@ -470,19 +504,24 @@ template <> struct Ieee<double> {
 // Every operation is rounded on its own (the x86-64 build of the reference
 // has no FMA), so FP32 and FP64 results equal the native kernel's bit for bit.
 // d2q9_equilibrium1 (c/d2q9.h:59-81) operation by operation.
+// The divisions are the IEEE ones, computed faster with the same results:
+// by a constant through its correctly rounded reciprocal (div_by_rcp), and
+// x / 2 as x * 0.5 (both are the one rounding of the exact x/2).
 template <class R>
 __device__ __forceinline__ void equilibrium_native(R rho, R ux, R uy, R (&feq)[9]) {
     using O = Ieee<R>;
-    const R w0 = O::div(O::mul(R(4), rho), R(9)), w1 = O::div(rho, R(9)), w5 = O::div(rho, R(36));
+    constexpr R r9 = R(1) / R(9), r36 = R(1) / R(36), r6 = R(1) / R(6);  // RN(1/9), RN(1/36), RN(1/6)
+    const R w0 = div_by_rcp(O::mul(R(4), rho), R(9), r9), w1 = div_by_rcp(rho, R(9), r9),
+            w5 = div_by_rcp(rho, R(36), r36);
     ux = O::mul(ux, R(3));
     uy = O::mul(uy, R(3));
     const R cu[9] = {R(0), ux, uy, -ux, -uy, O::add(ux, uy), O::add(-ux, uy), O::sub(-ux, uy), O::sub(ux, uy)};
-    const R uu = O::div(O::add(O::mul(ux, ux), O::mul(uy, uy)), R(6));
+    const R uu = div_by_rcp(O::add(O::mul(ux, ux), O::mul(uy, uy)), R(6), r6);
     feq[0] = O::mul(w0, O::sub(R(1), uu));
 #pragma unroll
     for (int i = 1; i < 9; ++i) {
         // 1 - ux is rounded as 1 + (-ux): the same IEEE result
-        const R p = O::sub(O::add(O::add(R(1), cu[i]), O::div(O::mul(cu[i], cu[i]), R(2))), uu);
+        const R p = O::sub(O::add(O::add(R(1), cu[i]), O::mul(O::mul(cu[i], cu[i]), R(0.5))), uu);
         feq[i] = O::mul(i <= 4 ? w1 : w5, p);
     }
 }
@@ -499,7 +538,8 @@ __device__ __forceinline__ void bgk_collide_native(R (&f)[9], R omega) {
     jy = O::sub(O::add(O::add(jy, f[5]), f[6]), f[7]);
     jy = O::sub(jy, f[8]);
     R feq[9];
-    equilibrium_native(rho, O::div(jx, rho), O::div(jy, rho), feq);
+    const R y = O::rcp(rho);  // RN(1/rho), shared by both quotients
+    equilibrium_native(rho, div_by_rcp(jx, rho, y), div_by_rcp(jy, rho, y), feq);
 #pragma unroll
     for (int i = 0; i < 9; ++i) f[i] = O::add(f[i], O::mul(omega, O::sub(feq[i], f[i])));
 }

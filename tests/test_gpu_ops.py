@@ -86,6 +86,49 @@ def test_collide_ragged_and_strided(cuda, n, dtype):
     assert (big[:, n:] == 0).all()
 
 
+def _same_bits(a, b):
+    """Bit-identical arrays, except that any NaN equals any NaN (the payload
+    of a generated NaN differs between the host CPU and the GPU)."""
+    na, nb = np.isnan(a), np.isnan(b)
+    np.testing.assert_array_equal(na, nb)
+    iv = np.uint32 if a.dtype == np.float32 else np.uint64
+    np.testing.assert_array_equal(a[~na].view(iv), b[~nb].view(iv))
+
+
+def _wide(rng, shape, dtype):
+    """Magnitudes from 2^-100 to 2^100 of both signs, a quarter of typical
+    populations (0.02 .. 0.22) and 1 % exact zeros."""
+    f = np.where(rng.random(shape) < 0.3, -1.0, 1.0) * np.exp2(rng.uniform(-100, 100, shape))
+    typical = 0.02 + 0.2 * rng.random(shape)
+    pick = rng.random(shape[-1]) < 0.25
+    f[..., pick] = typical[..., pick]
+    f[..., rng.random(shape[-1]) < 0.01] = 0.0
+    return f.astype(dtype)
+
+
+@pytest.mark.parametrize("dtype", [np.float32, np.float64])
+def test_native_divisions_bit_exact_over_wide_ranges(cuda, dtype):
+    """The native operators divide by 9, 36, 6 and rho through the correctly
+    rounded reciprocal with Markstein's correction inside a safe operand range
+    and by the IEEE division outside it (and x/2 as x*0.5): bit for bit the
+    IEEE results of the numpy restatement, including signed zeros, subnormal
+    and overflowing intermediates."""
+    rng = np.random.default_rng(11)
+    n = 1 << 20
+    f = _wide(rng, (9, n), dtype)
+    ref = f.copy()
+    with np.errstate(all="ignore"):
+        oracle.collide_cxx(ref, 1.3)
+    g = T(f, cuda)
+    PyLB.collide(g, 1.3)
+    _same_bits(g.cpu().numpy(), ref)
+    rho, ux, uy = (_wide(rng, (n,), dtype) for _ in range(3))
+    out = torch.empty((9, n), dtype=g.dtype, device=cuda)
+    PyLB.equilibrium(T(rho, cuda), T(ux, cuda), T(uy, cuda), out)
+    with np.errstate(all="ignore"):
+        _same_bits(out.cpu().numpy(), oracle.equilibrium_cxx(rho, ux, uy))
+
+
 @pytest.mark.parametrize("n", [1, 5, 4099])
 @pytest.mark.parametrize("dtype", [np.float64, np.float32])
 def test_collide_keep_mass_option(cuda, n, dtype):
