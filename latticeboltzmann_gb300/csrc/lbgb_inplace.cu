@@ -148,6 +148,36 @@ __device__ __forceinline__ bool ip_halo_item(int i, const IpTile &T, const IpLay
     return false;
 }
 
+// ip_halo_item for a full tile (txn = IP_TX, tyn = TY): the same items, the
+// index split by compile-time constants.
+template <class raw>
+__device__ __forceinline__ bool ip_halo_item_full(int i, const IpTile &T, const IpLayout &L, int nx, int ny,
+                                                  int &soff, long long &widx) {
+    using G = IpGeom<raw>;
+    constexpr int w = G::TY + 2, nrow = 6 * w;
+    if (i < nrow) {
+        const int hi = i / (3 * w), rem = i % (3 * w), j = rem / w, col = rem % w - 1;
+        int l = T.c + col;
+        if (l < 0) l += ny;
+        if (l >= ny) l -= ny;
+        const int tlo = (T.tx == 0 ? (int)L.ntx : T.tx) - 1, thi = (T.tx + 1 == L.ntx) ? 0 : T.tx + 1;
+        const long long rec = hi ? ((long long)thi * 2 + 0) * 3 + j : ((long long)tlo * 2 + 1) * 3 + j;
+        soff = ip_S<raw>(edge_ch(hi ? 0 : 1, j), hi ? IP_TX + 1 : 0, G::VW + col);
+        widx = rec * ny + l;
+        return true;
+    }
+    i -= nrow;
+    if (i < 6 * IP_TX) {
+        const int hi = i / (3 * IP_TX), rem = i % (3 * IP_TX), j = rem / IP_TX, r = rem % IP_TX;
+        const int ulo = (T.ty == 0 ? (int)L.nty : T.ty) - 1, uhi = (T.ty + 1 == L.nty) ? 0 : T.ty + 1;
+        const long long rec = hi ? ((long long)uhi * 2 + 0) * 3 + j : ((long long)ulo * 2 + 1) * 3 + j;
+        soff = ip_S<raw>(edge_ch(hi ? 2 : 3, j), r + 1, hi ? G::VW + G::TY : G::VW - 1);
+        widx = L.col_off + rec * nx + T.a + r;
+        return true;
+    }
+    return false;
+}
+
 // Every value of tile T from the stage s (interior and halo filled), pulled,
 // reflected at the cavity walls and lid, written back over the tile in f.
 // NT threads, a multiple of the tile width: thread tid owns column tid % TY.
@@ -268,6 +298,19 @@ k_ip_stream_pipe(typename Codec<DT>::raw *f, const typename Codec<DT>::raw *__re
 
     auto issue = [&](long long tt, raw *stage) {
         const IpTile T = ip_tile<raw>(tt, L, nx, ny);
+        const raw *src = f + (size_t)T.a * ny + T.c;
+        if (T.txn == IP_TX && T.tyn == G::TY) {
+            // full tile: the index split by constants (shifts)
+#pragma unroll
+            for (int q = 0; q < QMAX; ++q) {
+                const int i = tid + q * IPP_THREADS;
+                const int ch = i / (IP_TX * G::VPR), rem = i % (IP_TX * G::VPR), r = rem / G::VPR,
+                          v = rem % G::VPR;
+                cp_async16(stage + ip_S<raw>(ch, r + 1, G::VW + v * G::VW),
+                           src + ch * cs + (size_t)r * ny + v * G::VW);
+            }
+            return;
+        }
         const int vpr = T.tyn / G::VW, per_ch = T.txn * vpr, nvec = 9 * per_ch;
 #pragma unroll
         for (int q = 0; q < QMAX; ++q) {
@@ -275,19 +318,28 @@ k_ip_stream_pipe(typename Codec<DT>::raw *f, const typename Codec<DT>::raw *__re
             if (i < nvec) {
                 const int ch = i / per_ch, rem = i - ch * per_ch, r = rem / vpr, v = rem - r * vpr;
                 cp_async16(stage + ip_S<raw>(ch, r + 1, G::VW + v * G::VW),
-                           f + ch * cs + (size_t)(T.a + r) * ny + T.c + v * G::VW);
+                           src + ch * cs + (size_t)r * ny + v * G::VW);
             }
         }
     };
     raw hv[HMAX];
     int hs[HMAX];
     auto fetch_halo = [&](long long tt) {
-        const IpTile T = ip_tile<raw>(tt, L, nx, ny);
+        IpTile T = ip_tile<raw>(tt, L, nx, ny);
+        const bool full = T.txn == IP_TX && T.tyn == G::TY;
+        if (full) {
+            // the same items with the tile's sizes as constants (divisions
+            // by constants)
+            T.txn = IP_TX;
+            T.tyn = G::TY;
+        }
 #pragma unroll
         for (int q = 0; q < HMAX; ++q) {
             int soff;
             long long widx;
-            if (ip_halo_item<raw>(tid + q * IPP_THREADS, T, L, nx, ny, soff, widx)) {
+            const bool ok = full ? ip_halo_item_full<raw>(tid + q * IPP_THREADS, T, L, nx, ny, soff, widx)
+                                 : ip_halo_item<raw>(tid + q * IPP_THREADS, T, L, nx, ny, soff, widx);
+            if (ok) {
                 hs[q] = soff;
                 hv[q] = ws[widx];
             } else {
