@@ -562,6 +562,14 @@ def storage_comparison(args, dev, gpu_index):
 WEIGHTS = os.path.join(ROOT, "latticeboltzmann_gb300", "weights", "fno_cavity256_bf16.npz")
 
 
+def weight_files():
+    """The committed network and any further ensemble members
+    (fno_cavity256_bf16_m<k>.npz, trained on the same data and split)."""
+    import glob
+    extra = sorted(glob.glob(os.path.join(os.path.dirname(WEIGHTS), "fno_cavity256_bf16_m*.npz")))
+    return [WEIGHTS] + extra
+
+
 def warm_start(args, dev):
     """Time to steady state of the lid-driven cavity started from rest (cold)
     and from the surrogate's prediction in its Chapman-Enskog state (warm; the
@@ -577,15 +585,20 @@ def warm_start(args, dev):
     from latticeboltzmann_gb300.fno import FNO2d
     if not os.path.exists(WEIGHTS):
         return {"unavailable": "no trained weights at %s" % os.path.relpath(WEIGHTS, ROOT)}
-    net = FNO2d.load(WEIGHTS, device=dev)
-    meta = net.meta or {}
+    files = weight_files()
+    members = [FNO2d.load(p, device=dev) for p in files]
+    meta = members[0].meta or {}
     re, u = np.asarray(meta.get("held_out_re", [])), np.asarray(meta.get("held_out_u", []))
     if re.size == 0:
         return {"unavailable": "the weights file names no held-out cases"}
+    if any(list((m.meta or {}).get("held_out_re", [])) != re.tolist() for m in members[1:]):
+        return {"unavailable": "the ensemble members were not trained on the same held-out split"}
+    net = members[0] if len(members) == 1 else S.Ensemble(members)
     order = np.argsort(re)
     pick = order[np.linspace(0, len(order) - 1, min(args.warm_cases, len(order))).astype(int)]
-    out = {"weights": os.path.relpath(WEIGHTS, ROOT), "tol": 1e-7,
-           "network": {k: meta.get(k) for k in ("epochs", "train_s", "val_rel_l2_u", "val_rel_l2_rho", "samples")}}
+    keys = ("epochs", "train_s", "val_rel_l2_u", "val_rel_l2_rho", "samples", "train_seed")
+    out = {"weights": [os.path.relpath(p, ROOT) for p in files], "tol": 1e-7,
+           "network": [{k: (m.meta or {}).get(k) for k in keys} for m in members]}
     for n, sel in ((256, pick), (1024, order[:args.warm_cases_large])):
         if len(sel) == 0:
             continue

@@ -332,7 +332,15 @@ def main(argv=None):
     ap.add_argument("--study-large", type=int, default=1024, help="side of the upsampled study (0: skip)")
     ap.add_argument("--large-cases", type=int, default=4)
     ap.add_argument("--single-cases", type=int, default=8, help="held-out cavities timed one at a time")
-    ap.add_argument("--seed", type=int, default=0)
+    ap.add_argument("--seed", type=int, default=0, help="seed of the data set and its held-out split")
+    ap.add_argument("--train-seed", type=int, default=None,
+                    help="seed of the first network's initialisation and sample order (default: --seed)")
+    ap.add_argument("--members", type=int, default=1,
+                    help="networks trained one after another (seeds train-seed, train-seed + 1, ...), each with "
+                         "the full epoch / time budget; the study uses the mean of their predictions")
+    ap.add_argument("--ensemble-with", default=None,
+                    help="comma-separated trained networks (.npz) of the same data set and held-out split to add "
+                         "to the study's ensemble")
     ap.add_argument("--out", default="surrogate_out")
     ap.add_argument("--storage", default="f32dev", help="storage of the steady runs before any FP64 refinement")
     ap.add_argument("--switch-tol", type=float, default=None,
@@ -364,27 +372,48 @@ def main(argv=None):
     rng = np.random.default_rng(args.seed + 1)
     perm = rng.permutation(ok)
     val, tr = perm[:args.held_out], perm[args.held_out:]
-    net = FNO2d.load(args.init, device=dev) if args.init else FNO2d(device=dev, seed=args.seed)
-    t1 = time.perf_counter()
-    hist = train(net, data, tr, epochs=args.epochs, batch=args.batch, lr=args.lr, log=log, val_idx=val,
-                 seconds=args.train_seconds, weighting=args.weighting, rho_weight=args.rho_weight,
-                 re_exp=args.re_exp)
-    torch.cuda.synchronize()
-    t_train = time.perf_counter() - t1
-    net.save(os.path.join(args.out, "fno.npz"))
-    vu, vr = evaluate(net, data, val, with_rho=True)
-    net.save(os.path.join(args.out, "fno_bf16.npz"), bf16=True, meta={
-        "n": args.n, "samples": args.samples, "seed": args.seed, "steady": int(len(ok)),
-        "held_out_re": data["re"][val].tolist(), "held_out_u": data["u"][val].tolist(),
-        "held_out_cold_steps": data["steps"][val].tolist(), "epochs": int(hist[-1][0]) + 1 if hist else 0,
-        "train_s": t_train, "weighting": args.weighting, "rho_weight": args.rho_weight, "re_exp": args.re_exp,
-        "val_rel_l2_u": vu, "val_rel_l2_rho": vr,
-        "init_epochs": int((getattr(net, "meta", None) or {}).get("epochs", 0)) if args.init else 0,
-        "init_train_s": float((getattr(net, "meta", None) or {}).get("train_s", 0.0)) if args.init else 0.0})
-    log("training: %.1f s, val rel-L2 u %.3e rho-1 %.3e" % (t_train, vu, vr))
+    tseed = args.seed if args.train_seed is None else args.train_seed
+    nets, hists, t_train = [], [], 0.0
+    for m in range(max(1, args.members)):
+        net = FNO2d.load(args.init, device=dev) if args.init else FNO2d(device=dev, seed=tseed + m)
+        t1 = time.perf_counter()
+        hist = train(net, data, tr, epochs=args.epochs, batch=args.batch, lr=args.lr, log=log, val_idx=val,
+                     seconds=args.train_seconds, weighting=args.weighting, rho_weight=args.rho_weight,
+                     re_exp=args.re_exp, seed=tseed + m)
+        torch.cuda.synchronize()
+        t_m = time.perf_counter() - t1
+        t_train += t_m
+        tag = "" if m == 0 else "_m%d" % m
+        net.save(os.path.join(args.out, "fno%s.npz" % tag))
+        vu, vr = evaluate(net, data, val, with_rho=True)
+        net.save(os.path.join(args.out, "fno_bf16%s.npz" % tag), bf16=True, meta={
+            "n": args.n, "samples": args.samples, "seed": args.seed, "train_seed": tseed + m,
+            "steady": int(len(ok)),
+            "held_out_re": data["re"][val].tolist(), "held_out_u": data["u"][val].tolist(),
+            "held_out_cold_steps": data["steps"][val].tolist(), "epochs": int(hist[-1][0]) + 1 if hist else 0,
+            "train_s": t_m, "weighting": args.weighting, "rho_weight": args.rho_weight, "re_exp": args.re_exp,
+            "val_rel_l2_u": vu, "val_rel_l2_rho": vr,
+            "init_epochs": int((getattr(net, "meta", None) or {}).get("epochs", 0)) if args.init else 0,
+            "init_train_s": float((getattr(net, "meta", None) or {}).get("train_s", 0.0)) if args.init else 0.0})
+        log("training (network %d, seed %d): %.1f s, val rel-L2 u %.3e rho-1 %.3e" % (m, tseed + m, t_m, vu, vr))
+        nets.append(net)
+        hists.append(hist)
+    for path in [p for p in (args.ensemble_with or "").split(",") if p]:
+        other = FNO2d.load(path, device=dev)
+        if list((other.meta or {}).get("held_out_re", [])) != data["re"][val].tolist():
+            raise SystemExit("%s was not trained on this data set and held-out split" % path)
+        vu, vr = evaluate(other, data, val, with_rho=True)
+        log("ensemble member %s: val rel-L2 u %.3e rho-1 %.3e" % (path, vu, vr))
+        nets.append(other)
+    net = nets[0] if len(nets) == 1 else Ensemble(nets)
+    if len(nets) > 1:
+        vu, vr = evaluate(net, data, val, with_rho=True)
+        log("ensemble of %d: val rel-L2 u %.3e rho-1 %.3e" % (len(nets), vu, vr))
+    hist = hists[0]
     res = {"samples": args.samples, "n": args.n, "steady": int(len(ok)), "data_wall_s": data["wall"],
            "data_steps": data["steps"].tolist(), "data_re": data["re"].tolist(), "data_u": data["u"].tolist(),
-           "held_out": val.tolist(), "train_s": t_train, "history": hist}
+           "held_out": val.tolist(), "train_s": t_train, "history": hist, "members": len(nets),
+           "histories": hists}
 
     def dump():
         with open(os.path.join(args.out, "results.json"), "w") as f:
