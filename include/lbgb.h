@@ -66,6 +66,7 @@ extern "C" {
 #define LBGB_ECUDA (-3)    /* a CUDA call or launch failed */
 #define LBGB_EWORKSPACE (-4) /* workspace missing or too small */
 #define LBGB_ETIMEOUT (-5) /* a bounded device-side wait gave up */
+#define LBGB_EUNSUPPORTED (-6) /* a fused form cannot take these operands: nothing launched, use the unfused calls */
 
 /* Library version as MAJOR*10000 + MINOR*100 + PATCH. */
 LBGB_API int lbgb_version(void);
@@ -349,6 +350,20 @@ LBGB_API int lbgb_gemm_bf16(int m, int n, int k, const void *A, long long a_rs, 
                             long long a_bs, const void *B, long long b_rs, long long b_cs,
                             long long b_bs, void *C, long long c_rs, long long c_cs, long long c_bs,
                             int batch, float alpha, float beta, int c_bf16, int engine, void *stream);
+
+/* One problem of lbgb_gemm_bf16 on the TMA pipeline with the surrogate
+ * layer's bias and activation in its epilogue: C = alpha A B + beta C, then
+ * C += bias[row / rows_per_bias] (bias may be NULL) and, when c_bf16_copy is
+ * not NULL, c_bf16_copy = BF16(act ? GELU(C) : C) at the same row and column
+ * -- the values of lbgb_gemm_bf16 followed by lbgb_fno_bias_act, without the
+ * second pass over C.  A K-major (a_cs = 1), B K-major (element (k, j) at
+ * B[j * b_cs + k]), C FP32 row-major with row stride c_rs (column stride 1),
+ * C and the copy 16-byte aligned; otherwise LBGB_EUNSUPPORTED (nothing
+ * launched).  No counterpart in the reference. */
+LBGB_API int lbgb_gemm_bf16_bias_act(int m, int n, int k, const void *A, long long a_rs, long long a_cs,
+                                     const void *B, long long b_cs, void *C, long long c_rs, float alpha,
+                                     float beta, const float *bias, long long rows_per_bias, int act,
+                                     void *c_bf16_copy, void *stream);
 
 /* Synchronizes and reports whether a bounded wait in the tensor-core GEMM gave
  * up since the last reset (LBGB_ETIMEOUT).  No counterpart in the reference. */

@@ -18,7 +18,7 @@ PERIODIC, CAVITY, CAVITY_LADD = 0, 1, 2
 # lbgb_collide_ex flags
 COLLIDE_KEEP_MASS = 1
 # return codes
-OK, EINVAL, EDTYPE, ECUDA, EWORKSPACE, ETIMEOUT = 0, -1, -2, -3, -4, -5
+OK, EINVAL, EDTYPE, ECUDA, EWORKSPACE, ETIMEOUT, EUNSUPPORTED = 0, -1, -2, -3, -4, -5, -6
 
 STORAGE_CODES = {"f32": F32, "f64": F64, "f16dev": F16DEV, "bf16dev": BF16DEV, "f32dev": F32DEV}
 BOUNDARY_CODES = {"periodic": PERIODIC, "cavity": CAVITY, "cavity-ladd": CAVITY_LADD}
@@ -74,6 +74,9 @@ SIGNATURES = {
     "lbgb_gemm_bf16": (_I, [_I, _I, _I, _P, ctypes.c_longlong, ctypes.c_longlong, ctypes.c_longlong, _P,
                             ctypes.c_longlong, ctypes.c_longlong, ctypes.c_longlong, _P, ctypes.c_longlong,
                             ctypes.c_longlong, ctypes.c_longlong, _I, ctypes.c_float, ctypes.c_float, _I, _I, _P]),
+    "lbgb_gemm_bf16_bias_act": (_I, [_I, _I, _I, _P, ctypes.c_longlong, ctypes.c_longlong, _P, ctypes.c_longlong,
+                                     _P, ctypes.c_longlong, ctypes.c_float, ctypes.c_float, _P, ctypes.c_longlong,
+                                     _I, _P, _P]),
     "lbgb_gemm_status": (_I, [_I]),
     "lbgb_fno_to_bf16": (_I, [_P, _P, ctypes.c_longlong, _P]),
     "lbgb_fno_bias_act": (_I, [_P, _P, _P, _P, _P, _I, ctypes.c_longlong, _I, _P]),

@@ -19,6 +19,7 @@
 #include <cuda.h>
 #include <stdio.h>
 
+#include "lbgb_act.cuh"
 #include "lbgb_common.cuh"
 
 namespace lbgb {
@@ -500,6 +501,17 @@ __device__ __forceinline__ void tc_ld16(uint32_t taddr, uint32_t (&v)[16]) {
     asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 }
 
+// Optional epilogue of a surrogate layer, applied by the TMA pipeline to a
+// row-major FP32 C of one problem: C += bias[row / rows] after alpha/beta,
+// and vb = BF16(act ? GELU(C) : C) at the same offset -- what lbgb_fno_bias_act
+// does as a separate pass over C.
+struct Epi {
+    const float *bias = nullptr;
+    long long rows = 1;
+    int act = 0;
+    __nv_bfloat16 *vb = nullptr;
+};
+
 // AMN: A is M-major (m contiguous, A(m, k) = A[k * a_cs + m]; the
 // channel-major activations of the pointwise layers).  Its tile is then two
 // 64-element-wide boxes per K block (m0 and m0 + 64), each 64 k rows of 128
@@ -510,7 +522,7 @@ template <int NT, typename OUT, bool AMN = false>
 __global__ void __launch_bounds__(TP_THREADS, 2)
 k_gemm_tma(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB, int a3d, int b3d, int M,
            int N, int K, int batch, OUT *__restrict__ C, long long c_rs, long long c_cs, long long c_bs, float alpha,
-           float beta) {
+           float beta, Epi ep) {
     using S = TmaShape<NT>;
     constexpr int STAGES = S::STAGES;
     extern __shared__ __align__(1024) unsigned char dsm[];
@@ -666,11 +678,32 @@ k_gemm_tma(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUte
                         const int row = m0 + 2 * i + (lane >> 4);
                         old[i] = (beta != 0.f && row < M && col < N) ? load_out(Cz + (long long)row * c_rs + col) : 0.f;
                     }
+                    if (ep.bias || ep.vb) {
+                        // the block's 32 rows meet at most one bias boundary
+                        // when rows >= 32: one division per block
+                        const long long b_lo = ep.rows >= 32 ? m0 / ep.rows : 0;
+                        const long long edge = (b_lo + 1) * ep.rows;
 #pragma unroll
-                    for (int i = 0; i < 16; ++i) {
-                        const int r = 2 * i + (lane >> 4), row = m0 + r;
-                        if (row < M && col < N)
-                            store_out(Cz + (long long)row * c_rs + col, alpha * ostage[r * 17 + j] + beta * old[i]);
+                        for (int i = 0; i < 16; ++i) {
+                            const int r = 2 * i + (lane >> 4), row = m0 + r;
+                            if (row < M && col < N) {
+                                float val = alpha * ostage[r * 17 + j] + beta * old[i];
+                                if (ep.bias) {
+                                    const long long bi = ep.rows >= 32 ? b_lo + (row >= edge) : row / ep.rows;
+                                    val = val + ep.bias[bi];
+                                }
+                                store_out(Cz + (long long)row * c_rs + col, val);
+                                if (ep.vb)
+                                    ep.vb[(long long)row * c_rs + col] = __float2bfloat16_rn(ep.act ? gelu_f(val) : val);
+                            }
+                        }
+                    } else {
+#pragma unroll
+                        for (int i = 0; i < 16; ++i) {
+                            const int r = 2 * i + (lane >> 4), row = m0 + r;
+                            if (row < M && col < N)
+                                store_out(Cz + (long long)row * c_rs + col, alpha * ostage[r * 17 + j] + beta * old[i]);
+                        }
                     }
                     __syncwarp();
                 } else {
@@ -772,7 +805,7 @@ template <int NT, typename OUT>
 static int launch_gemm_tma_nt(int m, int n, int k, const __nv_bfloat16 *a, long long a_rs, long long a_cs,
                               long long a_bs, const __nv_bfloat16 *b, long long b_cs, long long b_bs, OUT *C,
                               long long c_rs, long long c_cs, long long c_bs, int batch, float alpha, float beta,
-                              cudaStream_t s) {
+                              const Epi &ep, cudaStream_t s) {
     using S = TmaShape<NT>;
     CUtensorMap ma, mb;
     int a3 = 0, b3 = 0;
@@ -800,10 +833,10 @@ static int launch_gemm_tma_nt(int m, int n, int k, const __nv_bfloat16 *a, long 
     const int grid = (int)(tiles < slots ? tiles : slots);
     if (amn)
         k_gemm_tma<NT, OUT, true><<<grid, TP_THREADS, S::SMEM, s>>>(ma, mb, a3, b3, m, n, k, batch, C, c_rs, c_cs, c_bs,
-                                                                    alpha, beta);
+                                                                    alpha, beta, ep);
     else
         k_gemm_tma<NT, OUT, false><<<grid, TP_THREADS, S::SMEM, s>>>(ma, mb, a3, b3, m, n, k, batch, C, c_rs, c_cs,
-                                                                     c_bs, alpha, beta);
+                                                                     c_bs, alpha, beta, ep);
     return check_launch("k_gemm_tma");
 }
 
@@ -811,7 +844,7 @@ template <typename OUT>
 static int launch_gemm_tma(int m, int n, int k, const __nv_bfloat16 *a, long long a_rs, long long a_cs, long long a_bs,
                            const __nv_bfloat16 *b, long long b_rs, long long b_cs, long long b_bs, OUT *C,
                            long long c_rs, long long c_cs, long long c_bs, int batch, float alpha, float beta,
-                           bool forced, cudaStream_t s) {
+                           bool forced, cudaStream_t s, const Epi &ep = Epi()) {
     if ((a_cs != 1 && a_rs != 1) || b_rs != 1 || k <= 0) return 1;
     // automatic choice: M-major A with more than 64 output columns stays on
     // the staged kernel -- there the output (the 128-channel projection:
@@ -820,12 +853,12 @@ static int launch_gemm_tma(int m, int n, int k, const __nv_bfloat16 *a, long lon
     if (!forced && a_cs != 1 && n > 64) return 1;
     if (n <= 32)
         return launch_gemm_tma_nt<32>(m, n, k, a, a_rs, a_cs, a_bs, b, b_cs, b_bs, C, c_rs, c_cs, c_bs, batch, alpha,
-                                      beta, s);
+                                      beta, ep, s);
     if (n <= 64)
         return launch_gemm_tma_nt<64>(m, n, k, a, a_rs, a_cs, a_bs, b, b_cs, b_bs, C, c_rs, c_cs, c_bs, batch, alpha,
-                                      beta, s);
+                                      beta, ep, s);
     return launch_gemm_tma_nt<128>(m, n, k, a, a_rs, a_cs, a_bs, b, b_cs, b_bs, C, c_rs, c_cs, c_bs, batch, alpha,
-                                   beta, s);
+                                   beta, ep, s);
 }
 
 template <typename OUT>
@@ -907,6 +940,34 @@ extern "C" int lbgb_gemm_bf16(int m, int n, int k, const void *A, long long a_rs
                            c_cs, c_bs, batch, alpha, beta, engine, s);
     return launch_gemm(m, n, k, a, a_rs, a_cs, a_bs, b, b_rs, b_cs, b_bs, static_cast<float *>(C), c_rs, c_cs, c_bs,
                        batch, alpha, beta, engine, s);
+}
+
+extern "C" int lbgb_gemm_bf16_bias_act(int m, int n, int k, const void *A, long long a_rs, long long a_cs,
+                                       const void *B, long long b_cs, void *C, long long c_rs, float alpha, float beta,
+                                       const float *bias, long long rows_per_bias, int act, void *c_bf16_copy,
+                                       void *stream) {
+    if (m <= 0 || n <= 0 || k <= 0 || rows_per_bias <= 0 || !A || !B || !C) {
+        set_error("lbgb_gemm_bf16_bias_act: bad sizes or operands (m=%d n=%d k=%d rows_per_bias=%lld)", m, n, k,
+                  rows_per_bias);
+        return LBGB_EINVAL;
+    }
+    if (a_cs != 1 || c_rs < n || c_rs <= 1 || !aligned(C, 16) || (c_bf16_copy && !aligned(c_bf16_copy, 16))) {
+        set_error("lbgb_gemm_bf16_bias_act: needs a K-major A and a row-major C (16-byte aligned)");
+        return LBGB_EUNSUPPORTED;
+    }
+    Epi ep;
+    ep.bias = bias;
+    ep.rows = rows_per_bias;
+    ep.act = act;
+    ep.vb = static_cast<__nv_bfloat16 *>(c_bf16_copy);
+    const int rc = launch_gemm_tma(m, n, k, static_cast<const __nv_bfloat16 *>(A), a_rs, a_cs, 0,
+                                   static_cast<const __nv_bfloat16 *>(B), 1, b_cs, 0, static_cast<float *>(C), c_rs, 1,
+                                   0, 1, alpha, beta, true, (cudaStream_t)stream, ep);
+    if (rc > 0) {
+        set_error("lbgb_gemm_bf16_bias_act: the TMA pipeline cannot address these operands");
+        return LBGB_EUNSUPPORTED;
+    }
+    return rc;
 }
 
 extern "C" int lbgb_gemm_status(int reset) {

@@ -198,6 +198,20 @@ class FNO2d:
         _lib.call("lbgb_gemm_bf16", m, n, k, A, a[0], a[1], a[2], B, b[0], b[1], b[2], C, c[0], c[1], c[2], batch,
                   1.0, beta, int(bf16_out), self.engine, self._s())
 
+    def _gemm_bias_act(self, m, n, k, A, a, B, b_cs, C, c_rs, bias, rows_per_bias, channels, cols, act, vb):
+        """C = A B + C, C += bias per channel (rows_per_bias rows of C each),
+        vb = BF16(act(C)): one fused launch on the tensor-core engine when the
+        TMA pipeline takes the operands, else the GEMM and lbgb_fno_bias_act."""
+        s = self._s()
+        if self.engine == ENGINE_TENSOR_CORES:
+            rc = _lib.load().lbgb_gemm_bf16_bias_act(m, n, k, A, a[0], a[1], B, b_cs, C, c_rs, 1.0, 1.0, bias,
+                                                     rows_per_bias, act, vb, s)
+            if rc != _lib.EUNSUPPORTED:
+                _lib.check(rc, "lbgb_gemm_bf16_bias_act")
+                return
+        self._gemm(m, n, k, A, (a[0], a[1], 0), B, (1, b_cs, 0), C, (c_rs, 1, 0), beta=1.0)
+        _lib.call("lbgb_fno_bias_act", C, bias, None, None, vb, channels, cols, act, s)
+
     def _splits(self, K):
         """Split count of a weight gradient over K pixels: the largest power of
         two up to ``max_splits`` that divides K and leaves >= 256 per split."""
@@ -301,11 +315,11 @@ class FNO2d:
             # inverse along H: Z (C, B, H, 2m)
             self._gemm(H, m2, q2, _ptr(G), (1, H, 0), _ptr(ws["Ym"]), (m2, 1, q2 * m2), _ptr(ws["Z"]),
                        (m2, 1, H * m2), batch=C * B, bf16_out=True)
-            # inverse along W, added onto the pointwise branch
-            self._gemm(C * B * H, W, m2, _ptr(ws["Z"]), (m2, 1, 0), _ptr(iw), (1, m2, 0), _ptr(z), (W, 1, 0),
-                       beta=1.0)
-            _lib.call("lbgb_fno_bias_act", _ptr(z), _ptr(self.flat, self.offsets["b%d" % l]), None, None,
-                      _ptr(ws["vb"][l + 1]), C, N, int(l < self.layers - 1), s)
+            # inverse along W, added onto the pointwise branch, then bias and
+            # activation (in the GEMM's epilogue where the TMA pipeline runs)
+            self._gemm_bias_act(C * B * H, W, m2, _ptr(ws["Z"]), (m2, 1), _ptr(iw), m2, _ptr(z), W,
+                                _ptr(self.flat, self.offsets["b%d" % l]), B * H, C, N, int(l < self.layers - 1),
+                                _ptr(ws["vb"][l + 1]))
         # projection
         h = ws["h"]
         self._gemm(N, self.hidden, C, _ptr(ws["vb"][self.layers]), (1, N, 0), _ptr(pb, self.offsets["Q1"]),

@@ -154,3 +154,52 @@ def test_tma_engine_rejects_other_layouts(cuda):
     C = torch.zeros(64, 32, device=cuda)
     with pytest.raises(ValueError):  # B is N-major here
         _call(64, 32, 16, A, (16, 1, 0), B, (32, 1, 0), C, (32, 1, 0), 1, 1.0, 0.0, 3)
+
+
+@pytest.mark.parametrize("rows_per_bias", [4096, 300, 16])
+@pytest.mark.parametrize("act", [0, 1])
+def test_gemm_bias_act_equals_gemm_then_bias_act(cuda, rows_per_bias, act):
+    """The TMA pipeline's fused bias + activation epilogue (one Fourier layer:
+    C = A B + C, C += bias per channel block of rows, BF16 copy of GELU(C))
+    gives the values of lbgb_gemm_bf16 followed by lbgb_fno_bias_act: C bit
+    for bit, the BF16 copy within one BF16 rounding step."""
+    m, n, k = 4096, 64, 24
+    g = torch.Generator(device="cpu").manual_seed(rows_per_bias + act)
+    a = torch.randn(m, k, generator=g).to(torch.bfloat16).to(cuda)                   # K-major A
+    bt = torch.randn(n, k, generator=g).to(torch.bfloat16).to(cuda)                  # B^T stored: K-major B
+    c0 = torch.randn(m, n, generator=g).to(cuda)
+    nb = (m + rows_per_bias - 1) // rows_per_bias
+    bias = torch.randn(nb, generator=g).to(cuda)
+    s = torch.cuda.current_stream().cuda_stream
+    # unfused: GEMM with beta = 1, then the bias pass per row block (channels x cols)
+    c1 = c0.clone()
+    _lib.call("lbgb_gemm_bf16", m, n, k, a.data_ptr(), k, 1, 0, bt.data_ptr(), 1, k, 0, c1.data_ptr(), n, 1, 0, 1,
+              1.0, 1.0, 0, 3, s)
+    vb1 = torch.empty(m, n, dtype=torch.bfloat16, device=cuda)
+    if m % rows_per_bias == 0:
+        _lib.call("lbgb_fno_bias_act", c1.data_ptr(), bias.data_ptr(), None, None, vb1.data_ptr(), nb,
+                  rows_per_bias * n, act, s)
+    else:
+        # ragged last block: the bias pass row block by row block
+        for i in range(nb):
+            r0, r1 = i * rows_per_bias, min(m, (i + 1) * rows_per_bias)
+            _lib.call("lbgb_fno_bias_act", c1[r0:r1].data_ptr(), bias[i:].data_ptr(), None, None,
+                      vb1[r0:r1].data_ptr(), 1, (r1 - r0) * n, act, s)
+    c2 = c0.clone()
+    vb2 = torch.empty(m, n, dtype=torch.bfloat16, device=cuda)
+    _lib.call("lbgb_gemm_bf16_bias_act", m, n, k, a.data_ptr(), k, 1, bt.data_ptr(), k, c2.data_ptr(), n, 1.0, 1.0,
+              bias.data_ptr(), rows_per_bias, act, vb2.data_ptr(), s)
+    _lib.call("lbgb_gemm_status", 1)
+    assert torch.equal(c1, c2)
+    d = (vb1.float() - vb2.float()).abs()
+    assert (d <= 2 ** -7 * vb1.float().abs().clamp_min(2 ** -100)).all()
+
+
+def test_gemm_bias_act_rejects_other_layouts(cuda):
+    m, n, k = 256, 32, 16
+    a = torch.zeros(k, m, dtype=torch.bfloat16, device=cuda)  # M-major A
+    bt = torch.zeros(n, k, dtype=torch.bfloat16, device=cuda)
+    c = torch.zeros(m, n, device=cuda)
+    rc = _lib.load().lbgb_gemm_bf16_bias_act(m, n, k, a.data_ptr(), 1, m, bt.data_ptr(), k, c.data_ptr(), n, 1.0, 0.0,
+                                             None, 1, 0, None, torch.cuda.current_stream().cuda_stream)
+    assert rc == _lib.EUNSUPPORTED
