@@ -214,20 +214,25 @@ class Lattice:
         return out
 
     # ------------------------------------------------------------------ host-resident populations
-    def step_host(self, f, n=1, blocks=48, check=True):
+    def step_host(self, f, n=1, blocks=48, check=True, copy_streams=1):
         """Advance populations that live in host memory by ``n`` steps, in place.
 
         ``f``: a pinned, contiguous ``(9, nx, ny)`` host tensor of the storage's
         dtype (f32 or f64 storage).  Each step copies f to the device, steps
         and copies the result back -- what the reference's drivers do with
-        their host array every step -- but by blocks of rows on three streams,
-        so that the upload of block j+1, the update of block j and the
-        download of block j-1 overlap (the host link carries both directions
-        at once).  Block 0 is updated last: its rows read the last row across
-        the periodic seam (and the lid density does at the corners).  The
-        device state ends up holding the same populations as ``f``.  At
-        8192^2 FP32, 32-64 blocks run at 15.3 ms per step (8 blocks: 18.0 ms;
-        the transfers alone take 14.1 ms at the link's two-way rate).
+        their host array every step -- but by blocks of rows on separate
+        streams, so that the upload of block j+1, the update of block j and
+        the download of block j-1 overlap (the host link carries both
+        directions at once).  Block 0 is updated last: its rows read the last
+        row across the periodic seam (and the lid density does at the
+        corners).  The device state ends up holding the same populations as
+        ``f``.  At 8192^2 FP32, 32-64 blocks run at 15.3 ms per step (8
+        blocks: 18.0 ms; the transfers alone take 14.1 ms at the link's
+        two-way rate with one copy stream per direction).
+
+        copy_streams: streams per direction; block j is copied on stream
+        j mod copy_streams, so that several copy engines can serve one
+        direction.
 
         check=True (default): wait for the last download and raise
         LBGBTimeout if a bounded device-side wait of a step gave up, so that
@@ -243,39 +248,48 @@ class Lattice:
                 self.state.dtype, (9, self.nx, self.ny)))
         nx, ny = self.nx, self.ny
         nb = max(1, min(int(blocks), nx))
+        k = max(1, int(copy_streams))
         edges = [nx * j // nb for j in range(nb + 1)]
-        if not hasattr(self, "_hstreams"):
-            self._hstreams = (torch.cuda.Stream(self.device), torch.cuda.Stream(self.device))
+        if getattr(self, "_hstreams_k", 0) != k:
+            self._hstreams = ([torch.cuda.Stream(self.device) for _ in range(k)],
+                              [torch.cuda.Stream(self.device) for _ in range(k)])
+            self._hstreams_k = k
         s_in, s_out = self._hstreams
         s_cmp = torch.cuda.current_stream(self.device)
         order = list(range(1, nb)) + [0]
         ev = lambda: torch.cuda.Event()
         for _ in range(int(n)):
             a, b = self._buf[self._cur], self._buf[1 - self._cur]
-            s_in.wait_stream(s_cmp)
-            s_in.wait_stream(s_out)
+            # this step's uploads overwrite rows that the last step read
+            # (device buffer) and wrote (host array)
+            for si in s_in:
+                si.wait_stream(s_cmp)
+                for so in s_out:
+                    si.wait_stream(so)
             ev_in = []
             for j in range(nb):
+                st = s_in[j % k]
                 _lib.call("lbgb_copy_rows", a.data_ptr(), f.data_ptr(), nx, ny, edges[j], edges[j + 1], self.code,
-                          s_in.cuda_stream)
+                          st.cuda_stream)
                 e = ev()
-                e.record(s_in)
+                e.record(st)
                 ev_in.append(e)
-            ev_out = []
             for j in order:
                 # rows of blocks j-1, j, j+1 (with wrap) must be on the device
-                need = max(j + 1 if j + 1 < nb else 0, j, j - 1 if j > 0 else nb - 1)
-                s_cmp.wait_event(ev_in[need])
+                for need in {j, j + 1 if j + 1 < nb else 0, j - 1 if j > 0 else nb - 1}:
+                    s_cmp.wait_event(ev_in[need])
                 _lib.call("lbgb_step_fused_rows", a.data_ptr(), b.data_ptr(), nx, ny, edges[j], edges[j + 1],
                           self.bcode, self.omega, self.u0, self.code, s_cmp.cuda_stream)
                 e = ev()
                 e.record(s_cmp)
-                s_out.wait_event(e)
+                so = s_out[j % k]
+                so.wait_event(e)
                 _lib.call("lbgb_copy_rows", f.data_ptr(), b.data_ptr(), nx, ny, edges[j], edges[j + 1], self.code,
-                          s_out.cuda_stream)
+                          so.cuda_stream)
             self._cur = 1 - self._cur
             self.steps_taken += 1
-        s_cmp.wait_stream(s_out)
+        for so in s_out:
+            s_cmp.wait_stream(so)
         if check:
             _lib.device_status()
         return f

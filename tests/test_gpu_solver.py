@@ -119,8 +119,10 @@ def test_full_size_cavity_properties(cuda, storage):
 @pytest.mark.parametrize("storage", ["f32", "f64"])
 @pytest.mark.parametrize("boundary", ["cavity", "cavity-ladd", "periodic"])
 @pytest.mark.parametrize("nx,ny,blocks", [(64, 96, 5), (37, 40, 16), (3, 8, 16), (130, 2048, 7), (8, 8, 1)])
-def test_step_host_equals_device_step(cuda, storage, boundary, nx, ny, blocks):
-    """The pipelined host step (row blocks, three streams) gives the populations
+@pytest.mark.parametrize("copy_streams", [1, 2, 4])
+def test_step_host_equals_device_step(cuda, storage, boundary, nx, ny, blocks, copy_streams):
+    """The pipelined host step (row blocks; uploads, updates and downloads on
+    separate streams, one or several per copy direction) gives the populations
     of the fused device step bit for bit, and leaves the device state equal."""
     rng = np.random.default_rng(nx + ny)
     f0 = oracle.equilibrium(1 + 0.01 * rng.standard_normal((nx, ny)), 0.03 * rng.standard_normal((nx, ny)),
@@ -130,7 +132,7 @@ def test_step_host_equals_device_step(cuda, storage, boundary, nx, ny, blocks):
     b = PyLB.Lattice(nx, ny, 1.3, boundary=boundary, u0=0.07, storage=storage, device=cuda).load(torch.from_numpy(f0))
     host = torch.from_numpy(f0).to(dt).pin_memory()
     a.step(3)
-    b.step_host(host, n=3, blocks=blocks)
+    b.step_host(host, n=3, blocks=blocks, copy_streams=copy_streams)
     torch.cuda.synchronize()
     assert torch.equal(host, a.state.cpu())
     assert torch.equal(b.state, a.state)
