@@ -67,6 +67,8 @@ def parse(argv=None):
     p.add_argument("--omega", type=float, default=1.7)
     p.add_argument("--u0", type=float, default=0.1)
     p.add_argument("--e2e-steps", type=int, default=5)
+    p.add_argument("--copy-streams", type=int, default=1,
+                   help="streams per copy direction of the end-to-end host step (and of its link bound)")
     p.add_argument("--cpu-seconds", type=float, default=10.0, help="bound of the CPU-baseline sample")
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-e2e", action="store_true")
@@ -418,7 +420,7 @@ def run_ours(args):
             if host_path:
                 # upload, update and download pipelined by row blocks (public
                 # API); the device status is checked once after the loop
-                lat.step_host(host, check=False)
+                lat.step_host(host, check=False, copy_streams=args.copy_streams)
             else:
                 lat.load(host)
                 lat.step(1)
@@ -437,15 +439,17 @@ def run_ours(args):
         d.barrier()
         e_mlups, _ = aggregate_mlups(lat.cells, args.e2e_steps, el, d, dev)
         nbytes = host.numel() * host.element_size()
-        link_s = host_link_seconds(host, dev)
+        link_s = host_link_seconds(host, dev, streams=args.copy_streams)
         bound = lat.cells / link_s / 1e6
         e2e = {"value": round(e_mlups, 3), "unit": UNIT, "h2d_bytes_per_step": nbytes, "d2h_bytes_per_step": nbytes,
                "steps": args.e2e_steps,
-               "path": "Lattice.step_host(pinned host): row blocks uploaded, updated and downloaded on three streams"
+               "path": ("Lattice.step_host(pinned host): row blocks uploaded, updated and downloaded, %d copy "
+                        "stream(s) per direction" % args.copy_streams)
                if host_path else "Lattice.load(pinned host) + Lattice.step + Lattice.populations(out=pinned host)",
                "link": {"two_way_gbs": round(2 * nbytes / link_s / 1e9, 1), "bound": round(bound, 1),
                         "frac": round(e_mlups / d.world / bound, 4),
-                        "how": "one step's upload and download as two concurrent copy-engine copies, no compute"}}
+                        "how": "one step's upload and download as concurrent copy-engine copies on %d stream(s) "
+                               "per direction, no compute" % args.copy_streams}}
         del host
 
     if d.rank != 0:
@@ -667,26 +671,32 @@ def operator_path(args, dev):
                     "float32 (%dx%d)" % (nx, ny)}
 
 
-def host_link_seconds(host, dev, reps=3):
+def host_link_seconds(host, dev, reps=3, streams=1):
     """Seconds for one step's host traffic with nothing else running: the upload
-    of ``host`` and a download of the same size as two concurrent copies on
-    their own streams -- the ceiling of any per-step host round trip."""
+    of ``host`` and a download of the same size as concurrent copies, each
+    direction split over ``streams`` streams -- the ceiling of any per-step
+    host round trip with that many copy streams."""
     import torch
     scratch = torch.empty(host.shape, dtype=host.dtype, device=dev)
     dev_buf = torch.empty_like(scratch)
     back = torch.empty(host.shape, dtype=host.dtype, pin_memory=True)
-    s_up, s_down = torch.cuda.Stream(dev), torch.cuda.Stream(dev)
+    k = max(1, int(streams))
+    ups = [torch.cuda.Stream(dev) for _ in range(k)]
+    downs = [torch.cuda.Stream(dev) for _ in range(k)]
+    parts = list(zip(torch.chunk(scratch.view(-1), k), torch.chunk(host.view(-1), k),
+                     torch.chunk(back.view(-1), k), torch.chunk(dev_buf.view(-1), k)))
     cur = torch.cuda.current_stream(dev)
 
     def once():
-        s_up.wait_stream(cur)
-        s_down.wait_stream(cur)
-        with torch.cuda.stream(s_up):
-            scratch.copy_(host, non_blocking=True)
-        with torch.cuda.stream(s_down):
-            back.copy_(dev_buf, non_blocking=True)
-        cur.wait_stream(s_up)
-        cur.wait_stream(s_down)
+        for su, sd, (sc, h, bk, db) in zip(ups, downs, parts):
+            su.wait_stream(cur)
+            sd.wait_stream(cur)
+            with torch.cuda.stream(su):
+                sc.copy_(h, non_blocking=True)
+            with torch.cuda.stream(sd):
+                bk.copy_(db, non_blocking=True)
+        for st in ups + downs:
+            cur.wait_stream(st)
 
     once()
     torch.cuda.synchronize(dev)
