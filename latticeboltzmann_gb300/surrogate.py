@@ -138,9 +138,6 @@ def train(net, data, idx, epochs=100, batch=16, lr=1e-3, lr_min=1e-5, log=None, 
             cur = lr_min + 0.5 * (lr - lr_min) * (1 + math.cos(math.pi * min(k, total) / total))
             net.adam(cur)
             k += 1
-        if seconds is not None and ep == 0:
-            torch.cuda.synchronize(device)
-            t_ep1 = time.perf_counter()
         if seconds is not None and ep == 2:
             torch.cuda.synchronize(device)
             per_epoch = (time.perf_counter() - t_ep1) / 2
@@ -159,6 +156,10 @@ def train(net, data, idx, epochs=100, batch=16, lr=1e-3, lr_min=1e-5, log=None, 
             tl = float(acc) / steps_per_epoch
             hist.append((ep, tl, vl, vr))
             log("epoch %d train %.3e val rel-L2 u %.3e rho-1 %.3e lr %.2e" % (ep, tl, vl, vr, cur))
+        if seconds is not None and ep == 0:
+            # after epoch 0's one-time set-up and its validation pass
+            torch.cuda.synchronize(device)
+            t_ep1 = time.perf_counter()
         ep += 1
     return hist
 
