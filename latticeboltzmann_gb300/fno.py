@@ -95,6 +95,8 @@ class FNO2d:
         if max_splits < 1 or max_splits & (max_splits - 1):
             raise ValueError("max_splits must be a power of two")
         self.max_splits = int(max_splits)  # weight gradients: split-K count over the pixels
+        # tensor-core engine: bias + activation in the epilogue of each layer's last GEMM
+        self.fused_epilogue = True
         shapes = [("P", (width, cin)), ("pb", (width,))]
         for l in range(layers):
             shapes += [("W%d" % l, (width, width)), ("b%d" % l, (width,)),
@@ -203,7 +205,7 @@ class FNO2d:
         vb = BF16(act(C)): one fused launch on the tensor-core engine when the
         TMA pipeline takes the operands, else the GEMM and lbgb_fno_bias_act."""
         s = self._s()
-        if self.engine == ENGINE_TENSOR_CORES:
+        if self.engine == ENGINE_TENSOR_CORES and self.fused_epilogue:
             rc = _lib.load().lbgb_gemm_bf16_bias_act(m, n, k, A, a[0], a[1], B, b_cs, C, c_rs, 1.0, 1.0, bias,
                                                      rows_per_bias, act, vb, s)
             if rc != _lib.EUNSUPPORTED:
@@ -464,10 +466,13 @@ def main(argv=None):
                     help="tensor: TMA pipeline where both operands are K-major, else the staged kernel; "
                          "staged: the staged tcgen05 kernel for every product; cuda: CUDA cores")
     ap.add_argument("--max-splits", type=int, default=1024, help="split-K count cap of the weight gradients")
+    ap.add_argument("--unfused", action="store_true",
+                    help="bias and activation as a separate pass after the layer's last GEMM (for comparison)")
     args = ap.parse_args(argv)
     dev = torch.device("cuda", torch.cuda.current_device())
     engine = {"tensor": ENGINE_TENSOR_CORES, "staged": ENGINE_STAGED, "cuda": ENGINE_CUDA_CORES}[args.engine]
     net = FNO2d(device=dev, engine=engine, max_splits=args.max_splits)
+    net.fused_epilogue = not args.unfused
     rng = np.random.default_rng(0)
     re = np.exp(rng.uniform(math.log(RE_RANGE[0]), math.log(RE_RANGE[1]), args.batch))
     a = net.inputs(re, rng.uniform(*U_RANGE, args.batch), args.n, args.n)
@@ -488,6 +493,7 @@ def main(argv=None):
     torch.cuda.synchronize(dev)
     fwd = (time.perf_counter() - t0) / max(args.steps, 1)
     print(json.dumps({"batch": args.batch, "n": args.n, "engine": args.engine, "max_splits": net.max_splits,
+                      "fused_epilogue": net.fused_epilogue,
                       "train_step_ms": round(train * 1e3, 3),
                       "forward_ms": round(fwd * 1e3, 3), "params": int(sum(np.prod(s) for s in net.shapes.values()))}))
 
