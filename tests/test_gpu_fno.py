@@ -159,3 +159,26 @@ def test_bf16_weights_file_gives_the_same_inference(cuda, tmp_path):
     assert net2.meta == {"held_out_re": [12.5]}
     for x, y in zip(net.predict([40.0], [0.07], 24, 32), net2.predict([40.0], [0.07], 24, 32)):
         assert torch.equal(x, y)
+
+
+def test_committed_ensemble(cuda):
+    """The committed networks were trained on one data set and held-out split
+    (their metadata name the same held-out cases), and the ensemble predicts
+    the mean of its members."""
+    import os
+    from latticeboltzmann_gb300 import surrogate as S
+    wdir = os.path.join(os.path.dirname(F.__file__), "weights")
+    paths = [os.path.join(wdir, f) for f in ("fno_cavity256_bf16.npz", "fno_cavity256_bf16_m1.npz",
+                                              "fno_cavity256_bf16_m2.npz")]
+    nets = [F.FNO2d.load(p, device=cuda) for p in paths]
+    held = [n.meta["held_out_re"] for n in nets]
+    assert all(h == held[0] for h in held) and len(held[0]) == 64
+    assert len({n.meta.get("train_seed", 0) for n in nets}) == 3
+    ens = S.load_networks(",".join(paths), cuda)
+    re, u = held[0][:3], nets[0].meta["held_out_u"][:3]
+    mean = None
+    for n in nets:
+        p = [x.clone() for x in n.predict(re, u, 64, 64)]
+        mean = p if mean is None else [m + x for m, x in zip(mean, p)]
+    for got, m in zip(ens.predict(re, u, 64, 64), mean):
+        assert torch.allclose(got, m / 3, rtol=0, atol=1e-6)
