@@ -12,9 +12,10 @@
 // exactly those edge values of every tile into a small workspace before any
 // tile is overwritten, and the second kernel takes its halo from there.
 //
-// Bytes per cell: 72 (FP32: 36 read, 36 written) plus the edge records, about
-// 15 % at the default tile (a column record's scattered reads fetch whole
-// lines); the stream-into-scratch-and-copy-back it replaces moved 144.
+// Bytes per cell: 72 (FP32: 36 read, 36 written) plus the edge records (the
+// pipelined kernel streams runs of tiles along y in order and needs column
+// records only at run ends); the stream-into-scratch-and-copy-back it
+// replaces moved 144.
 // Results equal the out-of-place kernels' bit for bit (same decode, same lid
 // arithmetic, same encode).
 #include <limits.h>
@@ -47,30 +48,37 @@ __host__ __device__ constexpr int edge_ch(int side, int j) {
                      : (j == 0 ? CN : j == 1 ? CNE : CNW);
 }
 
-// Workspace: row records [ntx][2][3][ny] (first / last row of each x tile),
-// then, from a 16-byte boundary, column records [nty][2][3][nx].
+// Tiles are streamed in runs of `run` consecutive tiles along y, one run by
+// one block in order (the generic kernel: runs of one tile).  Workspace: row
+// records [ntx][2][3][ny] (first / last row of each x tile), then, from a
+// 16-byte boundary, column records [nseg][2][3][nx] (first / last column of
+// each run; with runs of one tile, of each tile).
 struct IpLayout {
-    long long ntx, nty, col_off, total;  // counts and offsets in elements
+    long long ntx, nty, nseg, col_off, total;  // counts and offsets in elements
+    int run;
 };
 
 template <class raw>
-__host__ __device__ inline IpLayout ip_layout(int nx, int ny) {
+__host__ __device__ inline IpLayout ip_layout(int nx, int ny, int run = 1) {
     using G = IpGeom<raw>;
     IpLayout L;
+    L.run = run;
     L.ntx = (nx + IP_TX - 1) / IP_TX;
     L.nty = (ny + G::TY - 1) / G::TY;
+    L.nseg = (L.nty + run - 1) / run;
     const long long rows = 6 * L.ntx * (long long)ny;
     L.col_off = (rows + G::VW - 1) / G::VW * G::VW;
-    L.total = L.col_off + 6 * L.nty * (long long)nx;
+    L.total = L.col_off + 6 * L.nseg * (long long)nx;
     return L;
 }
 
 // One block per edge record: copies channel edge_ch(side, j) of one row or
 // column of f into the workspace.
 template <class raw>
-__global__ void __launch_bounds__(IP_THREADS) k_ip_save(const raw *f, raw *__restrict__ ws, int nx, int ny) {
+__global__ void __launch_bounds__(IP_THREADS) k_ip_save(const raw *f, raw *__restrict__ ws, int nx, int ny,
+                                                        int run) {
     using G = IpGeom<raw>;
-    const IpLayout L = ip_layout<raw>(nx, ny);
+    const IpLayout L = ip_layout<raw>(nx, ny, run);
     const size_t cs = (size_t)nx * ny;
     const long long rec = blockIdx.x;
     if (rec < 6 * L.ntx) {
@@ -82,7 +90,7 @@ __global__ void __launch_bounds__(IP_THREADS) k_ip_save(const raw *f, raw *__res
     } else {
         const long long r2 = rec - 6 * L.ntx;
         const int u = (int)(r2 / 6), side = (int)(r2 / 3 % 2), j = (int)(r2 % 3);
-        const int col = side == 0 ? u * G::TY : min((u + 1) * G::TY, ny) - 1;
+        const int col = side == 0 ? u * run * G::TY : min((u + 1) * run * G::TY, ny) - 1;
         const raw *src = f + (size_t)edge_ch(2 + side, j) * cs + col;
         raw *dst = ws + L.col_off + r2 * nx;
         for (int k = threadIdx.x; k < nx; k += IP_THREADS) dst[k] = src[(size_t)k * ny];
@@ -139,39 +147,10 @@ __device__ __forceinline__ bool ip_halo_item(int i, const IpTile &T, const IpLay
     i -= nrow;
     if (i < 6 * T.txn) {
         const int hi = i / (3 * T.txn), rem = i - hi * 3 * T.txn, j = rem / T.txn, r = rem - j * T.txn;
-        const int ulo = (T.ty == 0 ? (int)L.nty : T.ty) - 1, uhi = (T.ty + 1 == L.nty) ? 0 : T.ty + 1;
+        // runs of one tile: the tile's own column records
+        const int ulo = (T.ty == 0 ? (int)L.nseg : T.ty) - 1, uhi = (T.ty + 1 == L.nseg) ? 0 : T.ty + 1;
         const long long rec = hi ? ((long long)uhi * 2 + 0) * 3 + j : ((long long)ulo * 2 + 1) * 3 + j;
         soff = ip_S<raw>(edge_ch(hi ? 2 : 3, j), r + 1, hi ? G::VW + T.tyn : G::VW - 1);
-        widx = L.col_off + rec * nx + T.a + r;
-        return true;
-    }
-    return false;
-}
-
-// ip_halo_item for a full tile (txn = IP_TX, tyn = TY): the same items, the
-// index split by compile-time constants.
-template <class raw>
-__device__ __forceinline__ bool ip_halo_item_full(int i, const IpTile &T, const IpLayout &L, int nx, int ny,
-                                                  int &soff, long long &widx) {
-    using G = IpGeom<raw>;
-    constexpr int w = G::TY + 2, nrow = 6 * w;
-    if (i < nrow) {
-        const int hi = i / (3 * w), rem = i % (3 * w), j = rem / w, col = rem % w - 1;
-        int l = T.c + col;
-        if (l < 0) l += ny;
-        if (l >= ny) l -= ny;
-        const int tlo = (T.tx == 0 ? (int)L.ntx : T.tx) - 1, thi = (T.tx + 1 == L.ntx) ? 0 : T.tx + 1;
-        const long long rec = hi ? ((long long)thi * 2 + 0) * 3 + j : ((long long)tlo * 2 + 1) * 3 + j;
-        soff = ip_S<raw>(edge_ch(hi ? 0 : 1, j), hi ? IP_TX + 1 : 0, G::VW + col);
-        widx = rec * ny + l;
-        return true;
-    }
-    i -= nrow;
-    if (i < 6 * IP_TX) {
-        const int hi = i / (3 * IP_TX), rem = i % (3 * IP_TX), j = rem / IP_TX, r = rem % IP_TX;
-        const int ulo = (T.ty == 0 ? (int)L.nty : T.ty) - 1, uhi = (T.ty + 1 == L.nty) ? 0 : T.ty + 1;
-        const long long rec = hi ? ((long long)uhi * 2 + 0) * 3 + j : ((long long)ulo * 2 + 1) * 3 + j;
-        soff = ip_S<raw>(edge_ch(hi ? 2 : 3, j), r + 1, hi ? G::VW + G::TY : G::VW - 1);
         widx = L.col_off + rec * nx + T.a + r;
         return true;
     }
@@ -271,11 +250,55 @@ __device__ __forceinline__ void cp_async_wait_prev() { asm volatile("cp.async.wa
 
 // Pipelined form for rows of whole 16-byte vectors (16-byte aligned f, ny a
 // multiple of the vector width): one persistent block per SM with two
-// stages.  While a tile is streamed out of one stage, the next tile's
-// interior is on its way into the other (16-byte cp.async, one group per
-// tile) and its halo values into registers, so the SM's loads and stores
-// overlap instead of alternating.
+// stages, streaming runs of IP_RUN consecutive tiles along y, each run in
+// order.  While a tile is streamed out of one stage, the next tile's interior
+// is on its way into the other (16-byte cp.async, one group per tile) and its
+// halo values into registers, so the SM's loads and stores overlap instead of
+// alternating.  Within a run a tile's left halo column is the previous tile's
+// old last column, copied from that tile's stage, and its right halo column is
+// the next tile's first column, read from f before that tile is written (an
+// L2 hit: the next tile is loaded one iteration later); only the run ends
+// need column records, and a block touches no tile of another run.
 constexpr int IPP_THREADS = 512;
+constexpr int IP_RUN = 4;
+
+// Halo value i of tile T at position (first, last) of run sg: rows a - 1 and
+// a + txn over columns c - 1 .. c + tyn from the row records, then the left
+// column (the run's record at its first tile; otherwise carried: nullptr) and
+// the right column (the next run's record at its last tile; otherwise the
+// next tile's first column in f).  Sets the shared-memory offset and returns
+// the address to read; nullptr past the end or for a carried value.
+template <class raw, bool FULL>
+__device__ __forceinline__ const raw *ip_run_halo(int i, const IpTile &T, int sg, bool first, bool last,
+                                                  const IpLayout &L, int nx, int ny, const raw *f, const raw *ws,
+                                                  size_t cs, int &soff) {
+    using G = IpGeom<raw>;
+    const int txn = FULL ? IP_TX : T.txn, tyn = FULL ? G::TY : T.tyn;
+    const int w = tyn + 2, nrow = 6 * w;
+    if (i < nrow) {
+        const int hi = i / (3 * w), rem = i % (3 * w), j = rem / w, col = rem % w - 1;
+        int l = T.c + col;
+        if (l < 0) l += ny;
+        if (l >= ny) l -= ny;
+        const int tlo = (T.tx == 0 ? (int)L.ntx : T.tx) - 1, thi = (T.tx + 1 == L.ntx) ? 0 : T.tx + 1;
+        const long long rec = hi ? ((long long)thi * 2 + 0) * 3 + j : ((long long)tlo * 2 + 1) * 3 + j;
+        soff = ip_S<raw>(edge_ch(hi ? 0 : 1, j), hi ? txn + 1 : 0, G::VW + col);
+        return ws + rec * ny + l;
+    }
+    i -= nrow;
+    if (i >= 6 * txn) return nullptr;
+    const int hi = i / (3 * txn), rem = i % (3 * txn), j = rem / txn, r = rem % txn;
+    const int ch = edge_ch(hi ? 2 : 3, j);
+    soff = ip_S<raw>(ch, r + 1, hi ? G::VW + tyn : G::VW - 1);
+    if (hi) {
+        if (!last) return f + ch * cs + (size_t)(T.a + r) * ny + T.c + tyn;
+        const int uhi = (sg + 1 == L.nseg) ? 0 : sg + 1;
+        return ws + L.col_off + (((long long)uhi * 2 + 0) * 3 + j) * nx + T.a + r;
+    }
+    if (!first) return nullptr;
+    const int ulo = (sg == 0 ? (int)L.nseg : sg) - 1;
+    return ws + L.col_off + (((long long)ulo * 2 + 1) * 3 + j) * nx + T.a + r;
+}
 
 template <int DT, int BC>
 __global__ void __launch_bounds__(IPP_THREADS, 1)
@@ -289,15 +312,36 @@ k_ip_stream_pipe(typename Codec<DT>::raw *f, const typename Codec<DT>::raw *__re
     static_assert(9 * IP_TX * G::VPR % IPP_THREADS == 0, "full tiles split evenly over the threads");
     extern __shared__ __align__(16) unsigned char ip_smem[];
     raw *sm = reinterpret_cast<raw *>(ip_smem);
-    const IpLayout L = ip_layout<raw>(nx, ny);
+    const IpLayout L = ip_layout<raw>(nx, ny, IP_RUN);
     const size_t cs = (size_t)nx * ny;
     const int tid = threadIdx.x;
-    const long long ntiles = L.ntx * L.nty;
-    long long t = blockIdx.x;
-    if (t >= ntiles) return;
+    const long long nunits = L.ntx * L.nseg;
 
-    auto issue = [&](long long tt, raw *stage) {
-        const IpTile T = ip_tile<raw>(tt, L, nx, ny);
+    // position: run `unit` (x tile, run along y), tile p of it
+    struct Pos {
+        long long unit;
+        int p;
+    };
+    auto run_len = [&](long long u) {
+        const long long left = L.nty - (u % L.nseg) * L.run;
+        return (int)(left < L.run ? left : L.run);
+    };
+    auto next = [&](Pos q) -> Pos {
+        if (q.p + 1 < run_len(q.unit)) return Pos{q.unit, q.p + 1};
+        return Pos{q.unit + gridDim.x, 0};
+    };
+    auto tile = [&](Pos q) -> IpTile {
+        IpTile T;
+        T.tx = (int)(q.unit / L.nseg);
+        T.ty = (int)(q.unit - (long long)T.tx * L.nseg) * L.run + q.p;
+        T.a = T.tx * IP_TX;
+        T.c = T.ty * G::TY;
+        T.txn = min(IP_TX, nx - T.a);
+        T.tyn = min(G::TY, ny - T.c);
+        return T;
+    };
+
+    auto issue = [&](const IpTile &T, raw *stage) {
         const raw *src = f + (size_t)T.a * ny + T.c;
         if (T.txn == IP_TX && T.tyn == G::TY) {
             // full tile: the index split by constants (shifts)
@@ -324,50 +368,56 @@ k_ip_stream_pipe(typename Codec<DT>::raw *f, const typename Codec<DT>::raw *__re
     };
     raw hv[HMAX];
     int hs[HMAX];
-    auto fetch_halo = [&](long long tt) {
-        IpTile T = ip_tile<raw>(tt, L, nx, ny);
+    auto fetch_halo = [&](Pos q) {
+        const IpTile T = tile(q);
+        const int sg = (int)(q.unit % L.nseg);
+        const bool first = q.p == 0, last = q.p + 1 == run_len(q.unit);
         const bool full = T.txn == IP_TX && T.tyn == G::TY;
-        if (full) {
-            // the same items with the tile's sizes as constants (divisions
-            // by constants)
-            T.txn = IP_TX;
-            T.tyn = G::TY;
-        }
 #pragma unroll
-        for (int q = 0; q < HMAX; ++q) {
-            int soff;
-            long long widx;
-            const bool ok = full ? ip_halo_item_full<raw>(tid + q * IPP_THREADS, T, L, nx, ny, soff, widx)
-                                 : ip_halo_item<raw>(tid + q * IPP_THREADS, T, L, nx, ny, soff, widx);
-            if (ok) {
-                hs[q] = soff;
-                hv[q] = ws[widx];
-            } else {
-                hs[q] = -1;
-            }
+        for (int k = 0; k < HMAX; ++k) {
+            int soff = -1;
+            const raw *src = full ? ip_run_halo<raw, true>(tid + k * IPP_THREADS, T, sg, first, last, L, nx, ny, f,
+                                                           ws, cs, soff)
+                                  : ip_run_halo<raw, false>(tid + k * IPP_THREADS, T, sg, first, last, L, nx, ny, f,
+                                                            ws, cs, soff);
+            hs[k] = src ? soff : -1;
+            if (src) hv[k] = *src;
         }
     };
 
+    Pos cur{blockIdx.x, 0};
+    if (cur.unit >= nunits) return;
     int st = 0;
-    issue(t, sm);
+    issue(tile(cur), sm);
     cp_async_commit();
-    fetch_halo(t);
-    for (; t < ntiles; t += gridDim.x) {
-        const long long nt = t + gridDim.x;
-        raw *cur = sm + st * STAGE;
+    fetch_halo(cur);
+    while (cur.unit < nunits) {
+        const Pos nx_pos = next(cur);
+        const bool more = nx_pos.unit < nunits;
+        const IpTile T = tile(cur);
+        raw *stg = sm + st * STAGE, *stn = sm + (st ^ 1) * STAGE;
         // the other stage was last read by the previous tile, which every
         // thread finished before the barrier that ended the last iteration
-        if (nt < ntiles) issue(nt, sm + (st ^ 1) * STAGE);
+        if (more) issue(tile(nx_pos), stn);
         cp_async_commit();  // one group per iteration, empty at the end
 #pragma unroll
-        for (int q = 0; q < HMAX; ++q)
-            if (hs[q] >= 0) cur[hs[q]] = hv[q];
-        if (nt < ntiles) fetch_halo(nt);
+        for (int k = 0; k < HMAX; ++k)
+            if (hs[k] >= 0) stg[hs[k]] = hv[k];
+        if (more) fetch_halo(nx_pos);
         cp_async_wait_prev();  // this thread's copies of the current tile have landed
         __syncthreads();       // ... and everyone's, with the halo
-        ip_stream_tile<DT, BC, IPP_THREADS>(cur, f, ip_tile<raw>(t, L, nx, ny), nx, ny, u0, tid);
+        if (more && nx_pos.p > 0) {
+            // the next tile of this run takes this tile's old last column as
+            // its left halo (channels that cross that edge: N, NE, NW)
+            for (int i = tid; i < 3 * T.txn; i += IPP_THREADS) {
+                const int j = i / T.txn, r = i - j * T.txn, ch = edge_ch(3, j);
+                stn[ip_S<raw>(ch, r + 1, G::VW - 1)] = stg[ip_S<raw>(ch, r + 1, G::VW + T.tyn - 1)];
+            }
+        }
+        ip_stream_tile<DT, BC, IPP_THREADS>(stg, f, T, nx, ny, u0, tid);
         __syncthreads();
         st ^= 1;
+        cur = nx_pos;
     }
 }
 
@@ -405,8 +455,10 @@ int launch_ip(void *f, int nx, int ny, int boundary, double u0, void *ws, size_t
         return LBGB_EINVAL;
     }
     const bool vec = (ny % G::VW == 0) && aligned(f, 16);
+    const int run = vec ? IP_RUN : 1;
+    const IpLayout LR = ip_layout<raw>(nx, ny, run);
     raw *fp = static_cast<raw *>(f);
-    k_ip_save<raw><<<(unsigned)recs, IP_THREADS, 0, s>>>(fp, static_cast<raw *>(ws), nx, ny);
+    k_ip_save<raw><<<(unsigned)(6 * (LR.ntx + LR.nseg)), IP_THREADS, 0, s>>>(fp, static_cast<raw *>(ws), nx, ny, run);
     int rc = check_launch("k_ip_save");
     if (rc) return rc;
     // variants: periodic / cavity x generic / pipelined
@@ -428,7 +480,8 @@ int launch_ip(void *f, int nx, int ny, int boundary, double u0, void *ws, size_t
         return check_launch(name);
     };
     if (vec) {
-        const unsigned grid = (unsigned)(tiles < ip_sm_count() ? tiles : ip_sm_count());
+        const long long units = LR.ntx * LR.nseg;
+        const unsigned grid = (unsigned)(units < ip_sm_count() ? units : ip_sm_count());
         return boundary == LBGB_PERIODIC
                    ? go(k_ip_stream_pipe<DT, LBGB_PERIODIC>, grid, IPP_THREADS, "k_ip_stream_pipe")
                    : go(k_ip_stream_pipe<DT, LBGB_CAVITY>, grid, IPP_THREADS, "k_ip_stream_pipe");

@@ -8,8 +8,11 @@ tile, ragged tiles in both directions, rows that do not hold whole 16-byte
 vectors and a population pointer that is not 16-byte aligned (scalar loads),
 in every storage, periodic and with the cavity's walls and lid.  Lattices
 whose rows hold whole 16-byte vectors take the pipelined kernel (one
-persistent block per SM, two shared-memory stages); the two largest cases
-have more tiles than the GPU has SMs, so its blocks loop over several tiles.
+persistent block per SM, two shared-memory stages, runs of four tiles along
+y streamed in order with the column halo carried between them); the cases
+cover runs of one to four tiles, a single run wrapping onto itself, ragged
+last tiles in a run, and (the two largest) blocks that loop over several
+runs.
 """
 
 import numpy as np
