@@ -19,6 +19,8 @@
 #include <cuda.h>
 #include <stdio.h>
 
+#include <type_traits>
+
 #include "lbgb_act.cuh"
 #include "lbgb_common.cuh"
 
@@ -71,6 +73,29 @@ __device__ __forceinline__ void store_out(float *p, float x) { *p = x; }
 __device__ __forceinline__ void store_out(__nv_bfloat16 *p, float x) { *p = __float2bfloat16_rn(x); }
 __device__ __forceinline__ float load_out(const float *p) { return *p; }
 __device__ __forceinline__ float load_out(const __nv_bfloat16 *p) { return __bfloat162float(*p); }
+// four consecutive outputs (16 bytes of FP32, 8 of BF16; aligned)
+__device__ __forceinline__ void load4_out(const float *p, float (&x)[4]) {
+    const float4 v = *reinterpret_cast<const float4 *>(p);
+    x[0] = v.x, x[1] = v.y, x[2] = v.z, x[3] = v.w;
+}
+__device__ __forceinline__ void load4_out(const __nv_bfloat16 *p, float (&x)[4]) {
+    const uint2 v = *reinterpret_cast<const uint2 *>(p);
+    x[0] = __uint_as_float(v.x << 16), x[1] = __uint_as_float(v.x & 0xffff0000u);
+    x[2] = __uint_as_float(v.y << 16), x[3] = __uint_as_float(v.y & 0xffff0000u);
+}
+__device__ __forceinline__ uint2 pack4_bf16(const float (&x)[4]) {
+    const uint32_t a = (uint32_t)__bfloat16_as_ushort(__float2bfloat16_rn(x[0])) |
+                       ((uint32_t)__bfloat16_as_ushort(__float2bfloat16_rn(x[1])) << 16);
+    const uint32_t b = (uint32_t)__bfloat16_as_ushort(__float2bfloat16_rn(x[2])) |
+                       ((uint32_t)__bfloat16_as_ushort(__float2bfloat16_rn(x[3])) << 16);
+    return make_uint2(a, b);
+}
+__device__ __forceinline__ void store4_out(float *p, const float (&x)[4]) {
+    *reinterpret_cast<float4 *>(p) = make_float4(x[0], x[1], x[2], x[3]);
+}
+__device__ __forceinline__ void store4_out(__nv_bfloat16 *p, const float (&x)[4]) {
+    *reinterpret_cast<uint2 *>(p) = pack4_bf16(x);
+}
 
 constexpr int TC_M = 128;
 constexpr long long TC_WAIT = 1ll << 22;
@@ -518,7 +543,7 @@ struct Epi {
 // bytes with the 128-byte swizzle: the MN-major SWIZZLE_128B layout, 8-row
 // K groups 1024 bytes apart, the two 64-element M chunks 8192 bytes apart;
 // an MMA of K = 16 starts 2048 bytes further.
-template <int NT, typename OUT, bool AMN = false>
+template <int NT, typename OUT, bool AMN = false, bool EPI = false>
 __global__ void __launch_bounds__(TP_THREADS, 2)
 k_gemm_tma(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB, int a3d, int b3d, int M,
            int N, int K, int batch, OUT *__restrict__ C, long long c_rs, long long c_cs, long long c_bs, float alpha,
@@ -534,6 +559,12 @@ k_gemm_tma(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUte
     const int tiles_m = (M + TC_M - 1) / TC_M, tiles_n = (N + NT - 1) / NT;
     const long long tiles = (long long)tiles_m * tiles_n * batch;
     const int kblocks = (K + TP_KB - 1) / TP_KB;
+    // FP32 row-major C whose rows start on 16-byte boundaries (BF16 outputs keep
+    // the element-wise stores: their packing would not fit the register limit)
+    const bool vec_rm = std::is_same<OUT, float>::value && c_cs == 1 && c_rs != 1 && c_rs % 4 == 0 &&
+                        c_bs % 4 == 0 &&
+                        (reinterpret_cast<uintptr_t>(C) % (4 * sizeof(OUT))) == 0 &&
+                        (!EPI || !ep.vb || reinterpret_cast<uintptr_t>(ep.vb) % 8 == 0);
 
     if (warp == 1) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&tmem_slot)),
@@ -665,7 +696,44 @@ k_gemm_tma(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUte
             for (int c0 = half * (NT / 2); c0 < (half + 1) * (NT / 2); c0 += 16) {
                 uint32_t v[16];
                 tc_ld16(tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(buf * NT + c0), v);
-                if (c_cs == 1 && c_rs != 1) {
+                if (std::is_same<OUT, float>::value && vec_rm && n0 + c0 + 16 <= N) {
+                    // row-major C with aligned rows: stage the warp's 32 x 16
+                    // block; a lane then owns four consecutive columns of
+                    // rows 8i + lane/4 (16-byte loads and stores of C)
+#pragma unroll
+                    for (int j = 0; j < 16; ++j) ostage[lane * 17 + j] = __uint_as_float(v[j]);
+                    __syncwarp();
+                    const int quad = lane & 3, sub = lane >> 2, col = n0 + c0 + 4 * quad;
+                    // EPI: the block's 32 rows meet at most one bias boundary
+                    // when rows >= 32 (one division per block)
+                    const long long b_lo = EPI && ep.rows >= 32 ? m0 / ep.rows : 0;
+                    const long long edge = (b_lo + 1) * ep.rows;
+                    // one row at a time: the kernel runs at its register
+                    // limit (two CTAs of 320 threads per SM)
+#pragma unroll 1
+                    for (int i = 0; i < 4; ++i) {
+                        const int r = 8 * i + sub, row = m0 + r;
+                        if (row < M) {
+                            OUT *p = Cz + (long long)row * c_rs + col;
+                            float val[4] = {0.f, 0.f, 0.f, 0.f};
+                            if (beta != 0.f) load4_out(p, val);
+#pragma unroll
+                            for (int e = 0; e < 4; ++e) val[e] = alpha * ostage[r * 17 + 4 * quad + e] + beta * val[e];
+                            if (EPI && ep.bias) {
+                                const float b = ep.bias[ep.rows >= 32 ? b_lo + (row >= edge) : row / ep.rows];
+#pragma unroll
+                                for (int e = 0; e < 4; ++e) val[e] = val[e] + b;
+                            }
+                            store4_out(p, val);
+                            if (EPI && ep.vb) {
+#pragma unroll
+                                for (int e = 0; e < 4; ++e) val[e] = ep.act ? gelu_f(val[e]) : val[e];
+                                *reinterpret_cast<uint2 *>(ep.vb + (long long)row * c_rs + col) = pack4_bf16(val);
+                            }
+                        }
+                    }
+                    __syncwarp();
+                } else if (c_cs == 1 && c_rs != 1) {
                     // row-major C: stage the warp's 32 x 16 block and write two
                     // rows per instruction, 16 consecutive columns each
 #pragma unroll
@@ -678,7 +746,7 @@ k_gemm_tma(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUte
                         const int row = m0 + 2 * i + (lane >> 4);
                         old[i] = (beta != 0.f && row < M && col < N) ? load_out(Cz + (long long)row * c_rs + col) : 0.f;
                     }
-                    if (ep.bias || ep.vb) {
+                    if (EPI && (ep.bias || ep.vb)) {
                         // the block's 32 rows meet at most one bias boundary
                         // when rows >= 32: one division per block
                         const long long b_lo = ep.rows >= 32 ? m0 / ep.rows : 0;
@@ -813,30 +881,34 @@ static int launch_gemm_tma_nt(int m, int n, int k, const __nv_bfloat16 *a, long 
     if (!(amn ? mmajor_map(&ma, a, m, k, a_cs, batch, a_bs, &a3) : kmajor_map(&ma, a, m, k, a_rs, batch, a_bs, TC_M, &a3)) ||
         !kmajor_map(&mb, b, n, k, b_cs, batch, b_bs, NT, &b3))
         return 1;
-    static std::atomic<bool> attr[MAX_DEVICES][2];
+    const bool epi = ep.bias || ep.vb;
+    if (epi && amn) return 1;  // the layer epilogue is built for a K-major A only
+    // variants: K-major A, M-major A, K-major A with the layer epilogue
+    static std::atomic<bool> attr[MAX_DEVICES][3];
     const int dev = current_device();
-    if (!attr[dev][amn].load(std::memory_order_acquire)) {
+    const int variant = epi ? 2 : (amn ? 1 : 0);
+    auto kernel_of = [](int v) {
+        if constexpr (std::is_same<OUT, float>::value)
+            if (v == 2) return k_gemm_tma<NT, OUT, false, true>;
+        return v == 1 ? k_gemm_tma<NT, OUT, true, false> : k_gemm_tma<NT, OUT, false, false>;
+    };
+    if (epi && !std::is_same<OUT, float>::value) return 1;
+    const auto kernel = kernel_of(variant);
+    if (!attr[dev][variant].load(std::memory_order_acquire)) {
         std::lock_guard<std::mutex> lock(setup_mutex());
-        const cudaError_t e =
-            amn ? cudaFuncSetAttribute(k_gemm_tma<NT, OUT, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, S::SMEM)
-                : cudaFuncSetAttribute(k_gemm_tma<NT, OUT, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, S::SMEM);
+        const cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, S::SMEM);
         if (e != cudaSuccess) {
             set_error("k_gemm_tma: cannot reserve %d bytes of shared memory: %s", S::SMEM, cudaGetErrorString(e));
             return LBGB_ECUDA;
         }
-        attr[dev][amn].store(true, std::memory_order_release);
+        attr[dev][variant].store(true, std::memory_order_release);
     }
     int sms = 0;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     const long long tiles = (long long)((m + TC_M - 1) / TC_M) * ((n + NT - 1) / NT) * batch;
     const long long slots = 2ll * (sms > 0 ? sms : 1);
     const int grid = (int)(tiles < slots ? tiles : slots);
-    if (amn)
-        k_gemm_tma<NT, OUT, true><<<grid, TP_THREADS, S::SMEM, s>>>(ma, mb, a3, b3, m, n, k, batch, C, c_rs, c_cs, c_bs,
-                                                                    alpha, beta, ep);
-    else
-        k_gemm_tma<NT, OUT, false><<<grid, TP_THREADS, S::SMEM, s>>>(ma, mb, a3, b3, m, n, k, batch, C, c_rs, c_cs,
-                                                                     c_bs, alpha, beta, ep);
+    kernel<<<grid, TP_THREADS, S::SMEM, s>>>(ma, mb, a3, b3, m, n, k, batch, C, c_rs, c_cs, c_bs, alpha, beta, ep);
     return check_launch("k_gemm_tma");
 }
 
