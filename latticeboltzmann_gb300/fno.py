@@ -96,11 +96,9 @@ class FNO2d:
             raise ValueError("max_splits must be a power of two")
         self.max_splits = int(max_splits)  # weight gradients: split-K count over the pixels
         # bias + activation in the epilogue of each layer's last GEMM (tensor-
-        # core engine): measured slower than the separate vectorised pass at
-        # 16 x 256^2 (training step 4.35 against 4.06 ms, forward 1.92 against
-        # 1.62 ms) -- the persistent GEMM's 16 epilogue warps per SM store
-        # element by element -- so off by default
-        self.fused_epilogue = False
+        # core engine; 16 x 256^2: training step 3.95 against 4.03 ms, forward
+        # 1.54 against 1.62 ms with a separate pass)
+        self.fused_epilogue = True
         shapes = [("P", (width, cin)), ("pb", (width,))]
         for l in range(layers):
             shapes += [("W%d" % l, (width, width)), ("b%d" % l, (width,)),
@@ -206,9 +204,9 @@ class FNO2d:
 
     def _gemm_bias_act(self, m, n, k, A, a, B, b_cs, C, c_rs, bias, rows_per_bias, channels, cols, act, vb):
         """C = A B + C, C += bias per channel (rows_per_bias rows of C each),
-        vb = BF16(act(C)): the GEMM and lbgb_fno_bias_act, or, with
-        ``fused_epilogue``, one launch of the TMA pipeline when it takes the
-        operands."""
+        vb = BF16(act(C)): with ``fused_epilogue`` (default) one launch of the
+        TMA pipeline when it takes the operands, else the GEMM and
+        lbgb_fno_bias_act."""
         s = self._s()
         if self.engine == ENGINE_TENSOR_CORES and self.fused_epilogue:
             rc = _lib.load().lbgb_gemm_bf16_bias_act(m, n, k, A, a[0], a[1], B, b_cs, C, c_rs, 1.0, 1.0, bias,
@@ -471,13 +469,13 @@ def main(argv=None):
                     help="tensor: TMA pipeline where both operands are K-major, else the staged kernel; "
                          "staged: the staged tcgen05 kernel for every product; cuda: CUDA cores")
     ap.add_argument("--max-splits", type=int, default=1024, help="split-K count cap of the weight gradients")
-    ap.add_argument("--fused", action="store_true",
-                    help="bias and activation in the epilogue of the layer's last GEMM (for comparison)")
+    ap.add_argument("--unfused", action="store_true",
+                    help="bias and activation as a separate pass after the layer's last GEMM (for comparison)")
     args = ap.parse_args(argv)
     dev = torch.device("cuda", torch.cuda.current_device())
     engine = {"tensor": ENGINE_TENSOR_CORES, "staged": ENGINE_STAGED, "cuda": ENGINE_CUDA_CORES}[args.engine]
     net = FNO2d(device=dev, engine=engine, max_splits=args.max_splits)
-    net.fused_epilogue = args.fused
+    net.fused_epilogue = not args.unfused
     rng = np.random.default_rng(0)
     re = np.exp(rng.uniform(math.log(RE_RANGE[0]), math.log(RE_RANGE[1]), args.batch))
     a = net.inputs(re, rng.uniform(*U_RANGE, args.batch), args.n, args.n)
