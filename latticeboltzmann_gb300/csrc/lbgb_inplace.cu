@@ -426,6 +426,7 @@ int ip_sm_count() {
     const int dev = current_device();
     int v = cache[dev].load(std::memory_order_acquire);
     if (v) return v;
+    std::lock_guard<std::mutex> lock(setup_mutex());
     int n = 0;
     cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
     v = n > 0 ? n : 1;
