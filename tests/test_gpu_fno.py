@@ -167,13 +167,15 @@ def test_committed_ensemble(cuda):
     the mean of its members."""
     import os
     from latticeboltzmann_gb300 import surrogate as S
+    import glob
     wdir = os.path.join(os.path.dirname(F.__file__), "weights")
-    paths = [os.path.join(wdir, f) for f in ("fno_cavity256_bf16.npz", "fno_cavity256_bf16_m1.npz",
-                                              "fno_cavity256_bf16_m2.npz")]
+    paths = [os.path.join(wdir, "fno_cavity256_bf16.npz")] + sorted(
+        glob.glob(os.path.join(wdir, "fno_cavity256_bf16_m*.npz")))
+    assert len(paths) == 5
     nets = [F.FNO2d.load(p, device=cuda) for p in paths]
     held = [n.meta["held_out_re"] for n in nets]
     assert all(h == held[0] for h in held) and len(held[0]) == 64
-    assert len({n.meta.get("train_seed", 0) for n in nets}) == 3
+    assert len({n.meta.get("train_seed", 0) for n in nets}) == len(nets)
     ens = S.load_networks(",".join(paths), cuda)
     re, u = held[0][:3], nets[0].meta["held_out_u"][:3]
     mean = None
@@ -181,4 +183,4 @@ def test_committed_ensemble(cuda):
         p = [x.clone() for x in n.predict(re, u, 64, 64)]
         mean = p if mean is None else [m + x for m, x in zip(mean, p)]
     for got, m in zip(ens.predict(re, u, 64, 64), mean):
-        assert torch.allclose(got, m / 3, rtol=0, atol=1e-6)
+        assert torch.allclose(got, m / len(nets), rtol=0, atol=1e-6)
