@@ -60,6 +60,32 @@ def test_host_validation_before_any_launch(lib):
     assert rc == _lib.EINVAL
 
 
+def test_inplace_stream_and_fused_gemm_validation_before_any_launch(lib):
+    """The in-place streams and the fused GEMM reject bad arguments on the
+    host, before any launch (no GPU needed)."""
+    f, ws = 1 << 24, 1 << 30  # aligned fake device addresses: never dereferenced here
+    need = lib.lbgb_stream_inplace_workspace_bytes(64, 64, _lib.F32)
+    rc = lib.lbgb_stream_periodic_inplace(None, 64, 64, _lib.F32, ws, need, None)
+    assert rc == _lib.EINVAL and "null" in _lib.last_error()
+    rc = lib.lbgb_stream_periodic_inplace(f, 64, 64, 9, ws, need, None)
+    assert rc == _lib.EDTYPE
+    rc = lib.lbgb_stream_periodic_inplace(f, 64, 64, _lib.F32, ws, need - 1, None)
+    assert rc == _lib.EINVAL and "workspace" in _lib.last_error()
+    rc = lib.lbgb_stream_bounce_back_inplace(f, 64, 64, 0.1, _lib.F32, ws + 8, need, None)
+    assert rc == _lib.EINVAL and "16-byte" in _lib.last_error()
+    rc = lib.lbgb_stream_bounce_back_inplace(f, 1, 64, 0.1, _lib.F32, ws, need, None)
+    assert rc == _lib.EINVAL and "cavity" in _lib.last_error()
+    rc = lib.lbgb_stream_periodic_inplace(f + 2, 64, 64, _lib.F32, ws, need, None)
+    assert rc == _lib.EINVAL and "aligned" in _lib.last_error()
+    # fused GEMM: sizes, then layouts it cannot take (nothing launched)
+    rc = lib.lbgb_gemm_bf16_bias_act(0, 32, 16, f, 16, 1, f, 16, ws, 32, 1.0, 0.0, None, 1, 0, None, None)
+    assert rc == _lib.EINVAL
+    rc = lib.lbgb_gemm_bf16_bias_act(64, 32, 16, f, 1, 64, f, 16, ws, 32, 1.0, 0.0, None, 1, 0, None, None)
+    assert rc == _lib.EUNSUPPORTED
+    rc = lib.lbgb_gemm_bf16_bias_act(64, 32, 16, f, 16, 1, f, 16, ws + 4, 32, 1.0, 0.0, None, 1, 0, None, None)
+    assert rc == _lib.EUNSUPPORTED
+
+
 def test_workspace_size_is_small(lib):
     assert 0 < lib.lbgb_mass_momentum_workspace_bytes() <= 1 << 20
 
