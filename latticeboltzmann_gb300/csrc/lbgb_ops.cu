@@ -100,9 +100,16 @@ __global__ void k_chapman_enskog(const T *__restrict__ rho, const T *__restrict_
 // and FP64 only): the reference native kernel's arithmetic, operation by
 // operation (bgk_collide_native); otherwise the solver's collision with its
 // mass-preserving store (collide_encode).
+// Resident blocks per SM the register allocation must allow: the FP32
+// native-order collision of four cells per thread fits 80 registers without
+// spilling (three blocks of 256 threads per SM); the others keep the
+// compiler's choice (a bound of three makes them spill).
 template <int DT, int V, bool NATIVE>
-__global__ void k_collide(typename Codec<DT>::raw *__restrict__ f, int64_t n, int64_t cs,
-                          typename Codec<DT>::real omega) {
+constexpr int collide_min_blocks() { return (DT == LBGB_F32 && V == 4 && NATIVE) ? 3 : 1; }
+
+template <int DT, int V, bool NATIVE>
+__global__ void __launch_bounds__(256, collide_min_blocks<DT, V, NATIVE>())
+k_collide(typename Codec<DT>::raw *__restrict__ f, int64_t n, int64_t cs, typename Codec<DT>::real omega) {
     using C = Codec<DT>;
     using raw = typename C::raw;
     using real = typename C::real;
