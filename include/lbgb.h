@@ -164,10 +164,19 @@ LBGB_API int lbgb_step_fused_rows(const void *src, void *dst, int nx, int ny, in
 
 /* nsteps fused steps ping-ponging between a and b (a holds the initial
  * state); *which receives 0 if the result is in a, 1 if in b.  Launch-only:
- * suitable for CUDA-graph capture. */
+ * suitable for CUDA-graph capture.  Where lbgb_steps_per_launch says 2
+ * (LBGB_F32 or LBGB_F32DEV storage, periodic or cavity walls, nx a multiple
+ * of 16, ny of 256, 16-byte aligned buffers, LBGB_TUNE_TWO_STEP on and the
+ * auto kernel), pairs of steps run as one launch that keeps the intermediate
+ * step on chip (k_step2: one read and one write of the lattice per two
+ * steps); the results equal single steps bit for bit. */
 LBGB_API int lbgb_run_fused(void *a, void *b, int nx, int ny, int boundary,
                    double omega, double u0, int dtype, int nsteps, int *which,
                    void *stream);
+
+/* Steps lbgb_run_fused advances per launch on this lattice (1 or 2; any
+ * buffers 16-byte aligned). */
+LBGB_API int lbgb_steps_per_launch(int nx, int ny, int boundary, int dtype);
 
 /* As lbgb_run_fused, with stochastic rounding of the 16-bit storage codes
  * (LBGB_F16DEV, LBGB_BF16DEV; other codes run lbgb_run_fused).  Every stored
@@ -411,6 +420,9 @@ LBGB_API int lbgb_fno_sum_splits(const float *parts, float *out, int S, long lon
  *   LBGB_TUNE_STAGES          shared-memory stages of the pipelined kernel
  *   LBGB_TUNE_WAIT_LIMIT      tries per bounded device-side wait
  *   LBGB_TUNE_PIPE_MIN_CELLS  auto: lattices with fewer cells use the register kernel
+ *   LBGB_TUNE_TWO_STEP        1 (default): with the auto kernel, lbgb_run_fused advances
+ *                             pairs of steps in one launch (two steps per read and write of
+ *                             the lattice) where that kernel applies; 0: one step per launch
  *   LBGB_TUNE_TEST_STALL_PRODUCER  test hook: the pipelined kernel's producer
  *                             delivers nothing, so its consumers' bounded
  *                             waits expire (exercises the timeout path)
@@ -420,6 +432,7 @@ LBGB_API int lbgb_fno_sum_splits(const float *parts, float *out, int S, long lon
 #define LBGB_TUNE_WAIT_LIMIT 2
 #define LBGB_TUNE_PIPE_MIN_CELLS 3
 #define LBGB_TUNE_TEST_STALL_PRODUCER 4
+#define LBGB_TUNE_TWO_STEP 5
 LBGB_API int lbgb_set_tuning(int key, long long value);
 LBGB_API long long lbgb_get_tuning(int key);
 

@@ -57,6 +57,7 @@ SIGNATURES = {
     "lbgb_copy_rows": (_I, [_P, _P, _I, _I, _I, _I, _I, _P]),
     "lbgb_step_fused_rows": (_I, [_P, _P, _I, _I, _I, _I, _I, ctypes.c_double, ctypes.c_double, _I, _P]),
     "lbgb_run_fused": (_I, [_P, _P, _I, _I, _I, _D, _D, _I, _I, ctypes.POINTER(_I), _P]),
+    "lbgb_steps_per_launch": (_I, [_I, _I, _I, _I]),
     "lbgb_run_fused_sr": (_I, [_P, _P, _I, _I, _I, _D, _D, _I, _I, ctypes.c_uint, _P, ctypes.POINTER(_I), _P]),
     "lbgb_macroscopic": (_I, [_P, _P, _P, _P, _I64, _I64, _I, _P]),
     "lbgb_mass_momentum_workspace_bytes": (_SZ, []),
@@ -94,7 +95,7 @@ SIGNATURES = {
     "lbgb_device_status": (_I, [_I]),
 }
 
-TUNE_KERNEL, TUNE_STAGES, TUNE_WAIT_LIMIT, TUNE_PIPE_MIN_CELLS, TUNE_TEST_STALL_PRODUCER = 0, 1, 2, 3, 4
+TUNE_KERNEL, TUNE_STAGES, TUNE_WAIT_LIMIT, TUNE_PIPE_MIN_CELLS, TUNE_TEST_STALL_PRODUCER, TUNE_TWO_STEP = 0, 1, 2, 3, 4, 5
 KERNELS = {"auto": 0, "register": 1, "pipelined": 2}
 NOALLOC_MAX_CELLS = 268435456
 DIAG_CHUNKS = 64  # LBGB_DIAG_CHUNKS: partials per instance of the batch diagnostics

@@ -762,6 +762,21 @@ __device__ __forceinline__ void collide_encode_sr(float (&f)[9], float omega, un
     out[0] = round1(sr_rest<DT>(dm), 0);
 }
 
+// ---------------------------------------------------------------- cp.async
+// 16-byte global -> shared copies of the issuing thread, grouped; a wait
+// returns when at most N of the thread's groups are still in flight (a
+// hardware wait on the thread's own copies: nothing to bound).
+__device__ __forceinline__ void cp_async16(void *smem_dst, const void *gmem_src) {
+    const unsigned d = (unsigned)__cvta_generic_to_shared(smem_dst);
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(d), "l"(__cvta_generic_to_global(gmem_src))
+                 : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() {
+    asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory");
+}
+
 // ---------------------------------------------------------------- host side
 void set_error(const char *fmt, ...);
 int check_launch(const char *what);

@@ -240,14 +240,6 @@ k_ip_stream(typename Codec<DT>::raw *f, const typename Codec<DT>::raw *__restric
     ip_stream_tile<DT, BC, IP_THREADS>(s, f, T, nx, ny, u0, tid);
 }
 
-__device__ __forceinline__ void cp_async16(void *smem_dst, const void *gmem_src) {
-    const unsigned d = (unsigned)__cvta_generic_to_shared(smem_dst);
-    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(d), "l"(__cvta_generic_to_global(gmem_src))
-                 : "memory");
-}
-__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
-__device__ __forceinline__ void cp_async_wait_prev() { asm volatile("cp.async.wait_group 1;\n" ::: "memory"); }
-
 // Pipelined form for rows of whole 16-byte vectors (16-byte aligned f, ny a
 // multiple of the vector width): one persistent block per SM with two
 // stages, streaming runs of IP_RUN consecutive tiles along y, each run in
@@ -404,7 +396,7 @@ k_ip_stream_pipe(typename Codec<DT>::raw *f, const typename Codec<DT>::raw *__re
         for (int k = 0; k < HMAX; ++k)
             if (hs[k] >= 0) stg[hs[k]] = hv[k];
         if (more) fetch_halo(nx_pos);
-        cp_async_wait_prev();  // this thread's copies of the current tile have landed
+        cp_async_wait<1>();  // this thread's copies of the current tile have landed
         __syncthreads();       // ... and everyone's, with the halo
         if (more && nx_pos.p > 0) {
             // the next tile of this run takes this tile's old last column as

@@ -278,6 +278,7 @@ struct Tuning {
     long long wait_limit = 1ll << 22;    // tries per bounded mbarrier wait
     long long pipe_min_cells = 1 << 16;  // auto: smaller lattices use the register kernel
     long long stall_producer = 0;        // test hook: the producer delivers nothing
+    long long two_step = 1;              // auto kernel: two time steps per launch where k_step2 applies
 };
 static Tuning g_tune;
 
@@ -292,6 +293,58 @@ static int max_dyn_smem() {
     v = n > 0 ? n : 48 * 1024;
     cache[dev].store(v, std::memory_order_release);
     return v;
+}
+
+}  // namespace lbgb
+#include "lbgb_step2.cuh"
+namespace lbgb {
+
+// Rows per block of the two-step kernel: the largest of 128, 64, 32, 16 that
+// divides nx (0: none does).
+static int step2_rows(int nx) {
+    for (int r = 128; r >= 16; r /= 2)
+        if (nx % r == 0) return r;
+    return 0;
+}
+
+static bool step2_applies(const void *src, const void *dst, int nx, int ny, int boundary, int dtype) {
+    return g_tune.two_step && g_tune.kernel == 0 && (dtype == LBGB_F32 || dtype == LBGB_F32DEV) &&
+           (boundary == LBGB_PERIODIC || boundary == LBGB_CAVITY) && step2_rows(nx) && ny % S2_W == 0 &&
+           ny / S2_W <= 65535 && (!src || aligned(src, 16)) && (!dst || aligned(dst, 16));
+}
+
+template <int DT, int BC>
+static int launch_step2(const void *src, void *dst, int nx, int ny, double omega, double u0, cudaStream_t s) {
+    using raw = typename Codec<DT>::raw;
+    static std::atomic<bool> attr_set[MAX_DEVICES];
+    const int dev = current_device();
+    if (!attr_set[dev].load(std::memory_order_acquire)) {
+        std::lock_guard<std::mutex> lock(setup_mutex());
+        const cudaError_t e =
+            cudaFuncSetAttribute(k_step2<DT, BC>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)S2_SMEM);
+        if (e != cudaSuccess) {
+            set_error("k_step2: cannot reserve %zu bytes of shared memory: %s", S2_SMEM, cudaGetErrorString(e));
+            return LBGB_ECUDA;
+        }
+        attr_set[dev].store(true, std::memory_order_release);
+    }
+    const int rows = step2_rows(nx);
+    k_step2<DT, BC><<<dim3(nx / rows, ny / S2_W), S2_THREADS, S2_SMEM, s>>>(
+        static_cast<const raw *>(src), static_cast<raw *>(dst), nx, ny, rows, (typename Codec<DT>::real)omega,
+        (typename Codec<DT>::real)u0);
+    return check_launch("k_step2");
+}
+
+// Two fused steps src -> dst in one launch; 1 (nothing launched) where the
+// two-step kernel does not apply.
+static int step2(const void *src, void *dst, int nx, int ny, int boundary, double omega, double u0, int dtype,
+                 cudaStream_t s) {
+    if (!step2_applies(src, dst, nx, ny, boundary, dtype)) return 1;
+    if (dtype == LBGB_F32)
+        return boundary == LBGB_CAVITY ? launch_step2<LBGB_F32, LBGB_CAVITY>(src, dst, nx, ny, omega, u0, s)
+                                       : launch_step2<LBGB_F32, LBGB_PERIODIC>(src, dst, nx, ny, omega, 0.0, s);
+    return boundary == LBGB_CAVITY ? launch_step2<LBGB_F32DEV, LBGB_CAVITY>(src, dst, nx, ny, omega, u0, s)
+                                   : launch_step2<LBGB_F32DEV, LBGB_PERIODIC>(src, dst, nx, ny, omega, 0.0, s);
 }
 
 template <int DT, int BC, bool COLLIDE>
@@ -457,7 +510,17 @@ extern "C" int lbgb_run_fused(void *a, void *b, int nx, int ny, int boundary, do
     int rc = check_grid(a, b, nx, ny, dtype, boundary, "lbgb_run_fused");
     if (rc) return rc;
     void *src = a, *dst = b;
-    for (int s = 0; s < nsteps; ++s) {
+    int s = 0;
+    // pairs of steps in one launch each where the two-step kernel applies
+    for (; s + 1 < nsteps; s += 2) {
+        rc = step2(src, dst, nx, ny, boundary, omega, u0, dtype, (cudaStream_t)stream);
+        if (rc > 0) break;
+        if (rc < 0) return rc;
+        void *t = src;
+        src = dst;
+        dst = t;
+    }
+    for (; s < nsteps; ++s) {
         rc = lbgb_step_fused(src, dst, nx, ny, boundary, omega, u0, dtype, stream);
         if (rc) return rc;
         void *t = src;
@@ -466,6 +529,10 @@ extern "C" int lbgb_run_fused(void *a, void *b, int nx, int ny, int boundary, do
     }
     if (which) *which = (src == a) ? 0 : 1;
     return LBGB_OK;
+}
+
+extern "C" int lbgb_steps_per_launch(int nx, int ny, int boundary, int dtype) {
+    return step2_applies(nullptr, nullptr, nx, ny, boundary, dtype) ? 2 : 1;
 }
 
 namespace lbgb {
@@ -531,6 +598,9 @@ extern "C" int lbgb_set_tuning(int key, long long value) {
     case LBGB_TUNE_TEST_STALL_PRODUCER:
         g_tune.stall_producer = value ? 1 : 0;
         return LBGB_OK;
+    case LBGB_TUNE_TWO_STEP:
+        g_tune.two_step = value ? 1 : 0;
+        return LBGB_OK;
     default:
         set_error("lbgb_set_tuning: unknown key %d", key);
         return LBGB_EINVAL;
@@ -546,6 +616,7 @@ extern "C" long long lbgb_get_tuning(int key) {
     case LBGB_TUNE_WAIT_LIMIT: return g_tune.wait_limit;
     case LBGB_TUNE_PIPE_MIN_CELLS: return g_tune.pipe_min_cells;
     case LBGB_TUNE_TEST_STALL_PRODUCER: return g_tune.stall_producer;
+    case LBGB_TUNE_TWO_STEP: return g_tune.two_step;
     }
     return -1;
 }

@@ -106,8 +106,19 @@ class Lattice:
 
     @property
     def bytes_per_cell_update(self):
-        """Algorithmic HBM bytes per cell and step: 9 loads + 9 stores."""
+        """Algorithmic HBM bytes per cell and launch: 9 loads + 9 stores (one
+        step per launch; two where ``steps_per_launch`` is 2)."""
         return 18 * self._buf[0].element_size()
+
+    @property
+    def steps_per_launch(self):
+        """Steps that ``step(n)`` advances per launch for n >= 2: 2 where the
+        two-step kernel applies to this lattice (FP32 or f32dev storage,
+        rounding to nearest, periodic or cavity walls, nx a multiple of 16,
+        ny of 256), else 1."""
+        if self.rounding == "stochastic" and self.storage in ("f16dev", "bf16dev"):
+            return 1
+        return int(_lib.load().lbgb_steps_per_launch(self.nx, self.ny, self.bcode, self.code))
 
     @property
     def state(self):
