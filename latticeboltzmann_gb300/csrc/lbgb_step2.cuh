@@ -3,26 +3,28 @@
 // population is read once and written once per two steps, 36 bytes per cell
 // update instead of 72.
 //
-// A block owns S2_R consecutive rows x S2_W columns of the output and walks
-// its rows in order.  Each f(t) row it needs (its own rows and two more on
-// either side, with four columns more on either side, both periodic) comes
-// into a ring of S2_NA shared-memory rows by 16-byte cp.async, three rows
-// ahead of use.  When row j of f(t) has landed, the block computes row j-1 of
-// f(t+1) over its columns and one more on either side (pull, walls, lid,
-// collision: the single-step kernel's arithmetic) into a ring of three
-// shared-memory rows, stored as the storage's own codes, and then row j-2 of
-// f(t+2) over its own columns from that ring, written to global memory.  The
-// rows and columns next to the block's are computed twice, by this block and
-// by its neighbour (3 % more collisions at 128 x 256); the intermediate step
-// never leaves the SM, so the results equal two single steps bit for bit.
+// A block owns `rows` (16-128) consecutive rows x S2_W columns of the output
+// and walks its rows in order, two per iteration.  Each f(t) row it needs
+// (its own rows and two more on either side, with four columns more on
+// either side, both periodic) comes into a ring of S2_NA shared-memory rows
+// by 16-byte cp.async, two rows ahead of use.  When rows j, j+1 of f(t) have
+// landed, the block computes rows j-1, j of f(t+1) over its columns and one
+// more on either side (pull, walls, lid, collision: the single-step kernel's
+// arithmetic) into a ring of S2_NB shared-memory rows, stored as the
+// storage's own codes, and then rows j-2, j-1 of f(t+2) over its own columns
+// from that ring, written to global memory: two independent cells per thread
+// and phase.  The rows and columns next to the block's are computed twice,
+// by this block and by its neighbour (3 % more collisions at 128 x 256); the
+// intermediate step never leaves the SM, so the results equal two single
+// steps bit for bit.
 #pragma once
 
 namespace lbgb {
 
 constexpr int S2_W = 256;                 // output columns per block
-constexpr int S2_THREADS = 256;           // one output column per thread
-constexpr int S2_NA = 6;                  // f(t) ring: three rows in use, three in flight
-constexpr int S2_NB = 3;                  // f(t+1) ring
+constexpr int S2_THREADS = 288;           // one column of each of two rows per thread (258 for step t+1)
+constexpr int S2_NA = 6;                  // f(t) ring: four rows in use, two in flight
+constexpr int S2_NB = 4;                  // f(t+1) ring
 constexpr int S2_PITCH = S2_W + 8;        // columns Y0-4 .. Y0+W+3 of a channel row
 constexpr int S2_VROW = S2_W / 4 + 2;     // 16-byte copies per channel row (main + two halos)
 constexpr size_t S2_SMEM = (size_t)(S2_NA + S2_NB) * 9 * S2_PITCH * 4;
@@ -109,45 +111,53 @@ k_step2(const typename Codec<DT>::raw *__restrict__ src, typename Codec<DT>::raw
     auto arow = [&](int o) { return A + (o % S2_NA) * 9 * S2_PITCH; };
     auto brow = [&](int o) { return B + (o % S2_NB) * 9 * S2_PITCH; };
 
-    const int n_in = rows + 4;
+    // iteration t: inputs 2t, 2t+1 land; step t+1 at offsets 2t-1, 2t (valid
+    // 1 .. rows+2), step t+2 at offsets 2t-2, 2t-1 (valid 2 .. rows+1)
+    const int n_in = rows + 4, iters = n_in / 2;
     issue(0);
-    cp_async_commit();
     issue(1);
     cp_async_commit();
     issue(2);
+    issue(3);
     cp_async_commit();
-    for (int j = 0; j < n_in; ++j) {
-        // the slot of input j+3 held input j-3, last read by step t+1's row
-        // j-2 before the second barrier of the previous iteration
-        if (j + 3 < n_in) issue(j + 3);
-        cp_async_commit();
-        cp_async_wait<3>();  // this thread's copies of input j have landed
+    // step t+1 column of this thread (258 of them), step t+2 column (256)
+    const bool c1 = tid < S2_W + 2, c2 = tid < S2_W;
+    int l1 = Y0 - 1 + tid;
+    if (l1 < 0) l1 += ny;
+    if (l1 >= ny) l1 -= ny;
+    const int sc1 = 3 + tid, l2 = Y0 + tid, sc2 = 4 + tid;
+    for (int t = 0; t < iters; ++t) {
+        cp_async_wait<1>();  // this thread's copies of inputs 2t, 2t+1 have landed
         __syncthreads();     // ... everyone's; and the previous iteration is done
-        if (j >= 2) {
-            // step t+1, row j-1 (offset), columns Y0-1 .. Y0+W (periodic)
-            const int o = j - 1, k = row_of(o);
-            const raw *r0 = arow(o - 1), *r1 = arow(o), *r2 = arow(o + 1);
-            raw *b = brow(o);
-            for (int c = tid; c < S2_W + 2; c += S2_THREADS) {
-                int l = Y0 - 1 + c;
-                if (l < 0) l += ny;
-                if (l >= ny) l -= ny;
-                const int sc = 3 + c;
-                raw out[9];
-                s2_cell<DT, BC>(r0, r1, r2, sc, k, l, nx, ny, omega, u0, out);
+        if (t >= 1 && c1) {
+            const int oa = 2 * t - 1, ob = 2 * t;
+            raw outa[9], outb[9];
+            s2_cell<DT, BC>(arow(oa - 1), arow(oa), arow(oa + 1), sc1, row_of(oa), l1, nx, ny, omega, u0, outa);
+            s2_cell<DT, BC>(arow(ob - 1), arow(ob), arow(ob + 1), sc1, row_of(ob), l1, nx, ny, omega, u0, outb);
+            raw *ba = brow(oa), *bb = brow(ob);
 #pragma unroll
-                for (int ch = 0; ch < 9; ++ch) b[ch * S2_PITCH + sc] = out[ch];
+            for (int ch = 0; ch < 9; ++ch) {
+                ba[ch * S2_PITCH + sc1] = outa[ch];
+                bb[ch * S2_PITCH + sc1] = outb[ch];
             }
         }
         __syncthreads();
-        if (j >= 4) {
-            // step t+2, row j-2 (offset) = lattice row X0 + j - 4, own columns
-            const int o = j - 2, k = row_of(o), l = Y0 + tid, sc = 4 + tid;
-            raw out[9];
-            s2_cell<DT, BC>(brow(o - 1), brow(o), brow(o + 1), sc, k, l, nx, ny, omega, u0, out);
-            raw *d = dst + (size_t)k * ny + l;
+        // the slots of inputs 2t+4, 2t+5 held inputs 2t-2, 2t-1, last read by
+        // step t+1 above; they land during step t+2 and the next iteration's wait
+        if (2 * t + 4 < n_in) issue(2 * t + 4);
+        if (2 * t + 5 < n_in) issue(2 * t + 5);
+        cp_async_commit();
+        if (t >= 2 && c2) {
+            const int oa = 2 * t - 2, ob = 2 * t - 1, ka = row_of(oa), kb = row_of(ob);
+            raw outa[9], outb[9];
+            s2_cell<DT, BC>(brow(oa - 1), brow(oa), brow(oa + 1), sc2, ka, l2, nx, ny, omega, u0, outa);
+            s2_cell<DT, BC>(brow(ob - 1), brow(ob), brow(ob + 1), sc2, kb, l2, nx, ny, omega, u0, outb);
+            raw *da = dst + (size_t)ka * ny + l2, *db = dst + (size_t)kb * ny + l2;
 #pragma unroll
-            for (int ch = 0; ch < 9; ++ch) d[ch * cs] = out[ch];
+            for (int ch = 0; ch < 9; ++ch) {
+                da[ch * cs] = outa[ch];
+                db[ch * cs] = outb[ch];
+            }
         }
     }
 }
