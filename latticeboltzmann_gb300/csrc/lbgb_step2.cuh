@@ -46,10 +46,17 @@ __device__ __forceinline__ void s2_cell(const typename Codec<DT>::raw *r0, const
     };
     real v[9];
     v[0] = at(C0, 0, 0);
+    if (BC == LBGB_PERIODIC || (k != 0 && k != nx - 1)) {
+        // every row but the two wall rows (k is the same for the whole block:
+        // a uniform branch, one load per value)
 #pragma unroll
-    for (int ch = 1; ch < 9; ++ch) {
-        const bool wall = BC != LBGB_PERIODIC && ((cx(ch) > 0 && k == 0) || (cx(ch) < 0 && k == nx - 1));
-        v[ch] = wall ? C::dec(r1[opp(ch) * S2_PITCH + sc], ch) : at(ch, -cx(ch), -cy(ch));
+        for (int ch = 1; ch < 9; ++ch) v[ch] = at(ch, -cx(ch), -cy(ch));
+    } else {
+#pragma unroll
+        for (int ch = 1; ch < 9; ++ch) {
+            const bool wall = (cx(ch) > 0 && k == 0) || (cx(ch) < 0 && k == nx - 1);
+            v[ch] = wall ? C::dec(r1[opp(ch) * S2_PITCH + sc], ch) : at(ch, -cx(ch), -cy(ch));
+        }
     }
     if (BC != LBGB_PERIODIC) {
         if (l == 0) {
