@@ -5,76 +5,114 @@
 //
 // A block owns `rows` (16-128) consecutive rows x S2_W columns of the output
 // and walks its rows in order, two per iteration.  Each f(t) row it needs
-// (its own rows and two more on either side, with four columns more on
+// (its own rows and two more on either side, with eight columns more on
 // either side, both periodic) comes into a ring of S2_NA shared-memory rows
 // by 16-byte cp.async, two rows ahead of use.  When rows j, j+1 of f(t) have
-// landed, the block computes rows j-1, j of f(t+1) over its columns and one
+// landed, the block computes rows j-1, j of f(t+1) over its columns and four
 // more on either side (pull, walls, lid, collision: the single-step kernel's
 // arithmetic) into a ring of S2_NB shared-memory rows, stored as the
 // storage's own codes, and then rows j-2, j-1 of f(t+2) over its own columns
-// from that ring, written to global memory: two independent cells per thread
-// and phase.  The rows and columns next to the block's are computed twice,
-// by this block and by its neighbour (3 % more collisions at 128 x 256); the
-// intermediate step never leaves the SM, so the results equal two single
-// steps bit for bit.
+// from that ring, written to global memory.  A thread computes four
+// consecutive cells of a row (16-byte shared loads plus one edge value for
+// the channels that move along y; 16-byte stores).  The rows and columns
+// next to the block's are computed twice, by this block and by its
+// neighbour (~5 % more collisions at 128 x 256); the intermediate step never
+// leaves the SM, so the results equal two single steps bit for bit.
 #pragma once
 
 namespace lbgb {
 
 constexpr int S2_W = 256;                 // output columns per block
-constexpr int S2_THREADS = 288;           // one column of each of two rows per thread (258 for step t+1)
+constexpr int S2_HV = 2;                  // halo vectors (4 columns each) per side
+constexpr int S2_NV = S2_W / 4;           // output vectors per row (64)
+constexpr int S2_NV1 = S2_NV + 2;         // step t+1 vectors per row: one more per side (66)
+constexpr int S2_THREADS = 160;           // 2 rows x 66 step t+1 vectors, 2 x 64 step t+2 vectors
 constexpr int S2_NA = 6;                  // f(t) ring: four rows in use, two in flight
 constexpr int S2_NB = 4;                  // f(t+1) ring
-constexpr int S2_PITCH = S2_W + 8;        // columns Y0-4 .. Y0+W+3 of a channel row
-constexpr int S2_VROW = S2_W / 4 + 2;     // 16-byte copies per channel row (main + two halos)
+constexpr int S2_PITCH = S2_W + 8 * S2_HV;  // columns Y0-8 .. Y0+W+7 of a channel row
+constexpr int S2_VROW = S2_NV + 2 * S2_HV;  // 16-byte copies per channel row
 constexpr size_t S2_SMEM = (size_t)(S2_NA + S2_NB) * 9 * S2_PITCH * 4;
 
-// One cell's pull (walls and lid as the single-step kernel), collision and
-// encode.  r0, r1, r2: the shared rows of the source step at rows k-1, k, k+1
-// (channel-major, S2_PITCH apart); sc: the cell's shared column; k, l: its
-// lattice row and column.
+// Four consecutive cells (one 16-byte vector) of one row: pull (walls and lid
+// as the single-step kernel), collision and encode.  r0, r1, r2: the shared
+// rows of the source step at rows k-1, k, k+1 (channel-major, S2_PITCH
+// apart); sc: the shared column of the first cell; k, l0: its lattice row
+// and column (l0 a multiple of 4).
 template <int DT, int BC>
-__device__ __forceinline__ void s2_cell(const typename Codec<DT>::raw *r0, const typename Codec<DT>::raw *r1,
-                                        const typename Codec<DT>::raw *r2, int sc, int k, int l, int nx, int ny,
-                                        typename Codec<DT>::real omega, typename Codec<DT>::real u0,
-                                        typename Codec<DT>::raw (&out)[9]) {
+__device__ __forceinline__ void s2_vec(const typename Codec<DT>::raw *r0, const typename Codec<DT>::raw *r1,
+                                       const typename Codec<DT>::raw *r2, int sc, int k, int l0, int nx, int ny,
+                                       typename Codec<DT>::real omega, typename Codec<DT>::real u0,
+                                       typename Codec<DT>::raw (&out)[9][4]) {
     using C = Codec<DT>;
+    using raw = typename C::raw;
     using real = typename C::real;
-    auto at = [&](int ch, int dr, int dc) {
-        const typename C::raw *r = dr < 0 ? r0 : (dr > 0 ? r2 : r1);
-        return C::dec(r[ch * S2_PITCH + sc + dc], ch);
+    real v[9][4];
+    auto vec = [&](const raw *r, int ch, real (&o)[4], int dch) {
+        const float4 q = *reinterpret_cast<const float4 *>(r + ch * S2_PITCH + sc);
+        o[0] = C::dec(q.x, dch);
+        o[1] = C::dec(q.y, dch);
+        o[2] = C::dec(q.z, dch);
+        o[3] = C::dec(q.w, dch);
     };
-    real v[9];
-    v[0] = at(C0, 0, 0);
-    if (BC == LBGB_PERIODIC || (k != 0 && k != nx - 1)) {
-        // every row but the two wall rows (k is the same for the whole block:
-        // a uniform branch, one load per value)
 #pragma unroll
-        for (int ch = 1; ch < 9; ++ch) v[ch] = at(ch, -cx(ch), -cy(ch));
-    } else {
-#pragma unroll
-        for (int ch = 1; ch < 9; ++ch) {
-            const bool wall = (cx(ch) > 0 && k == 0) || (cx(ch) < 0 && k == nx - 1);
-            v[ch] = wall ? C::dec(r1[opp(ch) * S2_PITCH + sc], ch) : at(ch, -cx(ch), -cy(ch));
+    for (int ch = 0; ch < 9; ++ch) {
+        const raw *rp = cx(ch) > 0 ? r0 : (cx(ch) < 0 ? r2 : r1);
+        const float4 q = *reinterpret_cast<const float4 *>(rp + ch * S2_PITCH + sc);
+        if (cy(ch) > 0) {
+            v[ch][0] = C::dec(rp[ch * S2_PITCH + sc - 1], ch);
+            v[ch][1] = C::dec(q.x, ch);
+            v[ch][2] = C::dec(q.y, ch);
+            v[ch][3] = C::dec(q.z, ch);
+        } else if (cy(ch) < 0) {
+            v[ch][0] = C::dec(q.y, ch);
+            v[ch][1] = C::dec(q.z, ch);
+            v[ch][2] = C::dec(q.w, ch);
+            v[ch][3] = C::dec(rp[ch * S2_PITCH + sc + 4], ch);
+        } else {
+            v[ch][0] = C::dec(q.x, ch);
+            v[ch][1] = C::dec(q.y, ch);
+            v[ch][2] = C::dec(q.z, ch);
+            v[ch][3] = C::dec(q.w, ch);
         }
     }
     if (BC != LBGB_PERIODIC) {
-        if (l == 0) {
-            v[CN] = C::dec(r1[CS * S2_PITCH + sc], CN);
-            v[CNE] = C::dec(r1[CSW * S2_PITCH + sc], CNE);
-            v[CNW] = C::dec(r1[CSE * S2_PITCH + sc], CNW);
+        if (k == 0 || k == nx - 1) {
+            // side-wall rows: bounce-back from the same node, decoded as ch
+#pragma unroll
+            for (int ch = 1; ch < 9; ++ch)
+                if ((cx(ch) > 0 && k == 0) || (cx(ch) < 0 && k == nx - 1)) vec(r1, opp(ch), v[ch], ch);
         }
-        if (l == ny - 1) {
-            const real gN = at(CN, 0, 0), gNW = at(CNW, 0, 0), gNE = at(CNE, 0, 0);
-            const real rho_lid = gNW + gN + gNE + at(CNW, 1, -1) + at(CN, 0, -1) + at(CNE, -1, -1) + at(CW, 1, 0) +
-                                 at(C0, 0, 0) + at(CE, -1, 0);
+        if (l0 == 0) {
+            // bottom wall: N, NE, NW bounce back from the same node
+            v[CN][0] = C::dec(r1[CS * S2_PITCH + sc], CN);
+            v[CNE][0] = C::dec(r1[CSW * S2_PITCH + sc], CNE);
+            v[CNW][0] = C::dec(r1[CSE * S2_PITCH + sc], CNW);
+        }
+        if (l0 + 3 == ny - 1) {
+            // lid (the vector's last cell): the single-step kernel's rule and sum order
+            const int s3 = sc + 3;
+            const real gN = C::dec(r1[CN * S2_PITCH + s3], CN), gNW = C::dec(r1[CNW * S2_PITCH + s3], CNW),
+                       gNE = C::dec(r1[CNE * S2_PITCH + s3], CNE);
+            const real rho_lid = gNW + gN + gNE + C::dec(r2[CNW * S2_PITCH + s3 - 1], CNW) +
+                                 C::dec(r1[CN * S2_PITCH + s3 - 1], CN) + C::dec(r0[CNE * S2_PITCH + s3 - 1], CNE) +
+                                 C::dec(r2[CW * S2_PITCH + s3], CW) + C::dec(r1[C0 * S2_PITCH + s3], C0) +
+                                 C::dec(r0[CE * S2_PITCH + s3], CE);
             const real lid = lid_from_sum<C>(rho_lid, u0);
-            v[CS] = gN;
-            v[CSE] = (k == 0) ? gNW : gNW + lid;
-            v[CSW] = (k == nx - 1) ? gNE : gNE - lid;
+            v[CS][3] = gN;
+            v[CSE][3] = (k == 0) ? gNW : gNW + lid;
+            v[CSW][3] = (k == nx - 1) ? gNE : gNE - lid;
         }
     }
-    collide_encode<DT>(v, omega, out);
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+        real f[9];
+        raw r[9];
+#pragma unroll
+        for (int ch = 0; ch < 9; ++ch) f[ch] = v[ch][j];
+        collide_encode<DT>(f, omega, r);
+#pragma unroll
+        for (int ch = 0; ch < 9; ++ch) out[ch][j] = r[ch];
+    }
 }
 
 template <int DT, int BC>
@@ -96,23 +134,16 @@ k_step2(const typename Codec<DT>::raw *__restrict__ src, typename Codec<DT>::raw
         if (k >= nx) k -= nx;
         return k;
     };
+    // shared column 0 is lattice column Y0 - 8 (periodic)
     auto issue = [&](int o) {
         const raw *base = src + (size_t)row_of(o) * ny;
         raw *slot = A + (o % S2_NA) * 9 * S2_PITCH;
         for (int i = tid; i < 9 * S2_VROW; i += S2_THREADS) {
             const int ch = i / S2_VROW, v = i - ch * S2_VROW;
-            int gcol, scol;
-            if (v < S2_W / 4) {
-                gcol = Y0 + 4 * v;
-                scol = 4 + 4 * v;
-            } else if (v == S2_W / 4) {
-                gcol = Y0 == 0 ? ny - 4 : Y0 - 4;
-                scol = 0;
-            } else {
-                gcol = Y0 + S2_W == ny ? 0 : Y0 + S2_W;
-                scol = S2_W + 4;
-            }
-            cp_async16(slot + ch * S2_PITCH + scol, base + ch * cs + gcol);
+            int gcol = Y0 - 8 + 4 * v;
+            if (gcol < 0) gcol += ny;
+            if (gcol >= ny) gcol -= ny;
+            cp_async16(slot + ch * S2_PITCH + 4 * v, base + ch * cs + gcol);
         }
     };
     auto arow = [&](int o) { return A + (o % S2_NA) * 9 * S2_PITCH; };
@@ -127,25 +158,27 @@ k_step2(const typename Codec<DT>::raw *__restrict__ src, typename Codec<DT>::raw
     issue(2);
     issue(3);
     cp_async_commit();
-    // step t+1 column of this thread (258 of them), step t+2 column (256)
-    const bool c1 = tid < S2_W + 2, c2 = tid < S2_W;
-    int l1 = Y0 - 1 + tid;
+    // step t+1: thread -> (row r1i, vector u1) of 2 x 66, columns Y0-4 .. Y0+W+3;
+    // step t+2: thread -> (row r2i, vector u2) of 2 x 64, columns Y0 .. Y0+W-1
+    const bool c1 = tid < 2 * S2_NV1, c2 = tid < 2 * S2_NV;
+    const int r1i = tid >= S2_NV1, u1 = tid - r1i * S2_NV1;
+    const int r2i = tid >= S2_NV, u2 = tid - r2i * S2_NV;
+    int l1 = Y0 - 4 + 4 * u1;
     if (l1 < 0) l1 += ny;
     if (l1 >= ny) l1 -= ny;
-    const int sc1 = 3 + tid, l2 = Y0 + tid, sc2 = 4 + tid;
+    const int sc1 = 4 + 4 * u1, l2 = Y0 + 4 * u2, sc2 = 8 + 4 * u2;
     for (int t = 0; t < iters; ++t) {
         cp_async_wait<1>();  // this thread's copies of inputs 2t, 2t+1 have landed
         __syncthreads();     // ... everyone's; and the previous iteration is done
         if (t >= 1 && c1) {
-            const int oa = 2 * t - 1, ob = 2 * t;
-            raw outa[9], outb[9];
-            s2_cell<DT, BC>(arow(oa - 1), arow(oa), arow(oa + 1), sc1, row_of(oa), l1, nx, ny, omega, u0, outa);
-            s2_cell<DT, BC>(arow(ob - 1), arow(ob), arow(ob + 1), sc1, row_of(ob), l1, nx, ny, omega, u0, outb);
-            raw *ba = brow(oa), *bb = brow(ob);
+            const int o = 2 * t - 1 + r1i;
+            raw out[9][4];
+            s2_vec<DT, BC>(arow(o - 1), arow(o), arow(o + 1), sc1, row_of(o), l1, nx, ny, omega, u0, out);
+            raw *b = brow(o);
 #pragma unroll
             for (int ch = 0; ch < 9; ++ch) {
-                ba[ch * S2_PITCH + sc1] = outa[ch];
-                bb[ch * S2_PITCH + sc1] = outb[ch];
+                *reinterpret_cast<float4 *>(b + ch * S2_PITCH + sc1) =
+                    make_float4(out[ch][0], out[ch][1], out[ch][2], out[ch][3]);
             }
         }
         __syncthreads();
@@ -155,16 +188,13 @@ k_step2(const typename Codec<DT>::raw *__restrict__ src, typename Codec<DT>::raw
         if (2 * t + 5 < n_in) issue(2 * t + 5);
         cp_async_commit();
         if (t >= 2 && c2) {
-            const int oa = 2 * t - 2, ob = 2 * t - 1, ka = row_of(oa), kb = row_of(ob);
-            raw outa[9], outb[9];
-            s2_cell<DT, BC>(brow(oa - 1), brow(oa), brow(oa + 1), sc2, ka, l2, nx, ny, omega, u0, outa);
-            s2_cell<DT, BC>(brow(ob - 1), brow(ob), brow(ob + 1), sc2, kb, l2, nx, ny, omega, u0, outb);
-            raw *da = dst + (size_t)ka * ny + l2, *db = dst + (size_t)kb * ny + l2;
+            const int o = 2 * t - 2 + r2i, k = row_of(o);
+            raw out[9][4];
+            s2_vec<DT, BC>(brow(o - 1), brow(o), brow(o + 1), sc2, k, l2, nx, ny, omega, u0, out);
+            raw *d = dst + (size_t)k * ny + l2;
 #pragma unroll
-            for (int ch = 0; ch < 9; ++ch) {
-                da[ch * cs] = outa[ch];
-                db[ch * cs] = outb[ch];
-            }
+            for (int ch = 0; ch < 9; ++ch)
+                *reinterpret_cast<float4 *>(d + ch * cs) = make_float4(out[ch][0], out[ch][1], out[ch][2], out[ch][3]);
         }
     }
 }
