@@ -166,7 +166,7 @@ LBGB_API int lbgb_step_fused_rows(const void *src, void *dst, int nx, int ny, in
  * state); *which receives 0 if the result is in a, 1 if in b.  Launch-only:
  * suitable for CUDA-graph capture.  Where lbgb_steps_per_launch says 2
  * (LBGB_F32 or LBGB_F32DEV storage, periodic or cavity walls, nx a multiple
- * of 16, ny of 256, 16-byte aligned buffers, LBGB_TUNE_TWO_STEP on and the
+ * of 16, ny of 128, 16-byte aligned buffers, LBGB_TUNE_TWO_STEP on and the
  * auto kernel), pairs of steps run as one launch that keeps the intermediate
  * step on chip (k_step2: one read and one write of the lattice per two
  * steps); the results equal single steps bit for bit. */

@@ -16,17 +16,18 @@
 // consecutive cells of a row (16-byte shared loads plus one edge value for
 // the channels that move along y; 16-byte stores).  The rows and columns
 // next to the block's are computed twice, by this block and by its
-// neighbour (~5 % more collisions at 128 x 256); the intermediate step never
+// neighbour (~8 % more collisions at 128 x 128); the intermediate step never
 // leaves the SM, so the results equal two single steps bit for bit.
 #pragma once
 
 namespace lbgb {
 
-constexpr int S2_W = 256;                 // output columns per block
+constexpr int S2_W = 128;                 // output columns per block
 constexpr int S2_HV = 2;                  // halo vectors (4 columns each) per side
-constexpr int S2_NV = S2_W / 4;           // output vectors per row (64)
-constexpr int S2_NV1 = S2_NV + 2;         // step t+1 vectors per row: one more per side (66)
-constexpr int S2_THREADS = 160;           // 2 rows x 66 step t+1 vectors, 2 x 64 step t+2 vectors
+constexpr int S2_NV = S2_W / 4;           // output vectors per row (32)
+constexpr int S2_NV1 = S2_NV + 2;         // step t+1 vectors per row: one more per side (34)
+constexpr int S2_THREADS = 96;            // 2 rows x 34 step t+1 vectors, 2 x 32 step t+2 vectors
+constexpr int S2_MIN_BLOCKS = 4;          // resident blocks per SM (52 KB of shared memory each)
 constexpr int S2_NA = 6;                  // f(t) ring: four rows in use, two in flight
 constexpr int S2_NB = 4;                  // f(t+1) ring
 constexpr int S2_PITCH = S2_W + 8 * S2_HV;  // columns Y0-8 .. Y0+W+7 of a channel row
@@ -116,7 +117,7 @@ __device__ __forceinline__ void s2_vec(const typename Codec<DT>::raw *r0, const 
 }
 
 template <int DT, int BC>
-__global__ void __launch_bounds__(S2_THREADS, 2)
+__global__ void __launch_bounds__(S2_THREADS, S2_MIN_BLOCKS)
 k_step2(const typename Codec<DT>::raw *__restrict__ src, typename Codec<DT>::raw *__restrict__ dst, int nx, int ny,
         int rows, typename Codec<DT>::real omega, typename Codec<DT>::real u0) {
     using raw = typename Codec<DT>::raw;
@@ -158,8 +159,8 @@ k_step2(const typename Codec<DT>::raw *__restrict__ src, typename Codec<DT>::raw
     issue(2);
     issue(3);
     cp_async_commit();
-    // step t+1: thread -> (row r1i, vector u1) of 2 x 66, columns Y0-4 .. Y0+W+3;
-    // step t+2: thread -> (row r2i, vector u2) of 2 x 64, columns Y0 .. Y0+W-1
+    // step t+1: thread -> (row r1i, vector u1) of 2 x S2_NV1, columns Y0-4 .. Y0+W+3;
+    // step t+2: thread -> (row r2i, vector u2) of 2 x S2_NV, columns Y0 .. Y0+W-1
     const bool c1 = tid < 2 * S2_NV1, c2 = tid < 2 * S2_NV;
     const int r1i = tid >= S2_NV1, u1 = tid - r1i * S2_NV1;
     const int r2i = tid >= S2_NV, u2 = tid - r2i * S2_NV;
