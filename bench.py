@@ -3,7 +3,9 @@
 
 Workload (default): lid-driven cavity, 8192 x 8192 cells, FP32 populations,
 omega = 1.7, lid velocity 0.1, from rest at equilibrium.  One step = one
-fused pull-stream + collide pass over the whole lattice (one kernel launch).
+fused pull-stream + collide update of the whole lattice; the solver runs two
+steps per kernel launch where its two-step kernel applies (FP32 and f32dev
+storage: one read and one write of the lattice per two steps), else one.
 Metric: MLUPS (million lattice-cell updates per second, physical cells only).
 
 Lines printed (rank 0, one JSON line):
@@ -14,8 +16,9 @@ Lines printed (rank 0, one JSON line):
              copies them back, inside the timed region (Lattice.step_host:
              the three overlap by blocks of rows); e2e.link is the ceiling
              the host link sets, the same bytes copied both ways at once
-  roofline   HBM roofline of the fused kernel: 72 B/cell/step (FP32) or
-             36 B (16-bit deviations) over its CUDA-event launch time
+  roofline   HBM roofline of the fused kernel: the lattice bytes of one
+             launch (72 B/cell FP32, 36 B 16-bit deviations; a launch is two
+             steps for the two-step kernel) over its CUDA-event launch time
   cpu_baseline  the oracle's C port of the reference step on the host cores;
              cpu_baseline.numpy_opt1: the reference's numpy step, one process
              per host core
@@ -386,16 +389,16 @@ def run_ours(args):
     lat = PyLB.Lattice(args.nx, args.ny, args.omega, boundary=args.boundary, u0=args.u0, storage=args.storage,
                        device=dev, rounding=args.rounding)
     stream = torch.cuda.current_stream(dev)
-    for _ in range(args.warmup):
-        lat.step(1)
+    # one launch per event: two steps each where the two-step kernel applies
+    chunk = lat.steps_per_launch if args.steps % lat.steps_per_launch == 0 else 1
+    launches = args.steps // chunk
+    for _ in range(args.warmup):  # warm-up launches of the timed kernel
+        lat.step(chunk)
     torch.cuda.synchronize(dev)
 
     clocks = ClockSampler(d.local_rank)
     if d.rank == 0:
         clocks.start()
-    # one launch per event: two steps each where the two-step kernel applies
-    chunk = lat.steps_per_launch if args.steps % lat.steps_per_launch == 0 else 1
-    launches = args.steps // chunk
     ev = [torch.cuda.Event(enable_timing=True) for _ in range(launches + 1)]
     d.barrier()
     torch.cuda.synchronize(dev)
