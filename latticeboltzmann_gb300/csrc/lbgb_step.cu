@@ -308,7 +308,8 @@ static int step2_rows(int nx) {
 }
 
 static bool step2_applies(const void *src, const void *dst, int nx, int ny, int boundary, int dtype) {
-    return g_tune.two_step && g_tune.kernel == 0 && (dtype == LBGB_F32 || dtype == LBGB_F32DEV) &&
+    return g_tune.two_step && g_tune.kernel == 0 &&
+           (dtype == LBGB_F32 || dtype == LBGB_F32DEV || dtype == LBGB_F16DEV || dtype == LBGB_BF16DEV) &&
            (boundary == LBGB_PERIODIC || boundary == LBGB_CAVITY) && step2_rows(nx) && ny % S2_W == 0 &&
            ny / S2_W <= 65535 && (!src || aligned(src, 16)) && (!dst || aligned(dst, 16));
 }
@@ -321,15 +322,16 @@ static int launch_step2(const void *src, void *dst, int nx, int ny, double omega
     if (!attr_set[dev].load(std::memory_order_acquire)) {
         std::lock_guard<std::mutex> lock(setup_mutex());
         const cudaError_t e =
-            cudaFuncSetAttribute(k_step2<DT, BC>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)S2_SMEM);
+            cudaFuncSetAttribute(k_step2<DT, BC>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)S2Geom<raw>::SMEM);
         if (e != cudaSuccess) {
-            set_error("k_step2: cannot reserve %zu bytes of shared memory: %s", S2_SMEM, cudaGetErrorString(e));
+            set_error("k_step2: cannot reserve %zu bytes of shared memory: %s", S2Geom<raw>::SMEM,
+                      cudaGetErrorString(e));
             return LBGB_ECUDA;
         }
         attr_set[dev].store(true, std::memory_order_release);
     }
     const int rows = step2_rows(nx);
-    k_step2<DT, BC><<<dim3(nx / rows, ny / S2_W), S2_THREADS, S2_SMEM, s>>>(
+    k_step2<DT, BC><<<dim3(nx / rows, ny / S2_W), S2_THREADS, S2Geom<raw>::SMEM, s>>>(
         static_cast<const raw *>(src), static_cast<raw *>(dst), nx, ny, rows, (typename Codec<DT>::real)omega,
         (typename Codec<DT>::real)u0);
     return check_launch("k_step2");
@@ -340,11 +342,21 @@ static int launch_step2(const void *src, void *dst, int nx, int ny, double omega
 static int step2(const void *src, void *dst, int nx, int ny, int boundary, double omega, double u0, int dtype,
                  cudaStream_t s) {
     if (!step2_applies(src, dst, nx, ny, boundary, dtype)) return 1;
-    if (dtype == LBGB_F32)
-        return boundary == LBGB_CAVITY ? launch_step2<LBGB_F32, LBGB_CAVITY>(src, dst, nx, ny, omega, u0, s)
-                                       : launch_step2<LBGB_F32, LBGB_PERIODIC>(src, dst, nx, ny, omega, 0.0, s);
-    return boundary == LBGB_CAVITY ? launch_step2<LBGB_F32DEV, LBGB_CAVITY>(src, dst, nx, ny, omega, u0, s)
-                                   : launch_step2<LBGB_F32DEV, LBGB_PERIODIC>(src, dst, nx, ny, omega, 0.0, s);
+    const bool cav = boundary == LBGB_CAVITY;
+    switch (dtype) {
+    case LBGB_F32:
+        return cav ? launch_step2<LBGB_F32, LBGB_CAVITY>(src, dst, nx, ny, omega, u0, s)
+                   : launch_step2<LBGB_F32, LBGB_PERIODIC>(src, dst, nx, ny, omega, 0.0, s);
+    case LBGB_F32DEV:
+        return cav ? launch_step2<LBGB_F32DEV, LBGB_CAVITY>(src, dst, nx, ny, omega, u0, s)
+                   : launch_step2<LBGB_F32DEV, LBGB_PERIODIC>(src, dst, nx, ny, omega, 0.0, s);
+    case LBGB_F16DEV:
+        return cav ? launch_step2<LBGB_F16DEV, LBGB_CAVITY>(src, dst, nx, ny, omega, u0, s)
+                   : launch_step2<LBGB_F16DEV, LBGB_PERIODIC>(src, dst, nx, ny, omega, 0.0, s);
+    default:
+        return cav ? launch_step2<LBGB_BF16DEV, LBGB_CAVITY>(src, dst, nx, ny, omega, u0, s)
+                   : launch_step2<LBGB_BF16DEV, LBGB_PERIODIC>(src, dst, nx, ny, omega, 0.0, s);
+    }
 }
 
 template <int DT, int BC, bool COLLIDE>

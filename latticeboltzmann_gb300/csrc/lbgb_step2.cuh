@@ -1,7 +1,8 @@
-// Two time steps per pass over the lattice (temporal blocking), for 4-byte
-// storage (LBGB_F32, LBGB_F32DEV) with periodic or cavity walls: every
-// population is read once and written once per two steps, 36 bytes per cell
-// update instead of 72.
+// Two time steps per pass over the lattice (temporal blocking), for FP32,
+// f32dev and the 16-bit deviation storages (rounding to nearest) with
+// periodic or cavity walls: every population is read once and written once
+// per two steps, 36 bytes per FP32 cell update instead of 72 (18 instead of
+// 36 for 16-bit codes).
 //
 // A block owns `rows` (16-128) consecutive rows x S2_W columns of the output
 // and walks its rows in order, two per iteration.  Each f(t) row it needs
@@ -23,16 +24,42 @@
 namespace lbgb {
 
 constexpr int S2_W = 128;                 // output columns per block
-constexpr int S2_HV = 2;                  // halo vectors (4 columns each) per side
-constexpr int S2_NV = S2_W / 4;           // output vectors per row (32)
+constexpr int S2_NV = S2_W / 4;           // output four-cell vectors per row (32)
 constexpr int S2_NV1 = S2_NV + 2;         // step t+1 vectors per row: one more per side (34)
 constexpr int S2_THREADS = 96;            // 2 rows x 34 step t+1 vectors, 2 x 32 step t+2 vectors
-constexpr int S2_MIN_BLOCKS = 4;          // resident blocks per SM (52 KB of shared memory each)
 constexpr int S2_NA = 6;                  // f(t) ring: four rows in use, two in flight
 constexpr int S2_NB = 4;                  // f(t+1) ring
-constexpr int S2_PITCH = S2_W + 8 * S2_HV;  // columns Y0-8 .. Y0+W+7 of a channel row
-constexpr int S2_VROW = S2_NV + 2 * S2_HV;  // 16-byte copies per channel row
-constexpr size_t S2_SMEM = (size_t)(S2_NA + S2_NB) * 9 * S2_PITCH * 4;
+constexpr int S2_PITCH = S2_W + 16;       // columns Y0-8 .. Y0+W+7 of a channel row (elements)
+
+// Per storage size: 16-byte copies per channel row, shared memory per block
+// and resident blocks per SM (4-byte codes: 52 KB, four; 2-byte: 26 KB, six
+// -- the register limit of 96-thread blocks).
+template <class raw>
+struct S2Geom {
+    static constexpr int VL = 16 / (int)sizeof(raw);  // codes per 16-byte copy
+    static constexpr int VROW = S2_PITCH / VL;
+    static constexpr size_t SMEM = (size_t)(S2_NA + S2_NB) * 9 * S2_PITCH * sizeof(raw);
+    static constexpr int MIN_BLOCKS = sizeof(raw) == 4 ? 4 : 6;
+};
+
+// Four consecutive codes of a shared row (16 bytes of 4-byte codes, 8 of
+// 2-byte codes; aligned).
+__device__ __forceinline__ void s2_ld4(const float *p, float (&o)[4]) {
+    const float4 q = *reinterpret_cast<const float4 *>(p);
+    o[0] = q.x, o[1] = q.y, o[2] = q.z, o[3] = q.w;
+}
+__device__ __forceinline__ void s2_ld4(const unsigned short *p, unsigned short (&o)[4]) {
+    const uint2 q = *reinterpret_cast<const uint2 *>(p);
+    o[0] = (unsigned short)(q.x & 0xffffu), o[1] = (unsigned short)(q.x >> 16);
+    o[2] = (unsigned short)(q.y & 0xffffu), o[3] = (unsigned short)(q.y >> 16);
+}
+__device__ __forceinline__ void s2_st4(float *p, const float (&x)[4]) {
+    *reinterpret_cast<float4 *>(p) = make_float4(x[0], x[1], x[2], x[3]);
+}
+__device__ __forceinline__ void s2_st4(unsigned short *p, const unsigned short (&x)[4]) {
+    *reinterpret_cast<uint2 *>(p) = make_uint2((uint32_t)x[0] | ((uint32_t)x[1] << 16),
+                                               (uint32_t)x[2] | ((uint32_t)x[3] << 16));
+}
 
 // Four consecutive cells (one 16-byte vector) of one row: pull (walls and lid
 // as the single-step kernel), collision and encode.  r0, r1, r2: the shared
@@ -49,31 +76,29 @@ __device__ __forceinline__ void s2_vec(const typename Codec<DT>::raw *r0, const 
     using real = typename C::real;
     real v[9][4];
     auto vec = [&](const raw *r, int ch, real (&o)[4], int dch) {
-        const float4 q = *reinterpret_cast<const float4 *>(r + ch * S2_PITCH + sc);
-        o[0] = C::dec(q.x, dch);
-        o[1] = C::dec(q.y, dch);
-        o[2] = C::dec(q.z, dch);
-        o[3] = C::dec(q.w, dch);
+        raw q[4];
+        s2_ld4(r + ch * S2_PITCH + sc, q);
+#pragma unroll
+        for (int j = 0; j < 4; ++j) o[j] = C::dec(q[j], dch);
     };
 #pragma unroll
     for (int ch = 0; ch < 9; ++ch) {
         const raw *rp = cx(ch) > 0 ? r0 : (cx(ch) < 0 ? r2 : r1);
-        const float4 q = *reinterpret_cast<const float4 *>(rp + ch * S2_PITCH + sc);
+        raw q[4];
+        s2_ld4(rp + ch * S2_PITCH + sc, q);
         if (cy(ch) > 0) {
             v[ch][0] = C::dec(rp[ch * S2_PITCH + sc - 1], ch);
-            v[ch][1] = C::dec(q.x, ch);
-            v[ch][2] = C::dec(q.y, ch);
-            v[ch][3] = C::dec(q.z, ch);
+            v[ch][1] = C::dec(q[0], ch);
+            v[ch][2] = C::dec(q[1], ch);
+            v[ch][3] = C::dec(q[2], ch);
         } else if (cy(ch) < 0) {
-            v[ch][0] = C::dec(q.y, ch);
-            v[ch][1] = C::dec(q.z, ch);
-            v[ch][2] = C::dec(q.w, ch);
+            v[ch][0] = C::dec(q[1], ch);
+            v[ch][1] = C::dec(q[2], ch);
+            v[ch][2] = C::dec(q[3], ch);
             v[ch][3] = C::dec(rp[ch * S2_PITCH + sc + 4], ch);
         } else {
-            v[ch][0] = C::dec(q.x, ch);
-            v[ch][1] = C::dec(q.y, ch);
-            v[ch][2] = C::dec(q.z, ch);
-            v[ch][3] = C::dec(q.w, ch);
+#pragma unroll
+            for (int j = 0; j < 4; ++j) v[ch][j] = C::dec(q[j], ch);
         }
     }
     if (BC != LBGB_PERIODIC) {
@@ -117,11 +142,11 @@ __device__ __forceinline__ void s2_vec(const typename Codec<DT>::raw *r0, const 
 }
 
 template <int DT, int BC>
-__global__ void __launch_bounds__(S2_THREADS, S2_MIN_BLOCKS)
+__global__ void __launch_bounds__(S2_THREADS, S2Geom<typename Codec<DT>::raw>::MIN_BLOCKS)
 k_step2(const typename Codec<DT>::raw *__restrict__ src, typename Codec<DT>::raw *__restrict__ dst, int nx, int ny,
         int rows, typename Codec<DT>::real omega, typename Codec<DT>::real u0) {
     using raw = typename Codec<DT>::raw;
-    static_assert(sizeof(raw) == 4, "four-byte storage");
+    using G = S2Geom<raw>;
     extern __shared__ __align__(16) unsigned char s2_smem[];
     raw *A = reinterpret_cast<raw *>(s2_smem);
     raw *B = A + S2_NA * 9 * S2_PITCH;
@@ -139,12 +164,12 @@ k_step2(const typename Codec<DT>::raw *__restrict__ src, typename Codec<DT>::raw
     auto issue = [&](int o) {
         const raw *base = src + (size_t)row_of(o) * ny;
         raw *slot = A + (o % S2_NA) * 9 * S2_PITCH;
-        for (int i = tid; i < 9 * S2_VROW; i += S2_THREADS) {
-            const int ch = i / S2_VROW, v = i - ch * S2_VROW;
-            int gcol = Y0 - 8 + 4 * v;
+        for (int i = tid; i < 9 * G::VROW; i += S2_THREADS) {
+            const int ch = i / G::VROW, v = i - ch * G::VROW;
+            int gcol = Y0 - 8 + G::VL * v;
             if (gcol < 0) gcol += ny;
             if (gcol >= ny) gcol -= ny;
-            cp_async16(slot + ch * S2_PITCH + 4 * v, base + ch * cs + gcol);
+            cp_async16(slot + ch * S2_PITCH + G::VL * v, base + ch * cs + gcol);
         }
     };
     auto arow = [&](int o) { return A + (o % S2_NA) * 9 * S2_PITCH; };
@@ -177,10 +202,7 @@ k_step2(const typename Codec<DT>::raw *__restrict__ src, typename Codec<DT>::raw
             s2_vec<DT, BC>(arow(o - 1), arow(o), arow(o + 1), sc1, row_of(o), l1, nx, ny, omega, u0, out);
             raw *b = brow(o);
 #pragma unroll
-            for (int ch = 0; ch < 9; ++ch) {
-                *reinterpret_cast<float4 *>(b + ch * S2_PITCH + sc1) =
-                    make_float4(out[ch][0], out[ch][1], out[ch][2], out[ch][3]);
-            }
+            for (int ch = 0; ch < 9; ++ch) s2_st4(b + ch * S2_PITCH + sc1, out[ch]);
         }
         __syncthreads();
         // the slots of inputs 2t+4, 2t+5 held inputs 2t-2, 2t-1, last read by
@@ -194,8 +216,7 @@ k_step2(const typename Codec<DT>::raw *__restrict__ src, typename Codec<DT>::raw
             s2_vec<DT, BC>(brow(o - 1), brow(o), brow(o + 1), sc2, k, l2, nx, ny, omega, u0, out);
             raw *d = dst + (size_t)k * ny + l2;
 #pragma unroll
-            for (int ch = 0; ch < 9; ++ch)
-                *reinterpret_cast<float4 *>(d + ch * cs) = make_float4(out[ch][0], out[ch][1], out[ch][2], out[ch][3]);
+            for (int ch = 0; ch < 9; ++ch) s2_st4(d + ch * cs, out[ch]);
         }
     }
 }
