@@ -165,8 +165,7 @@ LBGB_API int lbgb_step_fused_rows(const void *src, void *dst, int nx, int ny, in
 /* nsteps fused steps ping-ponging between a and b (a holds the initial
  * state); *which receives 0 if the result is in a, 1 if in b.  Launch-only:
  * suitable for CUDA-graph capture.  Where lbgb_steps_per_launch says 2
- * (LBGB_F32, LBGB_F32DEV, LBGB_F16DEV or LBGB_BF16DEV storage with rounding
- * to nearest, periodic or cavity walls, nx a multiple
+ * (LBGB_F32 or LBGB_F32DEV storage, periodic or cavity walls, nx a multiple
  * of 16, ny of 128, 16-byte aligned buffers, LBGB_TUNE_TWO_STEP on and the
  * auto kernel), pairs of steps run as one launch that keeps the intermediate
  * step on chip (k_step2: one read and one write of the lattice per two

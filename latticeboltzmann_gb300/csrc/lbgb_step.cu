@@ -308,8 +308,10 @@ static int step2_rows(int nx) {
 }
 
 static bool step2_applies(const void *src, const void *dst, int nx, int ny, int boundary, int dtype) {
-    return g_tune.two_step && g_tune.kernel == 0 &&
-           (dtype == LBGB_F32 || dtype == LBGB_F32DEV || dtype == LBGB_F16DEV || dtype == LBGB_BF16DEV) &&
+    // 16-bit codes stay on the single-step kernel: issue-bound already, they
+    // measured slower with two steps per launch (8192^2 cavity: 148k against
+    // 169k MLUPS FP16, 149k against 171k BF16)
+    return g_tune.two_step && g_tune.kernel == 0 && (dtype == LBGB_F32 || dtype == LBGB_F32DEV) &&
            (boundary == LBGB_PERIODIC || boundary == LBGB_CAVITY) && step2_rows(nx) && ny % S2_W == 0 &&
            ny / S2_W <= 65535 && (!src || aligned(src, 16)) && (!dst || aligned(dst, 16));
 }
@@ -347,15 +349,9 @@ static int step2(const void *src, void *dst, int nx, int ny, int boundary, doubl
     case LBGB_F32:
         return cav ? launch_step2<LBGB_F32, LBGB_CAVITY>(src, dst, nx, ny, omega, u0, s)
                    : launch_step2<LBGB_F32, LBGB_PERIODIC>(src, dst, nx, ny, omega, 0.0, s);
-    case LBGB_F32DEV:
+    default:
         return cav ? launch_step2<LBGB_F32DEV, LBGB_CAVITY>(src, dst, nx, ny, omega, u0, s)
                    : launch_step2<LBGB_F32DEV, LBGB_PERIODIC>(src, dst, nx, ny, omega, 0.0, s);
-    case LBGB_F16DEV:
-        return cav ? launch_step2<LBGB_F16DEV, LBGB_CAVITY>(src, dst, nx, ny, omega, u0, s)
-                   : launch_step2<LBGB_F16DEV, LBGB_PERIODIC>(src, dst, nx, ny, omega, 0.0, s);
-    default:
-        return cav ? launch_step2<LBGB_BF16DEV, LBGB_CAVITY>(src, dst, nx, ny, omega, u0, s)
-                   : launch_step2<LBGB_BF16DEV, LBGB_PERIODIC>(src, dst, nx, ny, omega, 0.0, s);
     }
 }
 

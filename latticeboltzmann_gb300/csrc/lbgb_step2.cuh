@@ -1,8 +1,8 @@
-// Two time steps per pass over the lattice (temporal blocking), for FP32,
-// f32dev and the 16-bit deviation storages (rounding to nearest) with
-// periodic or cavity walls: every population is read once and written once
-// per two steps, 36 bytes per FP32 cell update instead of 72 (18 instead of
-// 36 for 16-bit codes).
+// Two time steps per pass over the lattice (temporal blocking) with periodic
+// or cavity walls: every population is read once and written once per two
+// steps, 36 bytes per FP32 cell update instead of 72.  Dispatched for FP32
+// and f32dev storage; the kernel also takes 2-byte codes (eight per 16-byte
+// copy), but the 16-bit single-step kernel is faster.
 //
 // A block owns `rows` (16-128) consecutive rows x S2_W columns of the output
 // and walks its rows in order, two per iteration.  Each f(t) row it needs

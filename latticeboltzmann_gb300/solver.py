@@ -113,9 +113,8 @@ class Lattice:
     @property
     def steps_per_launch(self):
         """Steps that ``step(n)`` advances per launch for n >= 2: 2 where the
-        two-step kernel applies to this lattice (FP32, f32dev, f16dev or
-        bf16dev storage with rounding to nearest, periodic or cavity walls,
-        nx a multiple of 16, ny of 128), else 1."""
+        two-step kernel applies to this lattice (FP32 or f32dev storage,
+        periodic or cavity walls, nx a multiple of 16, ny of 128), else 1."""
         if self.rounding == "stochastic" and self.storage in ("f16dev", "bf16dev"):
             return 1
         return int(_lib.load().lbgb_steps_per_launch(self.nx, self.ny, self.bcode, self.code))
