@@ -8,13 +8,12 @@
 // and walks its rows in order, two per iteration.  Each f(t) row it needs
 // (its own rows and two more on either side, with eight columns more on
 // either side, both periodic) comes into a ring of S2_NA shared-memory rows
-// by 16-byte cp.async, up to four rows ahead of use.  When rows j, j+1 of
-// f(t) have landed, one group of warps computes rows j-1, j of f(t+1) over
-// the block's columns and four more on either side (pull, walls, lid,
-// collision: the single-step kernel's arithmetic) into a ring of S2_NB
-// shared-memory rows, stored as the storage's own codes, while the other
-// group computes rows j-4, j-3 of f(t+2) over the block's own columns from
-// rows written earlier, to global memory: one barrier per row pair.  A thread computes four
+// by 16-byte cp.async, two rows ahead of use.  When rows j, j+1 of f(t) have
+// landed, the block computes rows j-1, j of f(t+1) over its columns and four
+// more on either side (pull, walls, lid, collision: the single-step kernel's
+// arithmetic) into a ring of S2_NB shared-memory rows, stored as the
+// storage's own codes, and then rows j-2, j-1 of f(t+2) over its own columns
+// from that ring, written to global memory.  A thread computes four
 // consecutive cells of a row (16-byte shared loads plus one edge value for
 // the channels that move along y; 16-byte stores).  The rows and columns
 // next to the block's are computed twice, by this block and by its
@@ -27,22 +26,20 @@ namespace lbgb {
 constexpr int S2_W = 128;                 // output columns per block
 constexpr int S2_NV = S2_W / 4;           // output four-cell vectors per row (32)
 constexpr int S2_NV1 = S2_NV + 2;         // step t+1 vectors per row: one more per side (34)
-constexpr int S2_T1 = 96;                 // threads of step t+1: 2 rows x 34 vectors (68 busy)
-constexpr int S2_T2 = 64;                 // threads of step t+2: 2 rows x 32 vectors
-constexpr int S2_THREADS = S2_T1 + S2_T2;
-constexpr int S2_NA = 8;                  // f(t) ring: four rows in use, four in flight
-constexpr int S2_NB = 6;                  // f(t+1) ring: two rows written, four read
+constexpr int S2_THREADS = 96;            // 2 rows x 34 step t+1 vectors, 2 x 32 step t+2 vectors
+constexpr int S2_NA = 6;                  // f(t) ring: four rows in use, two in flight
+constexpr int S2_NB = 4;                  // f(t+1) ring
 constexpr int S2_PITCH = S2_W + 16;       // columns Y0-8 .. Y0+W+7 of a channel row (elements)
 
 // Per storage size: 16-byte copies per channel row, shared memory per block
-// and resident blocks per SM (4-byte codes: 73 KB, three; 2-byte: 36 KB,
-// five -- the register limit of 160-thread blocks).
+// and resident blocks per SM (4-byte codes: 52 KB, four; 2-byte: 26 KB, six
+// -- the register limit of 96-thread blocks).
 template <class raw>
 struct S2Geom {
     static constexpr int VL = 16 / (int)sizeof(raw);  // codes per 16-byte copy
     static constexpr int VROW = S2_PITCH / VL;
     static constexpr size_t SMEM = (size_t)(S2_NA + S2_NB) * 9 * S2_PITCH * sizeof(raw);
-    static constexpr int MIN_BLOCKS = sizeof(raw) == 4 ? 3 : 5;
+    static constexpr int MIN_BLOCKS = sizeof(raw) == 4 ? 4 : 6;
 };
 
 // Four consecutive codes of a shared row (16 bytes of 4-byte codes, 8 of
@@ -179,21 +176,19 @@ k_step2(const typename Codec<DT>::raw *__restrict__ src, typename Codec<DT>::raw
     auto brow = [&](int o) { return B + (o % S2_NB) * 9 * S2_PITCH; };
 
     // iteration t: inputs 2t, 2t+1 land; step t+1 at offsets 2t-1, 2t (valid
-    // 1 .. rows+2) on threads [0, S2_T1) and, at the same time, step t+2 at
-    // offsets 2t-4, 2t-3 (valid 2 .. rows+1), whose step t+1 rows 2t-5 ..
-    // 2t-2 were written before this iteration's barrier, on threads
-    // [S2_T1, S2_THREADS): one barrier per iteration
-    const int n_in = rows + 4, iters = rows / 2 + 3;
+    // 1 .. rows+2), step t+2 at offsets 2t-2, 2t-1 (valid 2 .. rows+1)
+    const int n_in = rows + 4, iters = n_in / 2;
     issue(0);
     issue(1);
     cp_async_commit();
     issue(2);
     issue(3);
     cp_async_commit();
-    const bool g1 = tid < S2_T1, c1 = tid < 2 * S2_NV1;
-    const int t2 = tid - S2_T1;
+    // step t+1: thread -> (row r1i, vector u1) of 2 x S2_NV1, columns Y0-4 .. Y0+W+3;
+    // step t+2: thread -> (row r2i, vector u2) of 2 x S2_NV, columns Y0 .. Y0+W-1
+    const bool c1 = tid < 2 * S2_NV1, c2 = tid < 2 * S2_NV;
     const int r1i = tid >= S2_NV1, u1 = tid - r1i * S2_NV1;
-    const int r2i = t2 >= S2_NV, u2 = t2 - r2i * S2_NV;
+    const int r2i = tid >= S2_NV, u2 = tid - r2i * S2_NV;
     int l1 = Y0 - 4 + 4 * u1;
     if (l1 < 0) l1 += ny;
     if (l1 >= ny) l1 -= ny;
@@ -201,30 +196,27 @@ k_step2(const typename Codec<DT>::raw *__restrict__ src, typename Codec<DT>::raw
     for (int t = 0; t < iters; ++t) {
         cp_async_wait<1>();  // this thread's copies of inputs 2t, 2t+1 have landed
         __syncthreads();     // ... everyone's; and the previous iteration is done
-        // the slots of inputs 2t+4, 2t+5 held inputs 2t-4, 2t-3, last read by
-        // step t+1 of the previous iteration
+        if (t >= 1 && c1) {
+            const int o = 2 * t - 1 + r1i;
+            raw out[9][4];
+            s2_vec<DT, BC>(arow(o - 1), arow(o), arow(o + 1), sc1, row_of(o), l1, nx, ny, omega, u0, out);
+            raw *b = brow(o);
+#pragma unroll
+            for (int ch = 0; ch < 9; ++ch) s2_st4(b + ch * S2_PITCH + sc1, out[ch]);
+        }
+        __syncthreads();
+        // the slots of inputs 2t+4, 2t+5 held inputs 2t-2, 2t-1, last read by
+        // step t+1 above; they land during step t+2 and the next iteration's wait
         if (2 * t + 4 < n_in) issue(2 * t + 4);
         if (2 * t + 5 < n_in) issue(2 * t + 5);
         cp_async_commit();
-        if (g1) {
-            const int o = 2 * t - 1 + r1i;
-            if (c1 && o >= 1 && o <= rows + 2) {
-                raw out[9][4];
-                s2_vec<DT, BC>(arow(o - 1), arow(o), arow(o + 1), sc1, row_of(o), l1, nx, ny, omega, u0, out);
-                raw *b = brow(o);
+        if (t >= 2 && c2) {
+            const int o = 2 * t - 2 + r2i, k = row_of(o);
+            raw out[9][4];
+            s2_vec<DT, BC>(brow(o - 1), brow(o), brow(o + 1), sc2, k, l2, nx, ny, omega, u0, out);
+            raw *d = dst + (size_t)k * ny + l2;
 #pragma unroll
-                for (int ch = 0; ch < 9; ++ch) s2_st4(b + ch * S2_PITCH + sc1, out[ch]);
-            }
-        } else {
-            const int o = 2 * t - 4 + r2i;
-            if (o >= 2 && o <= rows + 1) {
-                const int k = row_of(o);
-                raw out[9][4];
-                s2_vec<DT, BC>(brow(o - 1), brow(o), brow(o + 1), sc2, k, l2, nx, ny, omega, u0, out);
-                raw *d = dst + (size_t)k * ny + l2;
-#pragma unroll
-                for (int ch = 0; ch < 9; ++ch) s2_st4(d + ch * cs, out[ch]);
-            }
+            for (int ch = 0; ch < 9; ++ch) s2_st4(d + ch * cs, out[ch]);
         }
     }
 }
