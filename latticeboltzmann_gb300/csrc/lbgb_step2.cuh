@@ -66,25 +66,11 @@ __device__ __forceinline__ void s2_st4(unsigned short *p, const unsigned short (
 // rows of the source step at rows k-1, k, k+1 (channel-major, S2_PITCH
 // apart); sc: the shared column of the first cell; k, l0: its lattice row
 // and column (l0 a multiple of 4).
-// A code moved between lanes of a warp (4-byte codes as their bits).
-__device__ __forceinline__ float s2_shfl_up(unsigned m, float x) { return __shfl_up_sync(m, x, 1); }
-__device__ __forceinline__ float s2_shfl_down(unsigned m, float x) { return __shfl_down_sync(m, x, 1); }
-__device__ __forceinline__ unsigned short s2_shfl_up(unsigned m, unsigned short x) {
-    return (unsigned short)__shfl_up_sync(m, (unsigned)x, 1);
-}
-__device__ __forceinline__ unsigned short s2_shfl_down(unsigned m, unsigned short x) {
-    return (unsigned short)__shfl_down_sync(m, (unsigned)x, 1);
-}
-
-// has_prev / has_next: the lanes before / after this one hold the previous /
-// next vector of the same row (their shared-row values are taken by shuffle
-// instead of a bank-conflicting scalar load).  m: the lanes of the warp that
-// call this together (the shuffles).
 template <int DT, int BC>
 __device__ __forceinline__ void s2_vec(const typename Codec<DT>::raw *r0, const typename Codec<DT>::raw *r1,
                                        const typename Codec<DT>::raw *r2, int sc, int k, int l0, int nx, int ny,
-                                       typename Codec<DT>::real omega, typename Codec<DT>::real u0, unsigned m,
-                                       bool has_prev, bool has_next, typename Codec<DT>::raw (&out)[9][4]) {
+                                       typename Codec<DT>::real omega, typename Codec<DT>::real u0,
+                                       typename Codec<DT>::raw (&out)[9][4]) {
     using C = Codec<DT>;
     using raw = typename C::raw;
     using real = typename C::real;
@@ -101,19 +87,15 @@ __device__ __forceinline__ void s2_vec(const typename Codec<DT>::raw *r0, const 
         raw q[4];
         s2_ld4(rp + ch * S2_PITCH + sc, q);
         if (cy(ch) > 0) {
-            raw e = s2_shfl_up(m, q[3]);
-            if (!has_prev) e = rp[ch * S2_PITCH + sc - 1];
-            v[ch][0] = C::dec(e, ch);
+            v[ch][0] = C::dec(rp[ch * S2_PITCH + sc - 1], ch);
             v[ch][1] = C::dec(q[0], ch);
             v[ch][2] = C::dec(q[1], ch);
             v[ch][3] = C::dec(q[2], ch);
         } else if (cy(ch) < 0) {
-            raw e = s2_shfl_down(m, q[0]);
-            if (!has_next) e = rp[ch * S2_PITCH + sc + 4];
             v[ch][0] = C::dec(q[1], ch);
             v[ch][1] = C::dec(q[2], ch);
             v[ch][2] = C::dec(q[3], ch);
-            v[ch][3] = C::dec(e, ch);
+            v[ch][3] = C::dec(rp[ch * S2_PITCH + sc + 4], ch);
         } else {
 #pragma unroll
             for (int j = 0; j < 4; ++j) v[ch][j] = C::dec(q[j], ch);
@@ -211,20 +193,13 @@ k_step2(const typename Codec<DT>::raw *__restrict__ src, typename Codec<DT>::raw
     if (l1 < 0) l1 += ny;
     if (l1 >= ny) l1 -= ny;
     const int sc1 = 4 + 4 * u1, l2 = Y0 + 4 * u2, sc2 = 8 + 4 * u2;
-    // neighbouring vectors of the same row in the neighbouring lanes
-    const int lane = tid & 31;
-    const bool prev1 = lane > 0 && u1 > 0, next1 = lane < 31 && u1 < S2_NV1 - 1;
-    const bool prev2 = lane > 0 && u2 > 0, next2 = lane < 31 && u2 < S2_NV - 1;
-    // the lanes of this warp that compute each step (all lanes vote here)
-    const unsigned m1 = __ballot_sync(0xffffffffu, c1), m2 = __ballot_sync(0xffffffffu, c2);
     for (int t = 0; t < iters; ++t) {
         cp_async_wait<1>();  // this thread's copies of inputs 2t, 2t+1 have landed
         __syncthreads();     // ... everyone's; and the previous iteration is done
         if (t >= 1 && c1) {
             const int o = 2 * t - 1 + r1i;
             raw out[9][4];
-            s2_vec<DT, BC>(arow(o - 1), arow(o), arow(o + 1), sc1, row_of(o), l1, nx, ny, omega, u0, m1, prev1,
-                           next1, out);
+            s2_vec<DT, BC>(arow(o - 1), arow(o), arow(o + 1), sc1, row_of(o), l1, nx, ny, omega, u0, out);
             raw *b = brow(o);
 #pragma unroll
             for (int ch = 0; ch < 9; ++ch) s2_st4(b + ch * S2_PITCH + sc1, out[ch]);
@@ -238,8 +213,7 @@ k_step2(const typename Codec<DT>::raw *__restrict__ src, typename Codec<DT>::raw
         if (t >= 2 && c2) {
             const int o = 2 * t - 2 + r2i, k = row_of(o);
             raw out[9][4];
-            s2_vec<DT, BC>(brow(o - 1), brow(o), brow(o + 1), sc2, k, l2, nx, ny, omega, u0, m2, prev2, next2,
-                           out);
+            s2_vec<DT, BC>(brow(o - 1), brow(o), brow(o + 1), sc2, k, l2, nx, ny, omega, u0, out);
             raw *d = dst + (size_t)k * ny + l2;
 #pragma unroll
             for (int ch = 0; ch < 9; ++ch) s2_st4(d + ch * cs, out[ch]);
